@@ -1,0 +1,255 @@
+/*
+ * svo_gb300.h -- C ABI of the GB300-native sparse-voxel-octree raycast and
+ * image-warp pipeline (libsvo_gb300.so).
+ *
+ * This ABI replaces the reference's OpenCL wrapper src/ocl.h and the buffer
+ * plumbing of its frame driver src/raycast.h (sp4cerat/Sparse-Voxel-Octree-
+ * Raycasting). Every entry point names the reference interface it stands in
+ * for. Conventions, as in the reference: one context drives one device through
+ * one in-order stream and is not re-entrant; the caller owns host memory.
+ * Unlike the reference (which stops the process through error_stop on any
+ * failure, src/ocl.h:29-41), every call returns an svo_status.
+ *
+ * Octree words keep the reference's compact node format (src/octree/octree.h:
+ * 95-293, kernel/kernel.cl:32-112): (offset<<9)|(isBlock<<8)|childmask8, ten-
+ * word normal nodes for the top depth-6 levels and 64-word-aligned byte-packed
+ * blocks for the last six.
+ */
+#ifndef SVO_GB300_H
+#define SVO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum svo_status {
+    SVO_OK = 0,
+    SVO_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad size or resolution */
+    SVO_ERR_CUDA = 2,             /* a CUDA runtime call failed (see svo_last_error) */
+    SVO_ERR_NO_OCTREE = 3,        /* raycast before svo_octree_upload */
+    SVO_ERR_BAD_OCTREE = 4,       /* upload validation found an out-of-range node word */
+    SVO_ERR_DEVICE_FAULT = 5,     /* a kernel flagged an out-of-range fetch or hit its step limit */
+    SVO_ERR_OUT_OF_MEMORY = 6,
+    SVO_ERR_CAPACITY = 7,         /* more voxels/nodes than the compact format addresses */
+    SVO_ERR_NOT_SUPPORTED = 8,
+    SVO_ERR_IO = 9
+} svo_status;
+
+/* Empty pixel marker of the colour planes (src/raycast.h:153,157). */
+#define SVO_EMPTY_PIXEL 0xffffff00u
+/* Pre-sized compact array length of octree_init (src/raycast.h:38). */
+#define SVO_DEFAULT_INITIAL_WORDS 2097152u
+#define SVO_MIN_DEPTH 8
+#define SVO_MAX_DEPTH 12
+
+/*
+ * One camera. pos is v0 of src/raycast.h:159 in world units (the kernels
+ * trace from pos*16). m is the row-major 4x4 view matrix m of
+ * src/raycast.h:121-128 (m[r*4+c]); its rows are the vx/vy/vz handed to
+ * raycast_proj (src/raycast.h:160-162) and its columns the mx/my/mz handed to
+ * raycast_holes/raycast_fine_2 (src/raycast.h:322-325). fovx/fovy are the
+ * kernels' fov arguments (kernel/kernel.cl:640-641; the reference passes 1.0).
+ */
+typedef struct svo_view {
+    float pos[4];
+    float m[16];
+    float fovx;
+    float fovy;
+    int32_t res_x;
+    int32_t res_y;
+} svo_view;
+
+typedef struct svo_context svo_context;
+typedef struct svo_target svo_target;
+typedef struct svo_builder svo_builder;
+
+/* ----------------------------------------------------------- context -- */
+
+/* Replaces ocl_init (src/ocl.h:57-146) and the device half of raycast_init
+ * (src/raycast.h:61-91). Creates a stream on `device`. */
+svo_status svo_context_create(int device, svo_context** out);
+/* Replaces raycast_exit (src/raycast.h:511-517) and ocl_exit (src/ocl.h:168-174). */
+svo_status svo_context_destroy(svo_context* ctx);
+/* Human-readable text of the last failure on this context (never null). */
+const char* svo_last_error(const svo_context* ctx);
+/* The cudaStream_t all work of this context is ordered on. */
+void* svo_context_stream(svo_context* ctx);
+/* Replaces ocl_end_all_kernels' wait (src/ocl.h:253-265): blocks until the
+ * stream drains and reports device-side fault flags (SVO_ERR_DEVICE_FAULT). */
+svo_status svo_synchronize(svo_context* ctx);
+/* Number of kernels this context has launched since creation. */
+uint64_t svo_launch_count(const svo_context* ctx);
+
+/* ------------------------------------------------------------ octree -- */
+
+/* Replaces ocl_malloc(size, &octree_array_compact[0]) of src/raycast.h:68
+ * together with the octree_root_normal global (src/octree/octree.h:25).
+ * Validates every node word reachable from root_word against n_words
+ * (SVO_ERR_BAD_OCTREE) unless validate == 0, then copies the words to the
+ * device. depth is OCTREE_DEPTH (kernel/kernel.cl:12), SVO_MIN_DEPTH..SVO_MAX_DEPTH. */
+svo_status svo_octree_upload(svo_context* ctx, const uint32_t* words, size_t n_words, uint32_t root_word,
+                             int depth, int validate);
+/* Flat variant: adopts words already resident on this context's device
+ * (nothing is copied; the caller keeps the allocation alive until the next
+ * upload or destroy). No validation. */
+svo_status svo_octree_upload_device(svo_context* ctx, const uint32_t* d_words, size_t n_words, uint32_t root_word,
+                                    int depth);
+/* Size in bytes of the octree's upper (normal-node) region that the traversal
+ * keeps in an L2 persisting window; 0 disables the window. */
+svo_status svo_octree_set_l2_window(svo_context* ctx, size_t bytes);
+
+/* ------------------------------------------------------- render target -- */
+
+/* A render target holds one camera stream's planes: the cache and current
+ * colour/coordinate planes of the warp pipeline (mem_screenbuffer and
+ * mem_backbuffer, src/raycast.h:82,85), the hole id buffer (:268-270), the
+ * displayed colour plane and the BGRX8 image that replaces the PBO
+ * (mem_screenbuffer_tex, :88-89). res_x, res_y <= 65535. */
+svo_status svo_target_create(svo_context* ctx, int res_x, int res_y, svo_target** out);
+svo_status svo_target_destroy(svo_target* t);
+
+/* ----------------------------------------------------------- frames ---- */
+
+/* Plain full raycast: raycast_fine_2 (kernel/kernel.cl:846-942) over every
+ * pixel, then raycast_colorize (:944-974). Writes the target's "full" planes:
+ * colour word 0xff000000+colour, float4 (hit xyz in world units, hit
+ * distance in world units), packed hit voxel (svo_read_voxels) and BGRX8.
+ * Asynchronous on the context stream. */
+svo_status svo_raycast_full(svo_context* ctx, svo_target* t, const svo_view* view);
+
+/* Batched full raycast: n views of any resolution (each into its own target)
+ * traced by one persistent launch fed by a global work queue. */
+svo_status svo_raycast_full_batch(svo_context* ctx, svo_target* const* targets, const svo_view* views, int n);
+
+/* One warped frame: the body of raycast_draw (src/raycast.h:147-441) without
+ * the GL blit. frame is the reference's static frame counter (:104): frames
+ * 0 and 1 start from cleared caches, frame selects the 8x4 refresh tile.
+ * The view must use fovx = fovy = 1 (raycast_proj has no fov term,
+ * kernel/kernel.cl:552-553). No host synchronisation inside (the hole count
+ * stays on the device). Asynchronous on the context stream. */
+svo_status svo_warp_frame(svo_context* ctx, svo_target* t, const svo_view* view, int frame);
+
+/* Capture the warp frame of this target as a CUDA graph on first use and
+ * replay it on later calls (per-frame parameters travel through one small
+ * host-to-device copy inside the graph). enable = 0 returns to direct launches. */
+svo_status svo_target_use_graph(svo_target* t, int enable);
+
+/* Per-stage CUDA-event timing of the next frames on this target (replaces
+ * the timeGetTime stage array of src/raycast.h:164-166,475-492). */
+svo_status svo_target_set_profiling(svo_target* t, int enable);
+/* Milliseconds of each stage of the last profiled frame. Warp frames fill
+ * [0] project, [1] resolve+gather, [2] scan, [3] hole list, [4] trace,
+ * [5] filter+colourise; full raycasts fill [4] trace and [5] colourise.
+ * Synchronises the stream. Returns the number of stages written. */
+int svo_target_stage_times(svo_target* t, float* ms, int cap);
+
+/* -------------------------------------------------------- readbacks ---- */
+/* All readbacks synchronise the context stream and copy into host memory of
+ * res_x*res_y elements (4 floats per pixel for coordinates). */
+
+/* Warp planes. plane 0: displayed colour words after raycast_fillhole2
+ * (reference plane 0 at the end of raycast_draw); plane 2: the cache plane
+ * (colour words before the filter, the memcpy target of :394-405);
+ * plane 1: the reference's never-written second cache (all SVO_EMPTY_PIXEL). */
+svo_status svo_read_colour(svo_target* t, int plane, uint32_t* host);
+/* Coordinate (back) buffer of the cache plane: x,y,z world hit position; w is
+ * the view-space depth for reprojected pixels and the ray distance for
+ * traced pixels. Only pixels whose colour is not SVO_EMPTY_PIXEL are defined. */
+svo_status svo_read_coords(svo_target* t, int plane, float* host);
+/* The hole id buffer of the last warp frame in the reference's layout
+ * (kernel/kernel.cl:276-340): [0] total entries, [tiles..2*tiles) exclusive
+ * offsets, [2*tiles..) packed x|y<<16 entries. *count receives the total. */
+svo_status svo_read_holes(svo_target* t, uint32_t* host, size_t cap_words, uint32_t* count);
+/* The BGRX8 image of the last frame (warped or full). */
+svo_status svo_read_bgrx(svo_target* t, uint32_t* host);
+/* Outputs of the last svo_raycast_full on this target. */
+svo_status svo_read_full(svo_target* t, uint32_t* colour, float* xyzw);
+/* Packed hit voxel of the last full raycast: bits 0-15 x, 16-31 y, 32-47 z
+ * (voxel coordinates of the hit cell's low corner), 48-55 hit level
+ * (1 = leaf), bit 63 set for a hit; 0 for rays that left the volume. */
+svo_status svo_read_voxels(svo_target* t, uint64_t* host);
+
+/* Device pointers of the target's outputs, for zero-copy consumers. */
+typedef struct svo_device_outputs {
+    uint32_t* bgrx;        /* res_x*res_y BGRX8 */
+    uint32_t* colour;      /* displayed colour words (warp) */
+    uint32_t* full_colour; /* full raycast colour words */
+    float* full_xyzw;      /* full raycast float4 */
+    uint64_t* full_voxel;  /* full raycast packed hit voxels */
+} svo_device_outputs;
+svo_status svo_target_device_outputs(svo_target* t, svo_device_outputs* out);
+
+/* ------------------------------------------------- host octree builder -- */
+/* Replaces set_voxel / convert_tree_blocks (src/octree/octree.h:32-89,
+ * 232-293) and octree_init (src/raycast.h:13-46). Produces the same compact
+ * words as the reference for the same voxels in the same insertion order:
+ * a node takes the colour of the first voxel inserted through it, a leaf the
+ * colour of the last insertion of that voxel. */
+svo_status svo_builder_create(int depth, svo_builder** out);
+svo_status svo_builder_destroy(svo_builder* b);
+/* set_voxel(x,y,z,uchar4): rgba is the uchar4 colour read as a little-endian
+ * word; only its low byte survives at leaf level (octree.h:117-135) and it
+ * must be non-zero. */
+svo_status svo_builder_set_voxel(svo_builder* b, uint32_t x, uint32_t y, uint32_t z, uint32_t rgba);
+svo_status svo_builder_set_voxels(svo_builder* b, const uint32_t* x, const uint32_t* y, const uint32_t* z,
+                                  const uint32_t* rgba, size_t n);
+/* convert_tree_blocks(octree_root) after octree_array_compact.resize(initial_words)
+ * (initial_words 0 means SVO_DEFAULT_INITIAL_WORDS). */
+svo_status svo_builder_finish(svo_builder* b, size_t initial_words, uint32_t* root_word, size_t* n_words);
+/* Copies the finished words (n_words of svo_builder_finish). */
+svo_status svo_builder_copy_words(const svo_builder* b, uint32_t* out);
+/* Voxel count (num_voxels, octree.h:27) and pointer-node count of the built tree. */
+svo_status svo_builder_stats(const svo_builder* b, uint64_t* voxels, uint64_t* nodes);
+
+/* Flat octree file: magic, depth, root word, word count, words. Lets deep
+ * scenes be built once (the reference rebuilds from .rle4 every start). */
+svo_status svo_octree_save(const char* path, const uint32_t* words, size_t n_words, uint32_t root_word, int depth);
+svo_status svo_octree_load_header(const char* path, size_t* n_words, uint32_t* root_word, int* depth);
+svo_status svo_octree_load_words(const char* path, uint32_t* words, size_t n_words);
+
+/* --------------------------------------------------- synthetic scenes -- */
+/* Seeded value-noise fBm terrain (6 octaves, lacunarity 2, gain 0.5,
+ * amplitude 0.3*extent, base 0.35*extent). shell = 0 inserts every voxel
+ * below the surface; shell = 1 only those down to the lowest 4-neighbour
+ * surface (the first hit of any ray from above is unchanged). Columns are
+ * inserted z-major, x-minor, top voxel first. Colour byte: 2-bit material
+ * from the height band | ramp intensity +-8 noise, never 0. */
+typedef struct svo_terrain_spec {
+    uint32_t seed;
+    int32_t depth;
+    int32_t shell;
+    int32_t boxes;      /* seeded axis-aligned solid boxes added after the terrain (0 = none) */
+} svo_terrain_spec;
+/* Inserts the terrain into a builder. */
+svo_status svo_terrain_build(svo_builder* b, const svo_terrain_spec* spec);
+/* Writes the terrain's voxels in insertion order (null arrays: count only). */
+svo_status svo_terrain_voxels(const svo_terrain_spec* spec, uint32_t* x, uint32_t* y, uint32_t* z, uint32_t* rgba,
+                              size_t cap, size_t* n);
+
+/* ------------------------------------------------------------ cameras -- */
+/* m = identity.rotate_z(rz).rotate_x(rx).rotate_y(ry), src/raycast.h:121-124. */
+svo_status svo_view_from_euler(float rx, float ry, float rz, const float pos[3], int res_x, int res_y, float fov,
+                               svo_view* out);
+/* Camera at `pos` looking at `target` (rx/ry chosen so that row 2 of m points
+ * at the target, rz = 0). */
+svo_status svo_view_look_at(const float pos[3], const float target[3], int res_x, int res_y, float fov,
+                            svo_view* out);
+/* Wraps pos*16 into [0, 2^(depth+1)) on every axis (src/raycast.h:136-145). */
+svo_status svo_wrap_position(float pos[3], int depth);
+/* Seeded camera paths over the synthetic terrain.
+ * kind 0: still camera at 1.5*extent from the centre, 20 degrees above it,
+ *         looking at the centre;
+ * kind 1: orbit at radius 1.5*extent, 0.5 degrees yaw per frame, height
+ *         sinusoid 0.02*extent over 64 frames, looking at the centre;
+ * kind 2: fast motion, 2 degrees yaw and 0.05*extent translation per frame;
+ * kind 3: seeded random pose (frame is the view index). */
+svo_status svo_camera_path(int kind, int depth, int frame, uint32_t seed, int res_x, int res_y, float fov,
+                           svo_view* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SVO_GB300_H */

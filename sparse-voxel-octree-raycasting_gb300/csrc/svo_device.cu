@@ -1,0 +1,745 @@
+// svo_device.cu -- device runtime of libsvo_gb300.so: context, octree upload,
+// render targets, the per-frame launch sequence and its C ABI.
+//
+// Replaces the reference's OpenCL wrapper (src/ocl.h) and the device half of
+// its frame driver (src/raycast.h). One context = one device, one in-order
+// stream (the reference's single command queue, src/ocl.h:140). Frames never
+// synchronise the host: the hole count that raycast_draw reads back with a
+// blocking 4-byte copy (src/raycast.h:298) stays on the device and sizes the
+// persistent trace launch's work queue.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/svo_gb300.h"
+#include "svo_kernels.cuh"
+
+using namespace svo;
+
+struct svo_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int sm_count = 0;
+    uint32_t* d_octree = nullptr;
+    bool owns_octree = false;
+    size_t n_words = 0;
+    uint32_t root = 0;
+    int depth = 0;
+    uint32_t* d_fault = nullptr;  // device fault flags (kFault*)
+    // Batch tables of full raycasts: a ring of pinned staging copies so a call
+    // never waits for the GPU unless it laps the ring.
+    static constexpr int kRing = 4;
+    FullBatch* d_batch[kRing] = {};
+    FullBatch* h_batch[kRing] = {};
+    cudaEvent_t batch_done[kRing] = {};
+    int batch_slot = 0;
+    uint32_t* d_counter = nullptr;
+    size_t l2_window = 0;
+    uint64_t launches = 0;
+    std::string err;
+};
+
+struct svo_target {
+    svo_context* ctx = nullptr;
+    int res_x = 0, res_y = 0;
+    size_t N = 0, tiles = 0;
+    TargetBuffers B{};
+    FrameParams* d_params = nullptr;
+    uint32_t* full_col = nullptr;
+    float4* full_xyzw = nullptr;
+    uint64_t* full_vox = nullptr;
+    uint64_t frames = 0;      // warp frames issued (parity of the current plane)
+    int last_cur = 0;
+    bool have_prev = false;
+    // CUDA graph of one warp frame
+    bool use_graph = false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    cudaGraphNode_t params_node = nullptr;
+    bool graph_profiled = false;
+    // per-stage timing
+    bool profiling = false;
+    cudaEvent_t ev[8] = {};
+    int n_events = 0;
+    int last_mode = 0;  // 1 warp, 2 full
+};
+
+namespace {
+
+const char* status_text(svo_status s) {
+    switch (s) {
+        case SVO_OK: return "ok";
+        case SVO_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case SVO_ERR_CUDA: return "CUDA error";
+        case SVO_ERR_NO_OCTREE: return "no octree uploaded";
+        case SVO_ERR_BAD_OCTREE: return "octree validation failed";
+        case SVO_ERR_DEVICE_FAULT: return "device fault flag set";
+        case SVO_ERR_OUT_OF_MEMORY: return "out of memory";
+        case SVO_ERR_CAPACITY: return "capacity exceeded";
+        case SVO_ERR_NOT_SUPPORTED: return "not supported";
+        case SVO_ERR_IO: return "I/O error";
+    }
+    return "unknown";
+}
+
+svo_status fail(svo_context* ctx, svo_status s, const std::string& what) {
+    if (ctx) ctx->err = std::string(status_text(s)) + ": " + what;
+    return s;
+}
+
+#define SVO_CUDA(ctx, call)                                                                   \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess) {                                                              \
+            return fail((ctx), e_ == cudaErrorMemoryAllocation ? SVO_ERR_OUT_OF_MEMORY : SVO_ERR_CUDA, \
+                        std::string(#call) + " -> " + cudaGetErrorString(e_));                \
+        }                                                                                     \
+    } while (0)
+
+#define SVO_LAUNCHED(ctx)                                                                     \
+    do {                                                                                      \
+        cudaError_t e_ = cudaGetLastError();                                                  \
+        if (e_ != cudaSuccess) return fail((ctx), SVO_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e_)); \
+        ++(ctx)->launches;                                                                    \
+    } while (0)
+
+RayCam make_raycam(const svo_view& v) {
+    // Rows of m^T = columns of m (src/raycast.h:225-228).
+    const float* m = v.m;
+    RayCam c;
+    c.px = v.pos[0];
+    c.py = v.pos[1];
+    c.pz = v.pos[2];
+    c.mxx = m[0];
+    c.mxy = m[4];
+    c.mxz = m[8];
+    c.myx = m[1];
+    c.myy = m[5];
+    c.myz = m[9];
+    c.mzx = m[2];
+    c.mzy = m[6];
+    c.mzz = m[10];
+    c.fovx = v.fovx;
+    c.fovy = v.fovy;
+    return c;
+}
+
+// Host walk of the compact octree in the builder's layout (normal nodes above
+// height 6, blocks below). Checks every address the traversal can form.
+struct Validator {
+    const uint32_t* w;
+    size_t n;
+    int depth;
+    size_t visits = 0, limit;
+    std::string why;
+
+    bool fail_at(const char* what, size_t at) {
+        char buf[128];
+        std::snprintf(buf, sizeof(buf), "%s at word %zu", what, at);
+        why = buf;
+        return false;
+    }
+    bool block(size_t local_root, uint32_t word, int h, bool is_root) {
+        if (++visits > limit) return fail_at("node visited twice (not a tree)", 0);
+        if (!(word & 256u)) return fail_at("block node without block flag", local_root);
+        const size_t pos = is_root ? local_root : local_root + (word >> 9);
+        const uint32_t mask = word & 0xffu;
+        const uint32_t kids = __builtin_popcount(mask);
+        if (h == 2) {
+            const size_t head = 1 + kids;
+            if (pos + (head + 3) / 4 > n) return fail_at("byte record past the end", pos);
+            size_t bytes = head;
+            for (uint32_t k = 0; k < kids; ++k) {
+                const size_t b = 1 + k;
+                bytes += __builtin_popcount((w[pos + b / 4] >> (8 * (b & 3))) & 0xffu);
+            }
+            if (pos + (bytes + 3) / 4 > n) return fail_at("byte record past the end", pos);
+            return true;
+        }
+        if (pos + 1 + kids > n) return fail_at("block node past the end", pos);
+        for (uint32_t k = 0; k < kids; ++k)
+            if (!block(local_root, w[pos + 1 + k], h - 1, false)) return false;
+        return true;
+    }
+    bool normal(uint32_t word, int h) {
+        if (++visits > limit) return fail_at("node visited twice (not a tree)", 0);
+        if (word & 256u) return fail_at("normal node with block flag", word >> 9);
+        const size_t at = word >> 9;
+        if (at + 10 > n) return fail_at("normal node past the end", at);
+        for (int j = 0; j < 8; ++j) {
+            if (!((word >> j) & 1u)) continue;
+            const uint32_t cw = w[at + j];
+            if (h - 1 >= 7) {
+                if (!normal(cw, h - 1)) return false;
+            } else {
+                const size_t lr = (size_t)(cw >> 9) << 6;
+                if (!block(lr, cw, h - 1, true)) return false;
+            }
+        }
+        return true;
+    }
+};
+
+template <int DEPTH>
+const void* trace_full_fn(bool vox) {
+    return vox ? (const void*)k_trace_full<DEPTH, true> : (const void*)k_trace_full<DEPTH, false>;
+}
+
+svo_status launch_trace_full(svo_context* ctx, FullBatch* d_batch, bool vox) {
+    Octree o{ctx->d_octree, (uint32_t)ctx->n_words, ctx->root};
+    const void* fn = nullptr;
+    switch (ctx->depth) {
+        case 8: fn = trace_full_fn<8>(vox); break;
+        case 9: fn = trace_full_fn<9>(vox); break;
+        case 10: fn = trace_full_fn<10>(vox); break;
+        case 11: fn = trace_full_fn<11>(vox); break;
+        case 12: fn = trace_full_fn<12>(vox); break;
+        default: return fail(ctx, SVO_ERR_NOT_SUPPORTED, "octree depth");
+    }
+    int per_sm = 0;
+    SVO_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kTraceBlock, 0));
+    const int grid = std::max(1, per_sm) * ctx->sm_count;
+    void* args[] = {&o, &d_batch, &ctx->d_counter, &ctx->d_fault};
+    SVO_CUDA(ctx, cudaLaunchKernel(fn, dim3(grid), dim3(kTraceBlock), args, 0, ctx->stream));
+    ++ctx->launches;
+    return SVO_OK;
+}
+
+template <int DEPTH>
+const void* trace_warp_fn() {
+    return (const void*)k_trace_warp<DEPTH>;
+}
+
+svo_status launch_trace_warp(svo_context* ctx, svo_target* t) {
+    Octree o{ctx->d_octree, (uint32_t)ctx->n_words, ctx->root};
+    const void* fn = nullptr;
+    switch (ctx->depth) {
+        case 8: fn = trace_warp_fn<8>(); break;
+        case 9: fn = trace_warp_fn<9>(); break;
+        case 10: fn = trace_warp_fn<10>(); break;
+        case 11: fn = trace_warp_fn<11>(); break;
+        case 12: fn = trace_warp_fn<12>(); break;
+        default: return fail(ctx, SVO_ERR_NOT_SUPPORTED, "octree depth");
+    }
+    int per_sm = 0;
+    SVO_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kTraceBlock, 0));
+    const int grid = std::max(1, per_sm) * ctx->sm_count;
+    void* args[] = {&o, &t->d_params, &t->B, &ctx->d_fault};
+    SVO_CUDA(ctx, cudaLaunchKernel(fn, dim3(grid), dim3(kTraceBlock), args, 0, ctx->stream));
+    ++ctx->launches;
+    return SVO_OK;
+}
+
+void record(svo_target* t, int i) {
+    if (t->profiling) cudaEventRecord(t->ev[i], t->ctx->stream);
+}
+
+FrameParams make_params(const svo_target* t, const svo_view& v, int frame, int cur, bool have_cache) {
+    FrameParams p{};
+    p.ray = make_raycam(v);
+    for (int i = 0; i < 3; ++i) {
+        p.vx[i] = v.m[0 + i];
+        p.vy[i] = v.m[4 + i];
+        p.vz[i] = v.m[8 + i];
+    }
+    p.frame = frame;
+    p.cur = cur;
+    p.have_cache = have_cache ? 1 : 0;
+    // raycast.h:363-366: tile (frame&7, (frame>>3)&3) of an 8x4 grid; the
+    // NDRange of res/8 x res/4 work-items is rounded up to 16 (ocl.h:234-235).
+    const int rx = t->res_x, ry = t->res_y;
+    p.add_x = (rx / 8) * (frame & 7);
+    p.add_y = (ry / 4) * ((frame >> 3) & 3);
+    const int gx = (rx / 8 + 15) / 16 * 16, gy = (ry / 4 + 15) / 16 * 16;
+    p.x_end = std::min(rx, p.add_x + gx);
+    p.y_end = std::min(ry, p.add_y + gy);
+    return p;
+}
+
+// The launch sequence of one warp frame after k_set_params.
+svo_status enqueue_warp_body(svo_context* ctx, svo_target* t) {
+    cudaStream_t s = ctx->stream;
+    const int res_x = t->res_x, res_y = t->res_y;
+    record(t, 0);
+    {
+        const int threads = 256;
+        int blocks = (int)std::min<size_t>((t->N + threads - 1) / threads, (size_t)ctx->sm_count * 8);
+        k_project<<<blocks, threads, 0, s>>>(t->d_params, t->B);
+        SVO_LAUNCHED(ctx);
+    }
+    record(t, 1);
+    k_resolve_gather<<<dim3((res_x + 15) / 16, (res_y + 15) / 16), 256, 0, s>>>(t->d_params, t->B);
+    SVO_LAUNCHED(ctx);
+    record(t, 2);
+    k_hole_scan<<<1, 1024, 0, s>>>(t->B);
+    SVO_LAUNCHED(ctx);
+    record(t, 3);
+    if (t->tiles > 0) {
+        k_hole_write<<<(unsigned)((t->tiles + 7) / 8), 256, 0, s>>>(t->B);
+        SVO_LAUNCHED(ctx);
+    }
+    record(t, 4);
+    svo_status st = launch_trace_warp(ctx, t);
+    if (st != SVO_OK) return st;
+    record(t, 5);
+    k_fill_colorize<<<dim3((res_x + 31) / 32, (res_y + 7) / 8), 256, 0, s>>>(t->d_params, t->B);
+    SVO_LAUNCHED(ctx);
+    record(t, 6);
+    return SVO_OK;
+}
+
+svo_status alloc(svo_context* ctx, void** p, size_t bytes) {
+    SVO_CUDA(ctx, cudaMalloc(p, bytes));
+    return SVO_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+svo_status svo_context_create(int device, svo_context** out) {
+    if (!out) return SVO_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return SVO_ERR_CUDA;
+    if (device < 0 || device >= n) return SVO_ERR_INVALID_ARGUMENT;
+    auto* ctx = new svo_context;
+    ctx->device = device;
+    auto cleanup = [&](svo_status s) {
+        svo_context_destroy(ctx);
+        return s;
+    };
+    if (cudaSetDevice(device) != cudaSuccess) return cleanup(SVO_ERR_CUDA);
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return cleanup(SVO_ERR_CUDA);
+    if (cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+        return cleanup(SVO_ERR_CUDA);
+    if (cudaMalloc(&ctx->d_fault, sizeof(uint32_t)) != cudaSuccess) return cleanup(SVO_ERR_OUT_OF_MEMORY);
+    if (cudaMalloc(&ctx->d_counter, sizeof(uint32_t)) != cudaSuccess) return cleanup(SVO_ERR_OUT_OF_MEMORY);
+    for (int i = 0; i < svo_context::kRing; ++i) {
+        if (cudaMalloc(&ctx->d_batch[i], sizeof(FullBatch)) != cudaSuccess) return cleanup(SVO_ERR_OUT_OF_MEMORY);
+        if (cudaMallocHost(&ctx->h_batch[i], sizeof(FullBatch)) != cudaSuccess) return cleanup(SVO_ERR_OUT_OF_MEMORY);
+        if (cudaEventCreateWithFlags(&ctx->batch_done[i], cudaEventDisableTiming) != cudaSuccess)
+            return cleanup(SVO_ERR_CUDA);
+    }
+    if (cudaMemsetAsync(ctx->d_fault, 0, sizeof(uint32_t), ctx->stream) != cudaSuccess) return cleanup(SVO_ERR_CUDA);
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return cleanup(SVO_ERR_CUDA);
+    *out = ctx;
+    return SVO_OK;
+}
+
+svo_status svo_context_destroy(svo_context* ctx) {
+    if (!ctx) return SVO_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->owns_octree && ctx->d_octree) cudaFree(ctx->d_octree);
+    if (ctx->d_fault) cudaFree(ctx->d_fault);
+    if (ctx->d_counter) cudaFree(ctx->d_counter);
+    for (int i = 0; i < svo_context::kRing; ++i) {
+        if (ctx->d_batch[i]) cudaFree(ctx->d_batch[i]);
+        if (ctx->h_batch[i]) cudaFreeHost(ctx->h_batch[i]);
+        if (ctx->batch_done[i]) cudaEventDestroy(ctx->batch_done[i]);
+    }
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return SVO_OK;
+}
+
+const char* svo_last_error(const svo_context* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+void* svo_context_stream(svo_context* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+uint64_t svo_launch_count(const svo_context* ctx) { return ctx ? ctx->launches : 0; }
+
+svo_status svo_synchronize(svo_context* ctx) {
+    if (!ctx) return SVO_ERR_INVALID_ARGUMENT;
+    SVO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    uint32_t f = 0;
+    SVO_CUDA(ctx, cudaMemcpy(&f, ctx->d_fault, sizeof(f), cudaMemcpyDeviceToHost));
+    if (f) {
+        SVO_CUDA(ctx, cudaMemset(ctx->d_fault, 0, sizeof(uint32_t)));
+        char buf[160];
+        std::snprintf(buf, sizeof(buf), "fault flags 0x%x (1: node fetch out of range, 2: ray step limit, "
+                      "4: hole entry outside the frame)", f);
+        return fail(ctx, SVO_ERR_DEVICE_FAULT, buf);
+    }
+    return SVO_OK;
+}
+
+svo_status svo_octree_upload(svo_context* ctx, const uint32_t* words, size_t n_words, uint32_t root_word, int depth,
+                             int validate) {
+    if (!ctx || !words || n_words < 10 || n_words >= 0xffffffc0ull) return SVO_ERR_INVALID_ARGUMENT;
+    if (depth < SVO_MIN_DEPTH || depth > SVO_MAX_DEPTH) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "depth");
+    if (validate) {
+        Validator v{words, n_words, depth, 0, n_words + 16, ""};
+        if (!v.normal(root_word, depth)) return fail(ctx, SVO_ERR_BAD_OCTREE, v.why);
+    }
+    SVO_CUDA(ctx, cudaSetDevice(ctx->device));
+    SVO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ctx->owns_octree && ctx->d_octree) cudaFree(ctx->d_octree);
+    ctx->d_octree = nullptr;
+    ctx->owns_octree = false;
+    void* p = nullptr;
+    SVO_CUDA(ctx, cudaMalloc(&p, n_words * 4));
+    ctx->d_octree = (uint32_t*)p;
+    ctx->owns_octree = true;
+    SVO_CUDA(ctx, cudaMemcpyAsync(p, words, n_words * 4, cudaMemcpyHostToDevice, ctx->stream));
+    SVO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->n_words = n_words;
+    ctx->root = root_word;
+    ctx->depth = depth;
+    return SVO_OK;
+}
+
+svo_status svo_octree_upload_device(svo_context* ctx, const uint32_t* d_words, size_t n_words, uint32_t root_word,
+                                    int depth) {
+    if (!ctx || !d_words || n_words < 10 || n_words >= 0xffffffc0ull) return SVO_ERR_INVALID_ARGUMENT;
+    if (depth < SVO_MIN_DEPTH || depth > SVO_MAX_DEPTH) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "depth");
+    SVO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (ctx->owns_octree && ctx->d_octree) cudaFree(ctx->d_octree);
+    ctx->d_octree = const_cast<uint32_t*>(d_words);
+    ctx->owns_octree = false;
+    ctx->n_words = n_words;
+    ctx->root = root_word;
+    ctx->depth = depth;
+    return SVO_OK;
+}
+
+svo_status svo_octree_set_l2_window(svo_context* ctx, size_t bytes) {
+    if (!ctx) return SVO_ERR_INVALID_ARGUMENT;
+    if (!ctx->d_octree) return fail(ctx, SVO_ERR_NO_OCTREE, "set_l2_window");
+    cudaStreamAttrValue attr;
+    std::memset(&attr, 0, sizeof(attr));
+    if (bytes > 0) {
+        int max_window = 0, max_persist = 0;
+        SVO_CUDA(ctx, cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, ctx->device));
+        SVO_CUDA(ctx, cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, ctx->device));
+        bytes = std::min(bytes, std::min(ctx->n_words * 4, (size_t)max_window));
+        SVO_CUDA(ctx, cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, std::min(bytes, (size_t)max_persist)));
+        attr.accessPolicyWindow.base_ptr = ctx->d_octree;
+        attr.accessPolicyWindow.num_bytes = bytes;
+        attr.accessPolicyWindow.hitRatio = 1.0f;
+        attr.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+        attr.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    }
+    SVO_CUDA(ctx, cudaStreamSetAttribute(ctx->stream, cudaStreamAttributeAccessPolicyWindow, &attr));
+    if (bytes == 0) {
+        SVO_CUDA(ctx, cudaCtxResetPersistingL2Cache());
+    }
+    ctx->l2_window = bytes;
+    return SVO_OK;
+}
+
+svo_status svo_target_create(svo_context* ctx, int res_x, int res_y, svo_target** out) {
+    if (!ctx || !out || res_x < 1 || res_y < 1 || res_x > 65535 || res_y > 65535) return SVO_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    SVO_CUDA(ctx, cudaSetDevice(ctx->device));
+    auto* t = new svo_target;
+    t->ctx = ctx;
+    t->res_x = res_x;
+    t->res_y = res_y;
+    t->N = (size_t)res_x * res_y;
+    t->B.res_x = res_x;
+    t->B.res_y = res_y;
+    t->B.tiles_x = res_x / 16;
+    t->B.tiles_y = res_y / 16;
+    t->tiles = (size_t)t->B.tiles_x * t->B.tiles_y;
+    const size_t N = t->N;
+    svo_status st = SVO_OK;
+    auto A = [&](void** p, size_t bytes) {
+        if (st == SVO_OK) st = alloc(ctx, p, bytes);
+    };
+    A((void**)&t->B.col[0], N * 4);
+    A((void**)&t->B.col[1], N * 4);
+    A((void**)&t->B.xyz[0], N * 16);
+    A((void**)&t->B.xyz[1], N * 16);
+    A((void**)&t->B.disp, N * 4);
+    A((void**)&t->B.bgrx, N * 4);
+    A((void**)&t->B.keys, N * 8);
+    A((void**)&t->B.ids, (N + 2 * t->tiles + 4) * 4);
+    A((void**)&t->B.tile_mask, (t->tiles + 1) * 8);
+    A((void**)&t->B.counters, 64);
+    A((void**)&t->d_params, sizeof(FrameParams));
+    A((void**)&t->full_col, N * 4);
+    A((void**)&t->full_xyzw, N * 16);
+    A((void**)&t->full_vox, N * 8);
+    if (st != SVO_OK) {
+        svo_target_destroy(t);
+        return st;
+    }
+    cudaStream_t s = ctx->stream;
+    SVO_CUDA(ctx, cudaMemsetAsync(t->B.keys, 0xff, N * 8, s));
+    SVO_CUDA(ctx, cudaMemsetAsync(t->B.col[0], 0xff, N * 4, s));
+    SVO_CUDA(ctx, cudaMemsetAsync(t->B.col[1], 0xff, N * 4, s));
+    SVO_CUDA(ctx, cudaMemsetAsync(t->B.xyz[0], 0, N * 16, s));
+    SVO_CUDA(ctx, cudaMemsetAsync(t->B.xyz[1], 0, N * 16, s));
+    SVO_CUDA(ctx, cudaMemsetAsync(t->B.ids, 0, (N + 2 * t->tiles + 4) * 4, s));
+    SVO_CUDA(ctx, cudaMemsetAsync(t->B.tile_mask, 0, (t->tiles + 1) * 8, s));
+    SVO_CUDA(ctx, cudaMemsetAsync(t->B.counters, 0, 64, s));
+    SVO_CUDA(ctx, cudaMemsetAsync(t->B.bgrx, 0, N * 4, s));
+    SVO_CUDA(ctx, cudaMemsetAsync(t->B.disp, 0xff, N * 4, s));
+    for (auto& e : t->ev) SVO_CUDA(ctx, cudaEventCreate(&e));
+    SVO_CUDA(ctx, cudaStreamSynchronize(s));
+    *out = t;
+    return SVO_OK;
+}
+
+svo_status svo_target_destroy(svo_target* t) {
+    if (!t) return SVO_OK;
+    svo_context* ctx = t->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (t->graph_exec) cudaGraphExecDestroy(t->graph_exec);
+    if (t->graph) cudaGraphDestroy(t->graph);
+    void* ptrs[] = {t->B.col[0], t->B.col[1], t->B.xyz[0], t->B.xyz[1], t->B.disp, t->B.bgrx, t->B.keys, t->B.ids,
+                    t->B.tile_mask, t->B.counters, t->d_params, t->full_col, t->full_xyzw, t->full_vox};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    for (auto& e : t->ev)
+        if (e) cudaEventDestroy(e);
+    delete t;
+    return SVO_OK;
+}
+
+svo_status svo_target_use_graph(svo_target* t, int enable) {
+    if (!t) return SVO_ERR_INVALID_ARGUMENT;
+    t->use_graph = enable != 0;
+    if (!t->use_graph && t->graph_exec) {
+        cudaGraphExecDestroy(t->graph_exec);
+        cudaGraphDestroy(t->graph);
+        t->graph_exec = nullptr;
+        t->graph = nullptr;
+        t->params_node = nullptr;
+    }
+    return SVO_OK;
+}
+
+svo_status svo_target_set_profiling(svo_target* t, int enable) {
+    if (!t) return SVO_ERR_INVALID_ARGUMENT;
+    t->profiling = enable != 0;
+    return SVO_OK;
+}
+
+int svo_target_stage_times(svo_target* t, float* ms, int cap) {
+    if (!t || !ms || t->n_events < 2) return 0;
+    if (cudaEventSynchronize(t->ev[t->n_events - 1]) != cudaSuccess) return 0;
+    int k = 0;
+    if (t->last_mode == 1) {
+        for (int i = 0; i < 6 && i < cap; ++i, ++k) {
+            float v = 0;
+            cudaEventElapsedTime(&v, t->ev[i], t->ev[i + 1]);
+            ms[i] = v;
+        }
+    } else {
+        for (int i = 0; i < cap && i < 6; ++i) ms[i] = 0.0f;
+        if (cap > 4) cudaEventElapsedTime(&ms[4], t->ev[0], t->ev[1]);
+        k = std::min(cap, 6);
+    }
+    return k;
+}
+
+static svo_status check_view(svo_context* ctx, const svo_target* t, const svo_view* v) {
+    if (!v) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "null view");
+    if (v->res_x != t->res_x || v->res_y != t->res_y) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "view resolution differs from the target");
+    if (!ctx->d_octree) return fail(ctx, SVO_ERR_NO_OCTREE, "upload an octree first");
+    return SVO_OK;
+}
+
+svo_status svo_raycast_full_batch(svo_context* ctx, svo_target* const* targets, const svo_view* views, int n) {
+    if (!ctx || !targets || !views || n < 1 || n > kMaxBatchViews) return SVO_ERR_INVALID_ARGUMENT;
+    if (!ctx->d_octree) return fail(ctx, SVO_ERR_NO_OCTREE, "upload an octree first");
+    for (int i = 0; i < n; ++i) {
+        if (!targets[i] || targets[i]->ctx != ctx) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "target");
+        svo_status s = check_view(ctx, targets[i], &views[i]);
+        if (s != SVO_OK) return s;
+    }
+    const int slot = ctx->batch_slot;
+    ctx->batch_slot = (slot + 1) % svo_context::kRing;
+    // The slot's previous copy must have left the staging buffer.
+    SVO_CUDA(ctx, cudaEventSynchronize(ctx->batch_done[slot]));
+    FullBatch* hb = ctx->h_batch[slot];
+    hb->n_views = n;
+    uint32_t packets = 0;
+    for (int i = 0; i < n; ++i) {
+        FullView& fv = hb->v[i];
+        const svo_view& v = views[i];
+        fv.ray = make_raycam(v);
+        fv.res_x = v.res_x;
+        fv.res_y = v.res_y;
+        fv.packets_x = (v.res_x + 7) / 8;
+        fv.packet_begin = packets;
+        packets += (uint32_t)fv.packets_x * (uint32_t)((v.res_y + 3) / 4);
+        fv.col = targets[i]->full_col;
+        fv.xyzw = targets[i]->full_xyzw;
+        fv.vox = targets[i]->full_vox;
+        fv.bgrx = targets[i]->B.bgrx;
+    }
+    hb->total_packets = packets;
+    const size_t bytes = offsetof(FullBatch, v) + sizeof(FullView) * n;
+    svo_target* t0 = targets[0];
+    if (t0->profiling) {
+        cudaEventRecord(t0->ev[0], ctx->stream);
+    }
+    SVO_CUDA(ctx, cudaMemcpyAsync(ctx->d_batch[slot], hb, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    k_reset_counter<<<1, 1, 0, ctx->stream>>>(ctx->d_counter);
+    SVO_LAUNCHED(ctx);
+    svo_status st = launch_trace_full(ctx, ctx->d_batch[slot], true);
+    SVO_CUDA(ctx, cudaEventRecord(ctx->batch_done[slot], ctx->stream));
+    if (st != SVO_OK) return st;
+    if (t0->profiling) {
+        cudaEventRecord(t0->ev[1], ctx->stream);
+        t0->n_events = 2;
+        t0->last_mode = 2;
+    }
+    return SVO_OK;
+}
+
+svo_status svo_raycast_full(svo_context* ctx, svo_target* t, const svo_view* view) {
+    if (!ctx || !t) return SVO_ERR_INVALID_ARGUMENT;
+    return svo_raycast_full_batch(ctx, &t, view, 1);
+}
+
+svo_status svo_warp_frame(svo_context* ctx, svo_target* t, const svo_view* view, int frame) {
+    if (!ctx || !t || t->ctx != ctx) return SVO_ERR_INVALID_ARGUMENT;
+    svo_status st = check_view(ctx, t, view);
+    if (st != SVO_OK) return st;
+    if (t->res_x < 16 || t->res_y < 16)
+        return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "warp frames need res >= 16 (the reference's 16x16 hole tiles)");
+    if (view->fovx != 1.0f || view->fovy != 1.0f)
+        return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "warp frames use fov 1 (raycast_proj has no fov term)");
+    if (frame < 0) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "frame");
+    const int cur = (int)(t->frames & 1);
+    const bool have_cache = frame >= 2 && t->have_prev;
+    FrameParams p = make_params(t, *view, frame, cur, have_cache);
+    cudaStream_t s = ctx->stream;
+    if (t->use_graph) {
+        if (!t->graph_exec || t->graph_profiled != t->profiling) {
+            if (t->graph_exec) {
+                cudaGraphExecDestroy(t->graph_exec);
+                cudaGraphDestroy(t->graph);
+                t->graph_exec = nullptr;
+                t->graph = nullptr;
+            }
+            SVO_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            k_set_params<<<1, 1, 0, s>>>(p, t->d_params, t->B.counters);
+            st = enqueue_warp_body(ctx, t);
+            cudaGraph_t g = nullptr;
+            cudaError_t ce = cudaStreamEndCapture(s, &g);
+            if (st != SVO_OK) {
+                if (g) cudaGraphDestroy(g);
+                return st;
+            }
+            if (ce != cudaSuccess) return fail(ctx, SVO_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(ce));
+            t->graph = g;
+            SVO_CUDA(ctx, cudaGraphInstantiate(&t->graph_exec, g, 0));
+            // Find the k_set_params node (the only root of the graph).
+            size_t nroots = 0;
+            SVO_CUDA(ctx, cudaGraphGetRootNodes(g, nullptr, &nroots));
+            std::vector<cudaGraphNode_t> roots(nroots);
+            SVO_CUDA(ctx, cudaGraphGetRootNodes(g, roots.data(), &nroots));
+            t->params_node = nullptr;
+            for (auto nd : roots) {
+                cudaGraphNodeType ty;
+                if (cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) {
+                    cudaKernelNodeParams kp;
+                    if (cudaGraphKernelNodeGetParams(nd, &kp) == cudaSuccess && kp.func == (void*)k_set_params)
+                        t->params_node = nd;
+                }
+            }
+            if (!t->params_node) return fail(ctx, SVO_ERR_CUDA, "graph: parameter node not found");
+            t->graph_profiled = t->profiling;
+        }
+        cudaKernelNodeParams kp;
+        SVO_CUDA(ctx, cudaGraphKernelNodeGetParams(t->params_node, &kp));
+        FrameParams* dst = t->d_params;
+        uint32_t* cnt = t->B.counters;
+        void* args[] = {&p, &dst, &cnt};
+        kp.kernelParams = args;
+        kp.extra = nullptr;
+        SVO_CUDA(ctx, cudaGraphExecKernelNodeSetParams(t->graph_exec, t->params_node, &kp));
+        SVO_CUDA(ctx, cudaGraphLaunch(t->graph_exec, s));
+        ctx->launches += 7;
+    } else {
+        k_set_params<<<1, 1, 0, s>>>(p, t->d_params, t->B.counters);
+        SVO_LAUNCHED(ctx);
+        st = enqueue_warp_body(ctx, t);
+        if (st != SVO_OK) return st;
+    }
+    if (t->profiling) {
+        t->n_events = 7;
+        t->last_mode = 1;
+    }
+    t->last_cur = cur;
+    t->have_prev = true;
+    ++t->frames;
+    return SVO_OK;
+}
+
+static svo_status read_back(svo_target* t, void* host, const void* dev, size_t bytes) {
+    svo_context* ctx = t->ctx;
+    if (!host) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "null host buffer");
+    SVO_CUDA(ctx, cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    SVO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SVO_OK;
+}
+
+svo_status svo_read_colour(svo_target* t, int plane, uint32_t* host) {
+    if (!t) return SVO_ERR_INVALID_ARGUMENT;
+    if (plane == 0) return read_back(t, host, t->B.disp, t->N * 4);
+    if (plane == 2) return read_back(t, host, t->B.col[t->last_cur], t->N * 4);
+    if (plane == 1) {
+        if (!host) return SVO_ERR_INVALID_ARGUMENT;
+        for (size_t i = 0; i < t->N; ++i) host[i] = SVO_EMPTY_PIXEL;
+        return SVO_OK;
+    }
+    return fail(t->ctx, SVO_ERR_INVALID_ARGUMENT, "plane");
+}
+
+svo_status svo_read_coords(svo_target* t, int plane, float* host) {
+    if (!t) return SVO_ERR_INVALID_ARGUMENT;
+    if (plane == 0 || plane == 2) return read_back(t, host, t->B.xyz[t->last_cur], t->N * 16);
+    return fail(t->ctx, SVO_ERR_INVALID_ARGUMENT, "plane");
+}
+
+svo_status svo_read_holes(svo_target* t, uint32_t* host, size_t cap_words, uint32_t* count) {
+    if (!t || !host) return SVO_ERR_INVALID_ARGUMENT;
+    uint32_t total = 0;
+    svo_status st = read_back(t, &total, t->B.counters + 1, 4);
+    if (st != SVO_OK) return st;
+    const size_t words = 2 * t->tiles + total;
+    if (count) *count = total;
+    if (cap_words < words) return fail(t->ctx, SVO_ERR_INVALID_ARGUMENT, "hole buffer too small");
+    return read_back(t, host, t->B.ids, words * 4);
+}
+
+svo_status svo_read_bgrx(svo_target* t, uint32_t* host) {
+    if (!t) return SVO_ERR_INVALID_ARGUMENT;
+    return read_back(t, host, t->B.bgrx, t->N * 4);
+}
+
+svo_status svo_read_full(svo_target* t, uint32_t* colour, float* xyzw) {
+    if (!t) return SVO_ERR_INVALID_ARGUMENT;
+    svo_status st = SVO_OK;
+    if (colour) st = read_back(t, colour, t->full_col, t->N * 4);
+    if (st == SVO_OK && xyzw) st = read_back(t, xyzw, t->full_xyzw, t->N * 16);
+    return st;
+}
+
+svo_status svo_read_voxels(svo_target* t, uint64_t* host) {
+    if (!t) return SVO_ERR_INVALID_ARGUMENT;
+    return read_back(t, host, t->full_vox, t->N * 8);
+}
+
+svo_status svo_target_device_outputs(svo_target* t, svo_device_outputs* out) {
+    if (!t || !out) return SVO_ERR_INVALID_ARGUMENT;
+    out->bgrx = t->B.bgrx;
+    out->colour = t->B.disp;
+    out->full_colour = t->full_col;
+    out->full_xyzw = (float*)t->full_xyzw;
+    out->full_voxel = t->full_vox;
+    return SVO_OK;
+}
+
+}  // extern "C"

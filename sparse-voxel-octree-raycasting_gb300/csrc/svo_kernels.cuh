@@ -1,0 +1,405 @@
+// svo_kernels.cuh -- the per-frame kernels of the raycast + warp pipeline.
+//
+// Reference call sequence (src/raycast.h:147-441) and how it maps here:
+//   memset plane 0 (+ all planes while frame<2)       } k_project (scatter) +
+//   raycast_proj x2 (kernel.cl:472-592)              } k_resolve_gather (gather,
+//   raycast_counthole (kernel.cl:234-274)            }   clear and hole count)
+//   raycast_sumids + blocking 4-byte readback         -> k_hole_scan (on device)
+//   raycast_writeids (kernel.cl:298-340)              -> k_hole_write
+//   raycast_holes + raycast_fine_2 (kernel.cl:594-942)-> k_trace<.., kWarp> (one
+//                                                         persistent launch)
+//   memcpy plane 0 -> plane 2 (raycast.h:390-405)      -> none: the current and
+//                                                         cache planes swap roles
+//   raycast_fillhole2 + raycast_colorize               -> k_fill_colorize
+//
+// Determinism: raycast_proj resolves depth ties racily on a GPU; here every
+// target takes the source with the smallest (depth key, source index) through
+// one 64-bit atomicMin, which is what running the work-items in order gives.
+// raycast_fillhole2 reads its neighbours from the unfiltered plane (the
+// filter writes a separate displayed plane), i.e. snapshot order.
+#pragma once
+#include <cstdint>
+
+#include "svo_trace.cuh"
+
+namespace svo {
+
+constexpr uint64_t kKeyEmpty = ~0ull;
+constexpr int kTraceBlock = 128;
+constexpr int kMaxBatchViews = 256;
+
+// Everything one warp frame needs, written to device memory by k_set_params
+// at the start of the frame (so a captured CUDA graph replays unchanged).
+struct FrameParams {
+    RayCam ray;                 // ray camera (rows of m^T)
+    float vx[3], vy[3], vz[3];  // rows of m (raycast_proj's a_mx/a_my/a_mz)
+    int frame;
+    int cur;         // which of the two colour/coordinate planes is current
+    int have_cache;  // the other plane holds the previous frame
+    int add_x, add_y, x_end, y_end;  // refresh tile rectangle (raycast.h:363-366)
+};
+
+// Buffers of one render target.
+struct TargetBuffers {
+    uint32_t* col[2];   // current / cache colour planes (swap every frame)
+    float4* xyz[2];     // current / cache coordinate planes
+    uint32_t* disp;     // displayed colour plane (after the filter)
+    uint32_t* bgrx;     // colourised output
+    uint64_t* keys;     // per-pixel projection keys, kKeyEmpty between frames
+    uint32_t* ids;      // hole id buffer in the reference layout
+    uint64_t* tile_mask;  // per 16x16 tile, bit j*8+i = 2x2 block (i,j) empty
+    uint32_t* counters;   // [0] trace work counter, [1] hole entries
+    int res_x, res_y;
+    int tiles_x, tiles_y;  // whole 16x16 tiles (res/16)
+};
+
+// One view of a (batched) full raycast.
+struct FullView {
+    RayCam ray;
+    int res_x, res_y;
+    int packets_x;          // ceil(res_x/8): 8x4-pixel ray packets per row
+    uint32_t packet_begin;  // first packet of this view in the batch
+    uint32_t* col;
+    float4* xyzw;
+    uint64_t* vox;
+    uint32_t* bgrx;
+};
+
+struct FullBatch {
+    int n_views;
+    uint32_t total_packets;
+    FullView v[kMaxBatchViews];
+};
+
+// Plane selection without dynamic indexing of the by-value parameter struct
+// (which would force a local-memory copy of it).
+__device__ __forceinline__ uint32_t* plane_col(const TargetBuffers& B, int i) { return i ? B.col[1] : B.col[0]; }
+__device__ __forceinline__ float4* plane_xyz(const TargetBuffers& B, int i) { return i ? B.xyz[1] : B.xyz[0]; }
+
+__global__ void k_set_params(FrameParams p, FrameParams* dst, uint32_t* counters) {
+    *dst = p;
+    counters[0] = 0;
+    counters[1] = 0;
+}
+
+__global__ void k_reset_counter(uint32_t* counter) { *counter = 0; }
+
+// ------------------------------------------------------- reprojection --
+// Screen coordinate of raycast_proj (kernel.cl:552-556):
+//   trunc(float(double(num)/double(z) + double(half)))
+// -- the unsuffixed 0.0 literals make the reference's expression double. The
+// float path decides every pixel whose value is further than its error bound
+// (2^-22 of the magnitude) from an integer; the rest (about 0.1%) take the
+// double path, which is exact.
+__device__ __forceinline__ int proj_coord(float num, float z, float half) {
+    const float q = __fdiv_rn(num, z);
+    const float y = __fadd_rn(q, half);
+    const float bound = __fmul_rn(__fadd_rn(__fadd_rn(fabsf(q), fabsf(half)), 1.0f), 2.384185791015625e-07f);
+    const float r = rintf(y);
+    if (r == 0.0f || fabsf(__fsub_rn(y, r)) > bound) return __float2int_rz(y);
+    const double v = __dadd_rn(__ddiv_rn((double)num, (double)z), (double)half);
+    return __float2int_rz(__double2float_rn(v));
+}
+
+__device__ __forceinline__ float dot3(float ax, float ay, float az, const float* b) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(ax, b[0]), __fmul_rn(ay, b[1])), __fmul_rn(az, b[2]));
+}
+
+// Scatter: every non-empty cache pixel proposes itself to the pixel it
+// reprojects to. Key = depth key (int(z*1000)<<8, unsigned) << 32 | source.
+__global__ void __launch_bounds__(256) k_project(const FrameParams* __restrict__ P, TargetBuffers B) {
+    if (!P->have_cache) return;
+    const int res_x = B.res_x, res_y = B.res_y;
+    const uint32_t N = (uint32_t)res_x * (uint32_t)res_y;
+    const int cache = P->cur ^ 1;
+    const uint32_t* __restrict__ col = plane_col(B, cache);
+    const float4* __restrict__ xyz = plane_xyz(B, cache);
+    const float px = P->ray.px, py = P->ray.py, pz = P->ray.pz;
+    float vx[3], vy[3], vz[3];
+    for (int i = 0; i < 3; ++i) {
+        vx[i] = P->vx[i];
+        vy[i] = P->vy[i];
+        vz[i] = P->vz[i];
+    }
+    const float hx = (float)res_x / 2.0f, hy = (float)res_y / 2.0f;
+    const float fry = (float)res_y;
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += gridDim.x * blockDim.x) {
+        const uint32_t c = __ldg(col + s);
+        if (c == kEmptyPixel) continue;
+        const float4 q = __ldg(xyz + s);
+        const float ax = __fsub_rn(q.x, px), ay = __fsub_rn(q.y, py), az = __fsub_rn(q.z, pz);
+        const float zz = dot3(ax, ay, az, vz);
+        if (zz < 0.05f) continue;  // (double)z < 0.05 <=> z < 0.05f for a binary32 z
+        const int sx = proj_coord(__fmul_rn(dot3(ax, ay, az, vx), fry), zz, hx);
+        const int sy = proj_coord(__fmul_rn(dot3(ax, ay, az, vy), fry), zz, hy);
+        if (sx >= res_x - 1 || sx < 0 || sy >= res_y - 1 || sy < 0) continue;
+        const uint32_t sz = (uint32_t)__float2int_rz(__fmul_rn(zz, 1000.0f)) << 8;
+        if (sz >= kEmptyPixel) continue;  // cannot beat the cleared value (kernel.cl:571)
+        const uint32_t t = (uint32_t)sy * (uint32_t)res_x + (uint32_t)sx;
+        atomicMin((unsigned long long*)(B.keys + t), (unsigned long long)(((uint64_t)sz << 32) | s));
+    }
+}
+
+// Gather + clear + hole count, one 16x16 tile per block: each target pixel
+// takes its winning source (or becomes empty), then the block marks the 2x2
+// blocks whose four pixels are empty (raycast_counthole's test with
+// HOLE_PIXEL_THRESHOLD = 4, kernel.cl:262-271). Only whole tiles are counted
+// (kernel.cl:243-244).
+__global__ void __launch_bounds__(256) k_resolve_gather(const FrameParams* __restrict__ P, TargetBuffers B) {
+    __shared__ uint8_t empty[16][17];
+    __shared__ uint32_t halves[2];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int x = blockIdx.x * 16 + tx, y = blockIdx.y * 16 + ty;
+    const int res_x = B.res_x, res_y = B.res_y;
+    const int cur = P->cur;
+    bool is_empty = true;
+    if (x < res_x && y < res_y) {
+        const uint32_t t = (uint32_t)y * (uint32_t)res_x + (uint32_t)x;
+        uint32_t outc = kEmptyPixel;
+        if (P->have_cache) {
+            const uint64_t key = B.keys[t];
+            if (key != kKeyEmpty) {
+                B.keys[t] = kKeyEmpty;
+                const uint32_t src = (uint32_t)key;
+                const float4 q = plane_xyz(B, cur ^ 1)[src];
+                const float ax = __fsub_rn(q.x, P->ray.px), ay = __fsub_rn(q.y, P->ray.py),
+                            az = __fsub_rn(q.z, P->ray.pz);
+                outc = (uint32_t)(key >> 32) + (plane_col(B, cur ^ 1)[src] & 255u);
+                plane_xyz(B, cur)[t] = make_float4(q.x, q.y, q.z, dot3(ax, ay, az, P->vz));
+            }
+        }
+        plane_col(B, cur)[t] = outc;
+        is_empty = outc == kEmptyPixel;
+    }
+    empty[ty][tx] = is_empty;
+    __syncthreads();
+    if (blockIdx.x >= (unsigned)B.tiles_x || blockIdx.y >= (unsigned)B.tiles_y) return;  // block-uniform
+    bool hole = false;
+    if (threadIdx.x < 64) {
+        const int i = threadIdx.x & 7, j = threadIdx.x >> 3;
+        hole = empty[2 * j][2 * i] && empty[2 * j][2 * i + 1] && empty[2 * j + 1][2 * i] && empty[2 * j + 1][2 * i + 1];
+    }
+    const uint32_t bal = __ballot_sync(0xffffffffu, hole);
+    if (threadIdx.x == 0 || threadIdx.x == 32) halves[threadIdx.x >> 5] = bal;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t tile = blockIdx.y * B.tiles_x + blockIdx.x;
+        B.tile_mask[tile] = (uint64_t)halves[0] | ((uint64_t)halves[1] << 32);
+    }
+}
+
+// raycast_sumids (kernel.cl:276-296) without the single-thread loop or the
+// host readback: one block scans the tile counts and leaves the total on the
+// device. ids[t] = 4*holes(t) except ids[0] = total; ids[tiles+t] = exclusive
+// offset of tile t.
+__global__ void __launch_bounds__(1024) k_hole_scan(TargetBuffers B) {
+    __shared__ uint32_t warp_sums[32];
+    const uint32_t tiles = (uint32_t)B.tiles_x * (uint32_t)B.tiles_y;
+    const uint32_t per = (tiles + blockDim.x - 1) / blockDim.x;
+    const uint32_t a = threadIdx.x * per, b = min(a + per, tiles);
+    uint32_t local = 0;
+    for (uint32_t t = a; t < b; ++t) local += 4u * (uint32_t)__popcll(B.tile_mask[t]);
+    // block exclusive scan of `local`
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = local;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0u;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t v = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += v;
+        }
+        warp_sums[lane] = w;  // inclusive warp prefix
+    }
+    __syncthreads();
+    uint32_t acc = incl - local + (warp > 0 ? warp_sums[warp - 1] : 0u);
+    for (uint32_t t = a; t < b; ++t) {
+        const uint32_t cnt = 4u * (uint32_t)__popcll(B.tile_mask[t]);
+        B.ids[tiles + t] = acc;
+        if (t > 0) B.ids[t] = cnt;
+        acc += cnt;
+    }
+    if (threadIdx.x == blockDim.x - 1) {
+        const uint32_t total = warp_sums[(blockDim.x >> 5) - 1];
+        if (tiles > 0) B.ids[0] = total;
+        B.counters[1] = total;
+        B.counters[0] = 0;
+    }
+}
+
+// raycast_writeids (kernel.cl:298-340): per tile, per empty 2x2 block (rows
+// outer, columns inner) the four entries (x,y),(x+1,y),(x+1,y+1),(x,y+1),
+// packed x | y<<16. One warp per tile.
+__global__ void __launch_bounds__(256) k_hole_write(TargetBuffers B) {
+    const uint32_t tiles = (uint32_t)B.tiles_x * (uint32_t)B.tiles_y;
+    const uint32_t tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (tile >= tiles) return;
+    const int lane = threadIdx.x & 31;
+    const uint64_t m = B.tile_mask[tile];
+    if (m == 0) return;
+    const uint32_t base = 2u * tiles + B.ids[tiles + tile];
+    const uint32_t x0 = (tile % (uint32_t)B.tiles_x) * 16u, y0 = (tile / (uint32_t)B.tiles_x) * 16u;
+    for (int bit = lane; bit < 64; bit += 32) {
+        if (!((m >> bit) & 1ull)) continue;
+        const uint32_t rank = (uint32_t)__popcll(m & ((1ull << bit) - 1ull));
+        const uint32_t i = bit & 7, j = bit >> 3;
+        const uint32_t val = (x0 + 2u * i) + ((y0 + 2u * j) << 16);
+        uint32_t* dst = B.ids + base + 4u * rank;
+        dst[0] = val;
+        dst[1] = val + 1u;
+        dst[2] = val + 1u + (1u << 16);
+        dst[3] = val + (1u << 16);
+    }
+}
+
+// ----------------------------------------------------------- tracing --
+// Persistent ray tracer. Each warp repeatedly takes a 32-ray packet from a
+// global atomic work counter. Full mode: packets are 8x4 pixel tiles of the
+// batch's views, in view order. Warp mode: first the hole list (32
+// consecutive entries = eight neighbouring 2x2 blocks), then the 8x4 tiles of
+// the refresh rectangle; holes inside the rectangle are left to it (both
+// would store identical values).
+template <int DEPTH, bool kVoxel>
+__global__ void __launch_bounds__(kTraceBlock) k_trace_full(Octree o, const FullBatch* __restrict__ batch,
+                                                          uint32_t* counter, uint32_t* fault_out) {
+    __shared__ uint32_t stack[(DEPTH + 1) * kTraceBlock];
+    const int lane = threadIdx.x & 31;
+    uint32_t* stk = stack + threadIdx.x;
+    uint32_t fault = 0;
+    const uint32_t total = batch->total_packets;
+    const int nv = batch->n_views;
+    for (;;) {
+        uint32_t p = 0;
+        if (lane == 0) p = atomicAdd(counter, 1u);
+        p = __shfl_sync(0xffffffffu, p, 0);
+        if (p >= total) break;
+        int v = 0;
+        {  // view of packet p (views are few; binary search on packet_begin)
+            int lo = 0, hi = nv - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (batch->v[mid].packet_begin <= p) lo = mid; else hi = mid - 1;
+            }
+            v = lo;
+        }
+        const FullView& fv = batch->v[v];
+        const uint32_t q = p - fv.packet_begin;
+        const int x = (int)(q % (uint32_t)fv.packets_x) * 8 + (lane & 7);
+        const int y = (int)(q / (uint32_t)fv.packets_x) * 4 + (lane >> 3);
+        if (x < fv.res_x && y < fv.res_y) {
+            const RayCam cam = fv.ray;
+            const RayResult r = trace_ray<DEPTH, kVoxel>(o, cam, x, y, fv.res_x, fv.res_y, stk, kTraceBlock, fault);
+            const size_t ofs = (size_t)y * fv.res_x + x;
+            fv.col[ofs] = r.colour;
+            fv.xyzw[ofs] = make_float4(r.hx, r.hy, r.hz, r.dist);
+            if (kVoxel) fv.vox[ofs] = r.voxel;
+            fv.bgrx[ofs] = colorize(r.colour);
+        }
+    }
+    if (fault) atomicOr(fault_out, fault);
+}
+
+template <int DEPTH>
+__global__ void __launch_bounds__(kTraceBlock) k_trace_warp(Octree o, const FrameParams* __restrict__ P,
+                                                          TargetBuffers B, uint32_t* fault_out) {
+    __shared__ uint32_t stack[(DEPTH + 1) * kTraceBlock];
+    const int lane = threadIdx.x & 31;
+    uint32_t* stk = stack + threadIdx.x;
+    uint32_t fault = 0;
+    const int res_x = B.res_x, res_y = B.res_y;
+    const uint32_t tiles = (uint32_t)B.tiles_x * (uint32_t)B.tiles_y;
+    const uint32_t holes = B.counters[1];
+    const uint32_t hole_packets = (holes + 31u) / 32u;
+    const int ax = P->add_x, ay = P->add_y, xe = P->x_end, ye = P->y_end;
+    const uint32_t rpx = (uint32_t)max(0, (xe - ax + 7) / 8), rpy = (uint32_t)max(0, (ye - ay + 3) / 4);
+    const uint32_t total = hole_packets + rpx * rpy;
+    const RayCam cam = P->ray;
+    float4* __restrict__ xyz = plane_xyz(B, P->cur);
+    uint32_t* __restrict__ col = plane_col(B, P->cur);
+    for (;;) {
+        uint32_t p = 0;
+        if (lane == 0) p = atomicAdd(B.counters, 1u);
+        p = __shfl_sync(0xffffffffu, p, 0);
+        if (p >= total) break;
+        int x, y;
+        bool valid;
+        if (p < hole_packets) {
+            const uint32_t e = p * 32u + (uint32_t)lane;
+            valid = e < holes;
+            const uint32_t xy = valid ? B.ids[2u * tiles + e] : 0u;
+            x = (int)(xy & 0xffffu);
+            y = (int)(xy >> 16);
+            if (valid && (x >= res_x || y >= res_y)) {
+                fault |= kFaultHoleEntry;
+                valid = false;
+            }
+            if (x >= ax && x < xe && y >= ay && y < ye) valid = false;  // traced by the refresh tile
+        } else {
+            const uint32_t q = p - hole_packets;
+            x = ax + (int)(q % rpx) * 8 + (lane & 7);
+            y = ay + (int)(q / rpx) * 4 + (lane >> 3);
+            valid = x < xe && y < ye;
+        }
+        if (valid) {
+            const RayResult r = trace_ray<DEPTH, false>(o, cam, x, y, res_x, res_y, stk, kTraceBlock, fault);
+            const size_t ofs = (size_t)y * res_x + x;
+            col[ofs] = r.colour;
+            xyz[ofs] = make_float4(r.hx, r.hy, r.hz, r.dist);
+        }
+    }
+    if (fault) atomicOr(fault_out, fault);
+}
+
+// ----------------------------------------------- filter + colourise ----
+// raycast_fillhole2 (kernel.cl:404-470) reading the unfiltered current plane
+// and writing the displayed plane, fused with raycast_colorize.
+__device__ __forceinline__ uint32_t read_lin(const uint32_t* __restrict__ s, long long o, long long n) {
+    // The reference addresses plane 0 linearly; reads past its end land in the
+    // never-written plane 1, i.e. an empty pixel.
+    return (o >= 0 && o < n) ? __ldg(s + o) : kEmptyPixel;
+}
+
+__global__ void __launch_bounds__(256) k_fill_colorize(const FrameParams* __restrict__ P, TargetBuffers B) {
+    const int idx = blockIdx.x * 32 + (threadIdx.x & 31);
+    const int idy = blockIdx.y * 8 + (threadIdx.x >> 5);
+    const int res_x = B.res_x, res_y = B.res_y;
+    if (idx >= res_x || idy >= res_y) return;
+    const uint32_t* __restrict__ s = plane_col(B, P->cur);
+    const long long n = (long long)res_x * res_y;
+    const long long ofs = (long long)idy * res_x + idx;
+    uint32_t col = __ldg(s + ofs);
+    if (col == kEmptyPixel && idx < res_x - 1 && idy < res_y - 1 && idx > 1 && idy > 1) {
+        const int c1 = (int)__ldg(s + ofs + 1), c2 = (int)__ldg(s + ofs - 1);
+        const int c3 = (int)__ldg(s + ofs + res_x), c4 = (int)__ldg(s + ofs - res_x);
+        const bool s1 = (uint32_t)c1 != kEmptyPixel, s2 = (uint32_t)c2 != kEmptyPixel;
+        const bool s3 = (uint32_t)c3 != kEmptyPixel, s4 = (uint32_t)c4 != kEmptyPixel;
+        if (s1 && s2 && s3 && s4) {
+            col = (uint32_t)((c1 & 3) + ((((c1 & 0xfc) + (c2 & 0xfc) + (c3 & 0xfc) + (c4 & 0xfc)) >> 2) & 0xfc));
+        } else if (s1 && s2) {
+            col = (uint32_t)((c1 & 3) + ((((c1 & 0xfc) + (c2 & 0xfc)) >> 1) & 0xfc));
+        } else if (s3 && s4) {
+            col = (uint32_t)((c3 & 3) + ((((c3 & 0xfc) + (c4 & 0xfc)) >> 1) & 0xfc));
+        } else {
+            for (int i = 0; i < 4; ++i) {
+                col = read_lin(s, ofs + (i & 1) + ((i >> 1) & 1) * res_x, n);
+                if (col != kEmptyPixel) break;
+            }
+            if (col == kEmptyPixel) {
+                for (int i = -2; i < 3 && col == kEmptyPixel; ++i)
+                    for (int j = -2; j < 3; ++j) {
+                        col = read_lin(s, ofs + i + (long long)j * res_x, n);
+                        if (col != kEmptyPixel) break;
+                    }
+            }
+        }
+    }
+    B.disp[ofs] = col;
+    B.bgrx[ofs] = colorize(col);
+}
+
+}  // namespace svo

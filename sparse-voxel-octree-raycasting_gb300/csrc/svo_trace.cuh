@@ -1,0 +1,269 @@
+// svo_trace.cuh -- device-side octree traversal for sm_103a.
+//
+// One ray = one thread. The walk is the reference's CAST_RAY
+// (kernel/kernel.cl:114-214) with its node fetches fetchChildOffset/fetchColor
+// (:32-112): the same float operations in the same order, so a GB300 ray
+// lands on the same voxel with the same colour word and the same hit
+// position bits as the strict-IEEE oracle. Every float operation is an
+// explicit round-to-nearest intrinsic (no FMA contraction, IEEE division and
+// square root); float->int conversions truncate like OpenCL's convert_int.
+//
+// GB300 layout choices:
+//   * node words are read through the read-only path (__ldg) with a bounds
+//     check against the uploaded word count (a bad word raises a fault flag
+//     instead of reading outside the allocation);
+//   * the per-ray node stack lives in shared memory as [level][thread], so the
+//     32 lanes of a warp always hit 32 different banks;
+//   * loop state stays in registers; the pop level is a count-leading-zeros
+//     instead of kernel.cl:202's log2 of a float (identical for every input
+//     the walk can produce, pinned by a known-answer test);
+//   * every walk is capped at kStepCap steps (fault flag 2) so no input can
+//     keep a kernel spinning.
+#pragma once
+#include <cstdint>
+
+namespace svo {
+
+constexpr uint32_t kEmptyPixel = 0xffffff00u;
+constexpr float kViewDistMax = 400000.0f;  // VIEW_DIST_MAX, kernel.cl:15
+constexpr uint32_t kStepCap = 1u << 20;
+constexpr uint32_t kFaultFetch = 1u;       // node word index outside the octree
+constexpr uint32_t kFaultSteps = 2u;       // a ray exceeded kStepCap steps
+constexpr uint32_t kFaultHoleEntry = 4u;   // hole list entry outside the frame
+
+struct Octree {
+    const uint32_t* __restrict__ words;
+    uint32_t n_words;
+    uint32_t root;
+};
+
+// Camera as the ray kernels consume it: position and the rows of m^T.
+struct RayCam {
+    float px, py, pz;
+    float mxx, mxy, mxz;
+    float myx, myy, myz;
+    float mzx, mzy, mzz;
+    float fovx, fovy;
+};
+
+struct RayResult {
+    uint32_t colour;   // 0xff000000 + fetched colour word (kernel.cl:934)
+    float hx, hy, hz;  // raypos/16 (kernel.cl:920)
+    float dist;        // distance/16
+    uint64_t voxel;    // packed hit cell (bit 63 = hit)
+};
+
+__device__ __forceinline__ uint32_t load_word(const Octree& o, uint32_t i, uint32_t& fault) {
+    if (i < o.n_words) return __ldg(o.words + i);
+    fault |= kFaultFetch;
+    return 0u;
+}
+
+__device__ __forceinline__ uint32_t popc8(uint32_t v) { return __popc(v & 0xffu); }
+
+// fetchChildOffset (kernel.cl:32-62). At rekursion 1 the walk always stops
+// right after this call and never reads the returned word (kernel.cl:79 reads
+// the colour through the parent words), so that load is skipped.
+__device__ __forceinline__ uint32_t fetch_child(const Octree& o, uint32_t node, uint32_t before, uint32_t& local_root,
+                                                uint32_t child, uint32_t child_test, int rek, uint32_t& fault) {
+    uint32_t n = node >> 9;
+    if (node & 256u) {
+        if (!(before & 256u)) {
+            local_root = n << 6;
+            n = 0;
+        }
+        n += local_root;
+        const uint32_t nadd = __popc(node & ((child_test << 1) - 1u));
+        if (rek == 2) {
+            const uint32_t w = load_word(o, n + (nadd >> 2), fault);
+            return ((w >> ((nadd & 3u) << 3)) & 255u) + 256u + (nadd << 9);
+        }
+        if (rek == 1) return 0u;
+        return load_word(o, n + nadd, fault);
+    }
+    return load_word(o, n + child, fault);
+}
+
+// fetchColor (kernel.cl:64-112).
+__device__ __forceinline__ uint32_t fetch_colour(const Octree& o, uint32_t node, uint32_t before, uint32_t before2,
+                                                 uint32_t local_root, int rek, uint32_t child_test, uint32_t& fault) {
+    uint32_t n = node >> 9;
+    if (rek == 1) {
+        n = (before >> 9) & 15u;
+        const uint32_t ofs = (before2 >> 9) + local_root;
+        uint32_t nadd = popc8(before2);
+        for (uint32_t i = 1; i < n; ++i) nadd += popc8(load_word(o, ofs + (i >> 2), fault) >> ((i & 3u) << 3));
+        nadd += popc8(before & ((child_test << 1) - 1u));
+        return load_word(o, ofs + (nadd >> 2), fault) >> ((nadd & 3u) << 3);
+    }
+    uint32_t nadd = 8;
+    if (node & 256u) {
+        if (!(before & 256u)) {
+            local_root = n << 6;
+            n = 0;
+        }
+        nadd = local_root;
+        if (rek == 2) {
+            const uint32_t ofs = (before >> 9) + local_root;
+            nadd = 1u + popc8(before);
+            for (uint32_t i = 1; i < n; ++i) nadd += popc8(load_word(o, ofs + (i >> 2), fault) >> ((i & 3u) << 3));
+            return load_word(o, ofs + (nadd >> 2), fault) >> ((nadd & 3u) << 3);
+        }
+    }
+    return load_word(o, n + nadd, fault);
+}
+
+// Ray setup of raycast_fine_2/raycast_holes (kernel.cl:883-899) + CAST_RAY +
+// the colour fetch. `stk` points at this thread's column of the shared stack
+// (entry for level L at stk[L * stride]); levels 1..DEPTH-1 are used.
+template <int DEPTH, bool kVoxel>
+__device__ __forceinline__ RayResult trace_ray(const Octree& o, const RayCam& c, int idx, int idy, int res_x,
+                                               int res_y, uint32_t* stk, int stride, uint32_t& fault) {
+    constexpr int kScaleMax = 1 << (DEPTH + 1);
+    constexpr int kDepthAnd = (1 << DEPTH) - 1;
+    constexpr int kTopBit = 2 * kDepthAnd + 2;
+    const float fscale = (float)kScaleMax;
+
+    // delta1 = ((idx-res_x/2+0.5)*fovx/res_y, (idy-res_y/2+0.5)*fovy/res_y, 1)
+    const float d1x = __fdiv_rn(__fmul_rn(__fadd_rn((float)(idx - (res_x >> 1)), 0.5f), c.fovx), (float)res_y);
+    const float d1y = __fdiv_rn(__fmul_rn(__fadd_rn((float)(idy - (res_y >> 1)), 0.5f), c.fovy), (float)res_y);
+    // delta = (dot(delta1, mx), dot(delta1, my), dot(delta1, mz)), left to right
+    float dx = __fadd_rn(__fadd_rn(__fmul_rn(d1x, c.mxx), __fmul_rn(d1y, c.mxy)), c.mxz);
+    float dy = __fadd_rn(__fadd_rn(__fmul_rn(d1x, c.myx), __fmul_rn(d1y, c.myy)), c.myz);
+    float dz = __fadd_rn(__fadd_rn(__fmul_rn(d1x, c.mzx), __fmul_rn(d1y, c.mzy)), c.mzz);
+    float rpx = __fmul_rn(c.px, 16.0f), rpy = __fmul_rn(c.py, 16.0f), rpz = __fmul_rn(c.pz, 16.0f);
+
+    const float eps = 9.5367431640625e-07f;  // 2^-20, kernel.cl:118
+    if (fabsf(dx) < eps) dx = dx > 0.0f ? eps : (dx < 0.0f ? -eps : dx);
+    if (fabsf(dy) < eps) dy = dy > 0.0f ? eps : (dy < 0.0f ? -eps : dy);
+    if (fabsf(dz) < eps) dz = dz > 0.0f ? eps : (dz < 0.0f ? -eps : dz);
+    uint32_t sxyz = 0;
+    if (dx < 0.0f) { sxyz |= 1u; rpx = __fsub_rn(fscale, rpx); dx = -dx; }
+    if (dy < 0.0f) { sxyz |= 2u; rpy = __fsub_rn(fscale, rpy); dy = -dy; }
+    if (dz < 0.0f) { sxyz |= 4u; rpz = __fsub_rn(fscale, rpz); dz = -dz; }
+
+    const float g0y = __fdiv_rn(dy, dx), g0z = __fdiv_rn(dz, dx);
+    const float g1x = __fdiv_rn(dx, dy), g1z = __fdiv_rn(dz, dy);
+    const float g2x = __fdiv_rn(dx, dz), g2y = __fdiv_rn(dy, dz);
+    const float lx = __fsqrt_rn(__fadd_rn(__fadd_rn(1.0f, __fmul_rn(g0y, g0y)), __fmul_rn(g0z, g0z)));
+    const float ly = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(g1x, g1x), 1.0f), __fmul_rn(g1z, g1z)));
+    const float lz = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(g2x, g2x), __fmul_rn(g2y, g2y)), 1.0f));
+
+    int rix = __float2int_rz(rpx), riy = __float2int_rz(rpy), riz = __float2int_rz(rpz);
+    int rek = DEPTH, lod = 1;
+    float lodswitch = (float)(res_x * 2);  // res_x*LOD_ADJUST*2, kernel.cl:908
+    float distance = 0.0f;
+    const uint32_t root = o.root;
+    uint32_t nodeid = root, nodeid_before = root, local_root = 0, node_test = 0;
+    int x0ry = 0;
+    bool hit = false;
+    int hcx = 0, hcy = 0, hcz = 0;
+    uint32_t steps = 0;
+
+    for (;;) {
+        if (++steps > kStepCap) {
+            fault |= kFaultSteps;
+            break;
+        }
+        const int p0x = rix >> rek, p0y = riy >> rek, p0z = riz >> rek;
+        const uint32_t ni = ((uint32_t)(p0x & 1) | ((uint32_t)(p0y & 1) << 1) | ((uint32_t)(p0z & 1) << 2)) ^ sxyz;
+        node_test = nodeid & (1u << ni);
+        if (node_test) {
+            const uint32_t parent = nodeid;
+            nodeid = fetch_child(o, nodeid, nodeid_before, local_root, ni, node_test, rek, fault);
+            nodeid_before = parent;
+            if (rek <= lod) {
+                hit = true;
+                hcx = p0x;
+                hcy = p0y;
+                hcz = p0z;
+                break;
+            }
+            --rek;
+            stk[rek * stride] = nodeid;
+            continue;
+        }
+        // Distances to the three next cell planes; step along the nearest.
+        const float m0x = __fsub_rn((float)((p0x + 1) << rek), rpx);
+        const float m0y = __fsub_rn((float)((p0y + 1) << rek), rpy);
+        const float m0z = __fsub_rn((float)((p0z + 1) << rek), rpz);
+        float best = __fmul_rn(m0x, lx);
+        const float idy_ = __fmul_rn(m0y, ly), idz_ = __fmul_rn(m0z, lz);
+        float mm = m0x, gx = 1.0f, gy = g0y, gz = g0z;
+        if (idy_ < best) { best = idy_; mm = m0y; gx = g1x; gy = 1.0f; gz = g1z; }
+        if (idz_ < best) { best = idz_; mm = m0z; gx = g2x; gy = g2y; gz = 1.0f; }
+        rpx = __fadd_rn(rpx, __fmul_rn(gx, mm));
+        rpy = __fadd_rn(rpy, __fmul_rn(gy, mm));
+        rpz = __fadd_rn(rpz, __fmul_rn(gz, mm));
+        const int bx = rix, by = riy, bz = riz;
+        rix = __float2int_rz(rpx);
+        riy = __float2int_rz(rpy);
+        riz = __float2int_rz(rpz);
+        distance = __fadd_rn(distance, best);
+        x0ry = by ^ riy;
+        const uint32_t x0r = (uint32_t)(((bx ^ rix) ^ x0ry ^ (bz ^ riz)) & kDepthAnd);
+        const int rek_new = x0r ? 31 - __clz(x0r) : -1;
+        if (distance > kViewDistMax) break;
+        if (rek_new >= rek) {
+            rek = rek_new + 1;
+            if (rek >= DEPTH) {
+                nodeid = nodeid_before = root;
+            } else {
+                nodeid = stk[rek * stride];
+                nodeid_before = (rek + 1 >= DEPTH) ? root : stk[(rek + 1) * stride];
+            }
+            if (distance > lodswitch) {
+                lodswitch = __fmul_rn(lodswitch, 2.0f);
+                ++lod;
+            }
+        }
+        if (x0ry & kTopBit) break;
+    }
+
+    if (sxyz & 1u) rpx = __fsub_rn(fscale, rpx);
+    if (sxyz & 2u) rpy = __fsub_rn(fscale, rpy);
+    if (sxyz & 4u) rpz = __fsub_rn(fscale, rpz);
+    const uint32_t before2 = (rek + 1 >= DEPTH) ? root : stk[(rek + 1) * stride];
+    const uint32_t col = fetch_colour(o, nodeid, nodeid_before, before2, local_root, rek, node_test, fault);
+
+    RayResult r;
+    r.colour = 0xff000000u + col;
+    r.hx = __fdiv_rn(rpx, 16.0f);
+    r.hy = __fdiv_rn(rpy, 16.0f);
+    r.hz = __fdiv_rn(rpz, 16.0f);
+    r.dist = __fdiv_rn(distance, 16.0f);
+    r.voxel = 0;
+    if (kVoxel && hit) {
+        const uint32_t cells = (uint32_t)kScaleMax >> rek;
+        uint32_t cx = (uint32_t)hcx, cy = (uint32_t)hcy, cz = (uint32_t)hcz;
+        if (sxyz & 1u) cx = cells - 1u - cx;
+        if (sxyz & 2u) cy = cells - 1u - cy;
+        if (sxyz & 4u) cz = cells - 1u - cz;
+        cx &= cells - 1u;
+        cy &= cells - 1u;
+        cz &= cells - 1u;
+        r.voxel = (1ull << 63) | ((uint64_t)(uint32_t)rek << 48) | ((uint64_t)(((cz << rek) >> 1) & 0xffffu) << 32) |
+                  ((uint64_t)(((cy << rek) >> 1) & 0xffffu) << 16) | (uint64_t)(((cx << rek) >> 1) & 0xffffu);
+    }
+    return r;
+}
+
+// raycast_colorize (kernel.cl:944-974): material a&3 picks an RGB factor,
+// intensity a&248, BGRX8 out.
+__device__ __forceinline__ uint32_t colorize(uint32_t word) {
+    const int a = (int)word;
+    const int m = a & 3;
+    const float fr = m == 0 ? 1.0f : (m == 1 ? 1.0f : (m == 2 ? 1.5f : 0.2f));
+    const float fg = m == 0 ? 1.0f : (m == 1 ? 0.7f : (m == 2 ? 0.8f : 0.8f));
+    const float fb = m == 0 ? 1.0f : (m == 1 ? 0.3f : (m == 2 ? 0.1f : 0.2f));
+    const float i = (float)(a & (255 - 7));
+    int r = __float2int_rz(__fmul_rn(i, fr));
+    int g = __float2int_rz(__fmul_rn(i, fg));
+    int b = __float2int_rz(__fmul_rn(i, fb));
+    r = r > 255 ? 255 : r;
+    g = g > 255 ? 255 : g;
+    b = b > 255 ? 255 : b;
+    return (uint32_t)(b + g * 256 + r * 65536);
+}
+
+}  // namespace svo

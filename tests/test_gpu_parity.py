@@ -1,0 +1,66 @@
+"""GPU parity: the CUDA path against the CPU oracle, bit for bit.
+
+Colour words, hit positions (float bits), hit distances and hit voxels of the
+full raycast; every plane, the hole list and the BGRX image of warp frames.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _full_oracle(orc, octree, view):
+    return orc.raycast_full(octree.depth, octree.words, octree.root, view.pos_array, view.m_array, view.res_x,
+                            view.res_y, view.fovx, view.fovy)
+
+
+@pytest.mark.parametrize("depth,shell,kind,W,H,fov", [
+    (8, True, 0, 160, 120, 1.1547),
+    (9, True, 1, 256, 128, 1.0),
+    (8, False, 3, 200, 152, 1.0),
+    (9, False, 0, 512, 512, 1.1547),   # the plain full raycast configuration: 512^2, depth 9, solid terrain
+])
+def test_full_raycast_bit_exact(svo, orc, scene, gpu_ctx, depth, shell, kind, W, H, fov):
+    octree = scene(depth, 1234, shell)
+    gpu_ctx.upload(octree)
+    tgt = gpu_ctx.target(W, H)
+    view = svo.camera_path(kind, depth, 5, W, H, fov=fov)
+    gpu_ctx.raycast_full(tgt, view)
+    gpu_ctx.synchronize()
+    col, xyzw = tgt.full()
+    vox = tgt.voxels()
+    ocol, oxyzw, ovox, stats = _full_oracle(orc, octree, view)
+    assert np.array_equal(col, ocol), f"{int((col != ocol).sum())} colour words differ"
+    assert np.array_equal(xyzw.view(np.uint32), oxyzw.view(np.uint32)), "hit position/distance bits differ"
+    assert np.array_equal(vox, ovox), "hit voxels differ"
+    assert np.array_equal(tgt.bgrx(), orc.colorize(ocol))
+    tgt.close()
+
+
+@pytest.mark.parametrize("depth,shell,kind,W,H,frames", [
+    (8, True, 1, 128, 96, 40),    # covers a whole 8x4 refresh cycle
+    (9, True, 2, 200, 120, 12),   # ragged: 200x120 is not a multiple of 16
+    (8, False, 1, 96, 64, 6),
+])
+def test_warp_frames_bit_exact(svo, orc, scene, gpu_ctx, depth, shell, kind, W, H, frames):
+    octree = scene(depth, 99, shell)
+    gpu_ctx.upload(octree)
+    tgt = gpu_ctx.target(W, H)
+    warp = orc.Warp(depth, W, H)
+    for f in range(frames):
+        v = svo.camera_path(kind, depth, f, W, H)
+        gpu_ctx.warp_frame(tgt, v, f)
+        warp.frame(octree.words, octree.root, v.pos_array, v.m_array, f)
+        gpu_ctx.synchronize()
+        screen = warp.screen()
+        ids, count = tgt.holes()
+        assert count == warp.hole_count(), f"frame {f}: hole count"
+        assert np.array_equal(ids, warp.ids()), f"frame {f}: hole id buffer"
+        assert np.array_equal(tgt.colour(2), screen[2]), f"frame {f}: cache plane (pre-filter colours)"
+        assert np.array_equal(tgt.colour(0), screen[0]), f"frame {f}: displayed plane (after the filter)"
+        assert np.array_equal(tgt.bgrx(), warp.tex()), f"frame {f}: BGRX"
+        ne = screen[2] != svo.EMPTY_PIXEL
+        got = tgt.coords(2)[ne]
+        want = warp.back()[2][ne]
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), f"frame {f}: coordinate buffer"
+    tgt.close()
