@@ -1,0 +1,425 @@
+"""Benchmark: warped sparse-voxel-octree frames/s at 1920x1024 on GB300.
+
+Workload (one step = one warped frame, the body of the reference's
+raycast_draw): 1920x1024, depth-11 (2048^3) seeded fBm terrain octree (visible
+shell), orbit camera at 1.5x extent, 0.5 degrees yaw per frame, height
+sinusoid 0.02x extent over 64 frames. Reported beside it: the plain full
+raycast of the same frames on the same GPU (Mrays/s, frames/s), the warped
+image's PSNR against it, per-stage times and the trace kernel's roofline.
+
+Timing: each step is bracketed by CUDA events on the library's stream; the L2
+is flushed (256 MiB device write) before every timed step and outside its
+events. `value` = frames of all ranks / max over ranks of the summed step
+times. `e2e` times the C-ABI calls a user makes with host buffers: camera in,
+svo_warp_frame, BGRX8 image out to pinned host memory, per step.
+
+--impl reference times the reference algorithm on the host CPU cores instead
+(oracle/_ref when it was compiled from the reference tree here, else the
+oracle port of kernel.cl/raycast.h), with all host threads.
+
+Multi-GPU: replicas only (the per-frame pipeline does not shard); each rank
+renders its own camera path on its own GPU, scaling "weak".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "sparse-voxel-octree-raycasting_gb300"))
+
+METRIC = "Mrays/s; 1920x1024 frames/s warped+learned vs full raycast at ≥38 dB PSNR"
+WORKLOAD = "warped pipeline 1920x1024, depth-11 terrain octree, 256-frame orbit (0.5 deg/frame)"
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def parse_args(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=120)
+    ap.add_argument("--warmup", type=int, default=8)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--res", default="1920x1024")
+    ap.add_argument("--depth", type=int, default=11)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--cpu-frames", type=int, default=-1, help="oracle frames for the CPU baseline (-1: all)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (for profiling runs)")
+    ap.add_argument("--graph", type=int, default=1, help="replay each warp frame as a CUDA graph")
+    return ap.parse_args(argv)
+
+
+# ------------------------------------------------------------ distributed --
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def reduce_max(value: float, world: int, device=None) -> float:
+    """Max over ranks (identity for one rank)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate(frames_per_rank: int, seconds_per_rank: float, world: int, device=None) -> tuple[float, float]:
+    """(value, max seconds): all ranks' frames over the slowest rank's time."""
+    t = reduce_max(seconds_per_rank, world, device)
+    return frames_per_rank * world / t, t
+
+
+def barrier(world: int) -> None:
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+# ----------------------------------------------------------------- clocks --
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self.reader = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.reader = threading.Thread(target=self._read, daemon=True)
+        self.reader.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.reader:
+            self.reader.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    try:
+        with open(PEAKS_FILE) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+# ------------------------------------------------------------- reference --
+def run_reference(args, rank: int, world: int) -> None:
+    """Times the reference algorithm on the host cores (rank 0 only)."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    import svo_gb300 as svo
+
+    oracle.build()
+    W, H = (int(v) for v in args.res.split("x"))
+    which = "reference" if oracle.ref_available() else "oracle"
+    x, y, z, c = svo.terrain_voxels(args.seed, args.depth, True)
+    words, root = oracle.build_octree(args.depth, x, y, z, c, which=which)
+    del x, y, z, c
+    warp = oracle.Warp(args.depth, W, H, which=which)
+    threads = oracle.max_threads()
+    for f in range(args.warmup):
+        v = svo.camera_path(1, args.depth, f, W, H)
+        warp.frame(words, root, v.pos_array, v.m_array, f, threads)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        f = args.warmup + i
+        v = svo.camera_path(1, args.depth, f, W, H)
+        warp.frame(words, root, v.pos_array, v.m_array, f, threads)
+    dt = time.perf_counter() - t0
+    fps = args.steps / dt
+    cores = 1 if which == "reference" else threads
+    line = {
+        "impl": "reference", "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "res": [W, H], "depth": args.depth, "seed": args.seed},
+        "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores,
+                         "kind": "reference" if which == "reference" else "port",
+                         "sample": f"{args.steps} consecutive warped frames (after {args.warmup} untimed) of the "
+                                   f"benchmark path at {W}x{H}"},
+        "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------- ours --
+def run_ours(args, rank: int, world: int, local_rank: int) -> None:
+    import torch
+
+    import svo_gb300 as svo
+
+    torch.cuda.set_device(local_rank)
+    device = torch.device("cuda", local_rank)
+    W, H = (int(v) for v in args.res.split("x"))
+    depth = args.depth
+    t_build = time.perf_counter()
+    octree = svo.build_terrain(depth, args.seed, shell=True)
+    t_build = time.perf_counter() - t_build
+    ctx = svo.Context(local_rank)
+    ctx.upload(octree, validate=True)
+    tgt = ctx.target(W, H)
+    full = ctx.target(W, H)
+    if args.graph:
+        tgt.use_graph(True)
+    ext = torch.cuda.ExternalStream(ctx.stream, device=device)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+    frame_offset = rank * 512  # replicas render different stretches of the orbit
+
+    def view(f):
+        return svo.camera_path(1, depth, frame_offset + f, W, H)
+
+    def flush_l2():
+        flush.zero_()
+        torch.cuda.synchronize(device)
+
+    # ---- warped frames, device time per step
+    for f in range(args.warmup):
+        ctx.warp_frame(tgt, view(f), f)
+    ctx.synchronize()
+    barrier(world)
+    torch.cuda.synchronize(device)
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    launches0 = ctx.launch_count()
+    step_ms = []
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    for i in range(args.steps):
+        f = args.warmup + i
+        v = view(f)
+        flush_l2()
+        starts[i].record(ext)
+        ctx.warp_frame(tgt, v, f)
+        ends[i].record(ext)
+    ctx.synchronize()
+    launches = ctx.launch_count() - launches0
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    clock_info = clocks.stop()
+    barrier(world)
+    torch.cuda.synchronize(device)
+    warped_s = sum(step_ms) / 1000.0
+    value, t_max = aggregate(args.steps, warped_s, world, device if world > 1 else None)
+    ms_per_step = 1000.0 * warped_s / args.steps
+
+    # ---- the same frames with per-stage events (roofline and breakdown)
+    tgt2 = ctx.target(W, H)
+    if args.graph:
+        tgt2.use_graph(True)
+    tgt2.set_profiling(True)
+    for f in range(args.warmup):
+        ctx.warp_frame(tgt2, view(f), f)
+    ctx.synchronize()
+    stages = []
+    for i in range(args.steps):
+        f = args.warmup + i
+        flush_l2()
+        ctx.warp_frame(tgt2, view(f), f)
+        stages.append(tgt2.stage_times())
+    stages = np.array(stages, np.float64)
+    stage_names = ["project", "resolve_gather", "hole_scan", "hole_write", "trace", "fill_colorize"]
+    stage_ms = {n: float(stages[:, k].mean()) for k, n in enumerate(stage_names)}
+    tgt2.close()
+
+    # ---- plain full raycast of the same frames
+    full_ms = []
+    for i in range(args.steps):
+        f = args.warmup + i
+        v = view(f)
+        flush_l2()
+        s_ev, e_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s_ev.record(ext)
+        ctx.raycast_full(full, v)
+        e_ev.record(ext)
+        e_ev.synchronize()
+        full_ms.append(s_ev.elapsed_time(e_ev))
+    ctx.synchronize()
+    full_fps = 1000.0 / statistics.mean(full_ms)
+    mrays_full = W * H * full_fps / 1e6
+
+    # ---- end to end through the C ABI with host buffers
+    host_img = torch.empty(W * H, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+    tgt3 = ctx.target(W, H)
+    if args.graph:
+        tgt3.use_graph(True)
+    for f in range(args.warmup):
+        ctx.warp_frame(tgt3, view(f), f)
+        tgt3.bgrx_into(host_img)
+    e2e_s = 0.0
+    for i in range(args.steps):
+        f = args.warmup + i
+        flush_l2()
+        t0 = time.perf_counter()
+        ctx.warp_frame(tgt3, view(f), f)  # camera parameters travel host -> device inside the call
+        tgt3.bgrx_into(host_img)           # BGRX8 frame device -> pinned host, synchronising
+        e2e_s += time.perf_counter() - t0
+    e2e_value, _ = aggregate(args.steps, e2e_s, world, device if world > 1 else None)
+
+    # ---- quality: warped frames vs full raycast of the same cameras
+    psnr, traced_frac = [], []
+    tgt4 = ctx.target(W, H)
+    for f in range(args.warmup + args.steps):
+        v = view(f)
+        ctx.warp_frame(tgt4, v, f)
+        if f >= args.warmup:
+            ctx.raycast_full(full, v)
+            a = tgt4.bgrx()
+            b = full.bgrx()
+            psnr.append(svo.psnr_bgrx(a, b))
+            _, holes = tgt4.holes()
+            traced_frac.append(holes / (W * H))
+    tgt4.close()
+    psnr_mean = float(np.mean([p for p in psnr if np.isfinite(p)])) if psnr else None
+
+    # ---- CPU oracle on the same frames: parity of the last frame, fetch
+    # counts for the roofline's algorithmic bytes, and the CPU baseline.
+    cpu = None
+    algo_bytes_trace = None
+    parity = None
+    if not args.no_cpu and rank == 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        oracle.build()
+        threads = oracle.max_threads()
+        warp = oracle.Warp(depth, W, H)
+        n_cpu = args.steps if args.cpu_frames < 0 else min(args.cpu_frames, args.steps)
+        fetch_bytes = []
+        for f in range(args.warmup):
+            v = view(f)
+            warp.frame(octree.words, octree.root, v.pos_array, v.m_array, f, threads)
+        t0 = time.perf_counter()
+        for i in range(n_cpu):
+            f = args.warmup + i
+            v = view(f)
+            warp.frame(octree.words, octree.root, v.pos_array, v.m_array, f, threads)
+            st = warp.stats()  # rays, child fetches, colour fetches, boundary rays
+            holes = warp.hole_count()
+            # per traced ray: node words read + colour word + float4 store; per
+            # hole entry: its 4-byte id read
+            fetch_bytes.append(4.0 * (int(st[1]) + int(st[2])) + 20.0 * int(st[0]) + 4.0 * holes)
+        cpu_s = time.perf_counter() - t0
+        cpu = {"value": n_cpu / cpu_s, "unit": "frames/s", "cores": threads, "kind": "port",
+               "sample": f"{n_cpu} consecutive warped frames of the benchmark path at {W}x{H} "
+                         f"(after {args.warmup} untimed), oracle port of kernel.cl/raycast.h, OpenMP"}
+        algo_bytes_trace = float(np.mean(fetch_bytes))
+        if n_cpu == args.steps:
+            parity = bool(np.array_equal(warp.tex(), tgt.bgrx()))
+
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs")
+    roofline = None
+    if algo_bytes_trace is not None and stage_ms["trace"] > 0:
+        achieved = algo_bytes_trace / (stage_ms["trace"] * 1e-3) / 1e9
+        peak = hbm if hbm else 6800.0
+        roofline = {"bound": "hbm", "kernel": "k_trace_warp", "achieved": achieved, "peak": peak,
+                    "unit": "GB/s", "frac": achieved / peak,
+                    "peak_source": "measured" if hbm else "fallback",
+                    "algorithmic_bytes_per_launch": algo_bytes_trace, "traffic": None}
+    rays_per_frame = None
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded value-noise fBm terrain (visible shell), seeded orbit camera",
+            "config": {"workload": WORKLOAD, "res": [W, H], "depth": depth, "seed": args.seed,
+                       "octree_words": int(octree.words.size), "voxels": int(octree.voxels),
+                       "l2": "flushed before every timed step (256 MiB device write, outside the step events)",
+                       "cuda_graph": bool(args.graph), "replicas": world},
+            "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": 4 * 33,
+                    "d2h_bytes_per_step": 4 * W * H},
+            "gpu_launches": int(launches),
+            "clocks": clock_info,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "full_raycast": {"frames_per_s": full_fps, "mrays_per_s": mrays_full,
+                             "ms_per_frame": statistics.mean(full_ms)},
+            "speedup_vs_full": value / world / full_fps,
+            "psnr_db_vs_full": psnr_mean,
+            "hole_pixel_fraction": float(np.mean(traced_frac)) if traced_frac else None,
+            "stage_ms": stage_ms,
+            "parity_last_frame_vs_oracle": parity,
+            "octree_build_s": t_build,
+        }
+        print(json.dumps(line), flush=True)
+    for t in (tgt, full, tgt3):
+        t.close()
+    ctx.close()
+
+
+def main(argv=None):
+    args = parse_args(argv)
+    rank, world, local_rank = dist_env()
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local_rank)
+        dist.init_process_group(backend=backend)
+    try:
+        if args.impl == "reference":
+            run_reference(args, rank, world)
+        else:
+            run_ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()
