@@ -266,8 +266,10 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
         flush_l2()
         ctx.warp_frame(tgt2, view(f), f)
         stages.append(tgt2.stage_times())
-    stages = np.array(stages, np.float64)
     stage_names = ["project", "resolve_gather", "hole_scan", "hole_write", "trace", "fill_colorize"]
+    stages = np.array([s for s in stages if len(s) == len(stage_names)], np.float64)
+    if stages.size == 0:
+        raise RuntimeError("per-stage CUDA events returned no timings")
     stage_ms = {n: float(stages[:, k].mean()) for k, n in enumerate(stage_names)}
     tgt2.close()
 

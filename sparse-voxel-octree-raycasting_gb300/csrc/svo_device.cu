@@ -60,6 +60,7 @@ struct svo_target {
     cudaGraphExec_t graph_exec = nullptr;
     cudaGraphNode_t params_node = nullptr;
     bool graph_profiled = false;
+    bool capturing = false;
     // per-stage timing
     bool profiling = false;
     cudaEvent_t ev[8] = {};
@@ -233,8 +234,14 @@ svo_status launch_trace_warp(svo_context* ctx, svo_target* t) {
     return SVO_OK;
 }
 
+// Stage events. Inside a graph capture they must be recorded as external
+// event-record nodes, or they would only order work within the capture.
 void record(svo_target* t, int i) {
-    if (t->profiling) cudaEventRecord(t->ev[i], t->ctx->stream);
+    if (!t->profiling) return;
+    if (t->capturing)
+        cudaEventRecordWithFlags(t->ev[i], t->ctx->stream, cudaEventRecordExternal);
+    else
+        cudaEventRecord(t->ev[i], t->ctx->stream);
 }
 
 FrameParams make_params(const svo_target* t, const svo_view& v, int frame, int cur, bool have_cache) {
@@ -623,8 +630,10 @@ svo_status svo_warp_frame(svo_context* ctx, svo_target* t, const svo_view* view,
                 t->graph = nullptr;
             }
             SVO_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            t->capturing = true;
             k_set_params<<<1, 1, 0, s>>>(p, t->d_params, t->B.counters);
             st = enqueue_warp_body(ctx, t);
+            t->capturing = false;
             cudaGraph_t g = nullptr;
             cudaError_t ce = cudaStreamEndCapture(s, &g);
             if (st != SVO_OK) {

@@ -1,0 +1,190 @@
+"""GPU tests of the runtime around the kernels: batched views, CUDA-graph
+replay, stage timing, fault reporting, edge cases and the reference-named C++
+host interface."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _oracle_full(orc, octree, v):
+    return orc.raycast_full(octree.depth, octree.words, octree.root, v.pos_array, v.m_array, v.res_x, v.res_y,
+                            v.fovx, v.fovy)
+
+
+def test_batched_views_match_single_views(svo, orc, scene, gpu_ctx):
+    octree = scene(9, 77, True)
+    gpu_ctx.upload(octree)
+    sizes = [(64, 48), (200, 120), (33, 17), (128, 128), (320, 180), (8, 4), (1, 1)]
+    targets = [gpu_ctx.target(w, h) for w, h in sizes]
+    views = [svo.camera_path(3, 9, i, w, h, seed=5) for i, (w, h) in enumerate(sizes)]
+    gpu_ctx.raycast_full_batch(targets, views)
+    gpu_ctx.synchronize()
+    for t, v in zip(targets, views):
+        col, xyzw = t.full()
+        ocol, oxyzw, ovox, _ = _oracle_full(orc, octree, v)
+        assert np.array_equal(col, ocol)
+        assert np.array_equal(xyzw.view(np.uint32), oxyzw.view(np.uint32))
+        assert np.array_equal(t.voxels(), ovox)
+        t.close()
+
+
+def test_graph_replay_matches_direct_launches(svo, scene, gpu_ctx):
+    octree = scene(8, 99, True)
+    gpu_ctx.upload(octree)
+    a, b = gpu_ctx.target(160, 96), gpu_ctx.target(160, 96)
+    b.use_graph(True)
+    for f in range(20):
+        v = svo.camera_path(2, 8, f, 160, 96)
+        gpu_ctx.warp_frame(a, v, f)
+        gpu_ctx.warp_frame(b, v, f)
+        gpu_ctx.synchronize()
+        assert np.array_equal(a.colour(0), b.colour(0)), f
+        assert np.array_equal(a.colour(2), b.colour(2)), f
+        assert np.array_equal(a.holes()[0], b.holes()[0]), f
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_stage_timing(svo, scene, gpu_ctx, graph):
+    octree = scene(8, 99, True)
+    gpu_ctx.upload(octree)
+    t = gpu_ctx.target(256, 128)
+    t.use_graph(graph)
+    t.set_profiling(True)
+    for f in range(4):
+        gpu_ctx.warp_frame(t, svo.camera_path(1, 8, f, 256, 128), f)
+        ms = t.stage_times()
+        assert ms.size == 6 and np.all(ms >= 0) and ms.sum() > 0
+    gpu_ctx.raycast_full(t, svo.camera_path(1, 8, 0, 256, 128))
+    ms = t.stage_times()
+    assert ms[4] > 0
+    t.close()
+
+
+def test_launch_count_and_device_outputs(svo, scene, gpu_ctx):
+    octree = scene(8, 99, True)
+    gpu_ctx.upload(octree)
+    t = gpu_ctx.target(64, 64)
+    n0 = gpu_ctx.launch_count()
+    gpu_ctx.warp_frame(t, svo.camera_path(1, 8, 0, 64, 64), 0)
+    gpu_ctx.synchronize()
+    assert gpu_ctx.launch_count() - n0 == 7  # params, project, resolve, scan, write, trace, filter
+    d = t.device_outputs()
+    assert d.bgrx and d.colour and d.full_colour and d.full_xyzw and d.full_voxel
+    t.close()
+
+
+def test_bad_octree_is_rejected_by_validation(svo, gpu_ctx):
+    words = np.zeros(64, np.uint32)
+    words[0] = (1000 << 9) | 0xFF  # child pointers far past the end
+    with pytest.raises(svo.SvoError) as e:
+        gpu_ctx.upload(svo.Octree(words, root=0x1, depth=8), validate=True)
+    assert e.value.status == 4
+
+
+def test_bad_octree_raises_device_fault_and_context_survives(svo, orc, scene, gpu_ctx):
+    words = np.zeros(4096, np.uint32)
+    words[:8] = (0x7FFFF << 9) | 0xFF  # every root child points outside the array
+    gpu_ctx.upload(svo.Octree(words, root=0xFF, depth=8), validate=False)
+    t = gpu_ctx.target(64, 48)
+    gpu_ctx.raycast_full(t, svo.camera_path(0, 8, 0, 64, 48))
+    with pytest.raises(svo.SvoError) as e:
+        gpu_ctx.synchronize()
+    assert e.value.status == 5
+    # the flag is cleared and the context keeps working with a good octree
+    octree = scene(8, 99, True)
+    gpu_ctx.upload(octree)
+    v = svo.camera_path(0, 8, 0, 64, 48)
+    gpu_ctx.raycast_full(t, v)
+    gpu_ctx.synchronize()
+    col, _ = t.full()
+    assert np.array_equal(col, _oracle_full(orc, octree, v)[0])
+    t.close()
+
+
+def test_empty_and_single_voxel_scenes(svo, orc, gpu_ctx):
+    b = svo.Builder(8)
+    empty = b.finish()
+    b = svo.Builder(8)
+    b.set_voxel(128, 60, 128, 0x00AB_CDEF)
+    single = b.finish()
+    for octree in (empty, single):
+        gpu_ctx.upload(octree)
+        t = gpu_ctx.target(96, 96)
+        pos = np.array([8.0, 10.0, 6.0], np.float32)
+        v = svo.view_look_at(pos, [16.0, 3.75, 16.0], 96, 96)
+        gpu_ctx.raycast_full(t, v)
+        gpu_ctx.synchronize()
+        col, xyzw = t.full()
+        ocol, oxyzw, ovox, _ = _oracle_full(orc, octree, v)
+        assert np.array_equal(col, ocol) and np.array_equal(xyzw.view(np.uint32), oxyzw.view(np.uint32))
+        assert np.array_equal(t.voxels(), ovox)
+        if octree is empty:
+            assert np.all(col == 0xFF000000)
+        t.close()
+
+
+@pytest.mark.parametrize("W,H", [(1, 1), (7, 3), (17, 9), (9, 31)])
+def test_tiny_resolutions(svo, orc, scene, gpu_ctx, W, H):
+    octree = scene(8, 99, True)
+    gpu_ctx.upload(octree)
+    t = gpu_ctx.target(W, H)
+    v = svo.camera_path(3, 8, 3, W, H)
+    gpu_ctx.raycast_full(t, v)
+    gpu_ctx.synchronize()
+    col, xyzw = t.full()
+    ocol, oxyzw, _, _ = _oracle_full(orc, octree, v)
+    assert np.array_equal(col, ocol) and np.array_equal(xyzw.view(np.uint32), oxyzw.view(np.uint32))
+    t.close()
+
+
+def test_warp_argument_checks(svo, scene, gpu_ctx):
+    octree = scene(8, 99, True)
+    gpu_ctx.upload(octree)
+    t = gpu_ctx.target(15, 64)
+    with pytest.raises(svo.SvoError):
+        gpu_ctx.warp_frame(t, svo.camera_path(1, 8, 0, 15, 64), 0)
+    t.close()
+    t = gpu_ctx.target(64, 64)
+    with pytest.raises(svo.SvoError):
+        gpu_ctx.warp_frame(t, svo.camera_path(1, 8, 0, 64, 64, fov=1.2), 0)
+    with pytest.raises(svo.SvoError):
+        gpu_ctx.warp_frame(t, svo.camera_path(1, 8, 0, 32, 64), 0)
+    t.close()
+
+
+def test_warp_frame_numbers_start_anywhere(svo, orc, scene, gpu_ctx):
+    # A target with no previous frame behaves like the reference's cleared
+    # caches, whatever frame number the caller starts at.
+    octree = scene(8, 99, True)
+    gpu_ctx.upload(octree)
+    t = gpu_ctx.target(96, 64)
+    w = orc.Warp(8, 96, 64)
+    for i, f in enumerate([5, 6, 7, 40]):
+        v = svo.camera_path(1, 8, f, 96, 64)
+        gpu_ctx.warp_frame(t, v, f)
+        if i == 0:
+            # the oracle has no previous frame either: run it at a frame < 2 equivalent
+            w.frame(octree.words, octree.root, v.pos_array, v.m_array, 0)
+            gpu_ctx.synchronize()
+            assert np.array_equal(t.holes()[0][:2 * w.tiles], w.ids()[:2 * w.tiles])
+    t.close()
+
+
+def test_reference_named_cpp_interface(svo, tmp_path):
+    exe = str(tmp_path / "raycast_mirror")
+    lib_dir = os.path.join(ROOT, "sparse-voxel-octree-raycasting_gb300")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "raycast_mirror.cpp"), "-o", exe, "-L", lib_dir,
+                    "-lsvo_gb300", f"-Wl,-rpath,{lib_dir}"], check=True)
+    out = subprocess.run([exe, "6"], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    assert "frames=6" in out.stdout
+    nonblack = int(out.stdout.split("nonblack=")[1])
+    assert nonblack > 256 * 160 // 4
