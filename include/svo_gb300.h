@@ -97,8 +97,11 @@ svo_status svo_octree_upload(svo_context* ctx, const uint32_t* words, size_t n_w
  * upload or destroy). No validation. */
 svo_status svo_octree_upload_device(svo_context* ctx, const uint32_t* d_words, size_t n_words, uint32_t root_word,
                                     int depth);
-/* Size in bytes of the octree's upper (normal-node) region that the traversal
- * keeps in an L2 persisting window; 0 disables the window. */
+/* Bytes of the octree (from its start: the normal-node region first) kept in
+ * an L2 persisting access-policy window on the context stream, so node words
+ * stay resident across frames and other traffic. Default: the whole array,
+ * clamped to the device's maximum window and set-aside; 0 disables it and
+ * releases the set-aside. Applies to the current and later uploads. */
 svo_status svo_octree_set_l2_window(svo_context* ctx, size_t bytes);
 
 /* ------------------------------------------------------- render target -- */

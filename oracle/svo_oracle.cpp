@@ -602,16 +602,17 @@ void orc_octree_free(void* h) { delete static_cast<OrcOctree*>(h); }
 
 // raycast_fine_2 over the whole frame. Outputs per pixel: colour word, float4
 // (hit xyz, distance), packed hit cell and per-ray counters. Any output may be
-// null. stats[0..3] = rays, child fetches, colour fetches, boundary rays.
+// null. stats[0..5] = rays, child fetches, colour fetches, boundary rays,
+// loop iterations, longest walk (iterations).
 int orc_raycast_full(int depth, const uint32_t* words, size_t n_words, uint32_t root, const float* pos4,
                      const float* m16, int res_x, int res_y, float fovx, float fovy, uint32_t* colour, float* xyzw,
                      uint64_t* voxel, uint64_t* stats, int threads) {
     if (res_x <= 0 || res_y <= 0 || res_x > 65535 || res_y > 65535) return -1;
     Tracer tr{words, n_words, root, depth};
     View v = make_view(pos4, m16);
-    uint64_t child = 0, col = 0, bnd = 0;
+    uint64_t child = 0, col = 0, bnd = 0, steps = 0, max_steps = 0;
     if (threads > 0) omp_set_num_threads(threads);
-#pragma omp parallel for schedule(dynamic, 4) reduction(+ : child, col, bnd)
+#pragma omp parallel for schedule(dynamic, 4) reduction(+ : child, col, bnd, steps) reduction(max : max_steps)
     for (int y = 0; y < res_y; ++y)
         for (int x = 0; x < res_x; ++x) {
             Ray r = tr.trace(v, x, y, res_x, res_y, fovx, fovy);
@@ -627,12 +628,16 @@ int orc_raycast_full(int depth, const uint32_t* words, size_t n_words, uint32_t 
             child += r.child_fetches;
             col += r.colour_fetches;
             bnd += r.boundary ? 1 : 0;
+            steps += r.steps;
+            if (r.steps > max_steps) max_steps = r.steps;
         }
     if (stats) {
         stats[0] = (uint64_t)res_x * res_y;
         stats[1] = child;
         stats[2] = col;
         stats[3] = bnd;
+        stats[4] = steps;
+        stats[5] = max_steps;
     }
     return 0;
 }

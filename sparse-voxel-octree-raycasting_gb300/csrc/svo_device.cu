@@ -38,6 +38,7 @@ struct svo_context {
     int batch_slot = 0;
     uint32_t* d_counter = nullptr;
     size_t l2_window = 0;
+    size_t l2_window_request = ~(size_t)0;  // default: the whole octree
     uint64_t launches = 0;
     std::string err;
 };
@@ -341,6 +342,10 @@ svo_status svo_context_destroy(svo_context* ctx) {
     if (!ctx) return SVO_OK;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->l2_window > 0) {
+        cudaCtxResetPersistingL2Cache();
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
+    }
     if (ctx->owns_octree && ctx->d_octree) cudaFree(ctx->d_octree);
     if (ctx->d_fault) cudaFree(ctx->d_fault);
     if (ctx->d_counter) cudaFree(ctx->d_counter);
@@ -397,7 +402,9 @@ svo_status svo_octree_upload(svo_context* ctx, const uint32_t* words, size_t n_w
     ctx->n_words = n_words;
     ctx->root = root_word;
     ctx->depth = depth;
-    return SVO_OK;
+    // Keep the node words resident in L2 across frames (persisting window over
+    // the whole array, clamped to what the device allows).
+    return svo_octree_set_l2_window(ctx, ctx->l2_window_request);
 }
 
 svo_status svo_octree_upload_device(svo_context* ctx, const uint32_t* d_words, size_t n_words, uint32_t root_word,
@@ -411,18 +418,20 @@ svo_status svo_octree_upload_device(svo_context* ctx, const uint32_t* d_words, s
     ctx->n_words = n_words;
     ctx->root = root_word;
     ctx->depth = depth;
-    return SVO_OK;
+    return svo_octree_set_l2_window(ctx, ctx->l2_window_request);
 }
 
 svo_status svo_octree_set_l2_window(svo_context* ctx, size_t bytes) {
     if (!ctx) return SVO_ERR_INVALID_ARGUMENT;
-    if (!ctx->d_octree) return fail(ctx, SVO_ERR_NO_OCTREE, "set_l2_window");
+    ctx->l2_window_request = bytes;
+    if (!ctx->d_octree) return SVO_OK;  // applied at the next upload
     cudaStreamAttrValue attr;
     std::memset(&attr, 0, sizeof(attr));
+    int max_window = 0, max_persist = 0;
+    SVO_CUDA(ctx, cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, ctx->device));
+    SVO_CUDA(ctx, cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, ctx->device));
+    if (max_window <= 0 || max_persist <= 0) bytes = 0;  // no persisting L2 on this device
     if (bytes > 0) {
-        int max_window = 0, max_persist = 0;
-        SVO_CUDA(ctx, cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, ctx->device));
-        SVO_CUDA(ctx, cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, ctx->device));
         bytes = std::min(bytes, std::min(ctx->n_words * 4, (size_t)max_window));
         SVO_CUDA(ctx, cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, std::min(bytes, (size_t)max_persist)));
         attr.accessPolicyWindow.base_ptr = ctx->d_octree;
@@ -432,8 +441,9 @@ svo_status svo_octree_set_l2_window(svo_context* ctx, size_t bytes) {
         attr.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
     }
     SVO_CUDA(ctx, cudaStreamSetAttribute(ctx->stream, cudaStreamAttributeAccessPolicyWindow, &attr));
-    if (bytes == 0) {
+    if (bytes == 0 && ctx->l2_window > 0) {
         SVO_CUDA(ctx, cudaCtxResetPersistingL2Cache());
+        SVO_CUDA(ctx, cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0));
     }
     ctx->l2_window = bytes;
     return SVO_OK;

@@ -113,6 +113,122 @@ __device__ __forceinline__ uint32_t fetch_colour(const Octree& o, uint32_t node,
     return load_word(o, n + nadd, fault);
 }
 
+// Exact int<->float conversions on the FMA pipe for values in [0, 2^23):
+// float(v) = (2^23 + v as bits) - 2^23, and trunc(x) = bits(x + 2^23 rounded
+// toward zero) - bits(2^23). They replace the I2F/F2I instructions of the
+// stepping loop, which run on a narrow pipe and throttled the trace kernel.
+__device__ __forceinline__ float u23_to_float(int v) {
+    return __fsub_rn(__int_as_float(0x4B000000 | v), 8388608.0f);
+}
+__device__ __forceinline__ int trunc_u23(float x) {
+    return __float_as_int(__fadd_rz(x, 8388608.0f)) - 0x4B000000;
+}
+template <bool kFast>
+__device__ __forceinline__ float int_to_float(int v) {
+    return kFast ? u23_to_float(v) : (float)v;
+}
+template <bool kFast>
+__device__ __forceinline__ int float_to_int(float x) {
+    return kFast ? trunc_u23(x) : __float2int_rz(x);
+}
+
+struct Walk {
+    float rpx, rpy, rpz;
+    float distance;
+    uint32_t nodeid, nodeid_before, local_root, node_test;
+    int rek;
+    bool hit;
+    int hcx, hcy, hcz;
+};
+
+// CAST_RAY's loop (kernel.cl:152-211). kFast: every coordinate of the walk
+// stays in [0, 2^23), checked by the caller from the mirrored start point
+// (each step moves a coordinate by at most the distance it adds, and the walk
+// stops once the distance passes VIEW_DIST_MAX).
+template <int DEPTH, bool kFast>
+__device__ __forceinline__ void walk(const Octree& o, Walk& w, uint32_t sxyz, float g0y, float g0z, float g1x,
+                                     float g1z, float g2x, float g2y, float lx, float ly, float lz, float lodswitch,
+                                     uint32_t* stk, int stride, uint32_t& fault) {
+    constexpr int kDepthAnd = (1 << DEPTH) - 1;
+    constexpr int kTopBit = 2 * kDepthAnd + 2;
+    float rpx = w.rpx, rpy = w.rpy, rpz = w.rpz;
+    int rix = float_to_int<kFast>(rpx), riy = float_to_int<kFast>(rpy), riz = float_to_int<kFast>(rpz);
+    int rek = DEPTH, lod = 1;
+    float distance = 0.0f;
+    const uint32_t root = o.root;
+    uint32_t nodeid = root, nodeid_before = root, local_root = 0, node_test = 0;
+    uint32_t steps = 0;
+    for (;;) {
+        if (++steps > kStepCap) {
+            fault |= kFaultSteps;
+            break;
+        }
+        const int p0x = rix >> rek, p0y = riy >> rek, p0z = riz >> rek;
+        const uint32_t ni = ((uint32_t)(p0x & 1) | ((uint32_t)(p0y & 1) << 1) | ((uint32_t)(p0z & 1) << 2)) ^ sxyz;
+        node_test = nodeid & (1u << ni);
+        if (node_test) {
+            const uint32_t parent = nodeid;
+            nodeid = fetch_child(o, nodeid, nodeid_before, local_root, ni, node_test, rek, fault);
+            nodeid_before = parent;
+            if (rek <= lod) {
+                w.hit = true;
+                w.hcx = p0x;
+                w.hcy = p0y;
+                w.hcz = p0z;
+                break;
+            }
+            --rek;
+            stk[rek * stride] = nodeid;
+            continue;
+        }
+        // Distances to the three next cell planes; step along the nearest.
+        const float m0x = __fsub_rn(int_to_float<kFast>((p0x + 1) << rek), rpx);
+        const float m0y = __fsub_rn(int_to_float<kFast>((p0y + 1) << rek), rpy);
+        const float m0z = __fsub_rn(int_to_float<kFast>((p0z + 1) << rek), rpz);
+        float best = __fmul_rn(m0x, lx);
+        const float idy_ = __fmul_rn(m0y, ly), idz_ = __fmul_rn(m0z, lz);
+        float mm = m0x, gx = 1.0f, gy = g0y, gz = g0z;
+        if (idy_ < best) { best = idy_; mm = m0y; gx = g1x; gy = 1.0f; gz = g1z; }
+        if (idz_ < best) { best = idz_; mm = m0z; gx = g2x; gy = g2y; gz = 1.0f; }
+        rpx = __fadd_rn(rpx, __fmul_rn(gx, mm));
+        rpy = __fadd_rn(rpy, __fmul_rn(gy, mm));
+        rpz = __fadd_rn(rpz, __fmul_rn(gz, mm));
+        const int bx = rix, by = riy, bz = riz;
+        rix = float_to_int<kFast>(rpx);
+        riy = float_to_int<kFast>(rpy);
+        riz = float_to_int<kFast>(rpz);
+        distance = __fadd_rn(distance, best);
+        const int x0ry = by ^ riy;
+        const uint32_t x0r = (uint32_t)(((bx ^ rix) ^ x0ry ^ (bz ^ riz)) & kDepthAnd);
+        if (distance > kViewDistMax) break;
+        // log2(x0r) >= rek <=> some bit at or above rek changed: pop to the
+        // level above the highest changed bit.
+        if (x0r >> rek) {
+            rek = 32 - __clz(x0r);
+            if (rek >= DEPTH) {
+                nodeid = nodeid_before = root;
+            } else {
+                nodeid = stk[rek * stride];
+                nodeid_before = (rek + 1 >= DEPTH) ? root : stk[(rek + 1) * stride];
+            }
+            if (distance > lodswitch) {
+                lodswitch = __fmul_rn(lodswitch, 2.0f);
+                ++lod;
+            }
+        }
+        if (x0ry & kTopBit) break;
+    }
+    w.rpx = rpx;
+    w.rpy = rpy;
+    w.rpz = rpz;
+    w.distance = distance;
+    w.nodeid = nodeid;
+    w.nodeid_before = nodeid_before;
+    w.local_root = local_root;
+    w.node_test = node_test;
+    w.rek = rek;
+}
+
 // Ray setup of raycast_fine_2/raycast_holes (kernel.cl:883-899) + CAST_RAY +
 // the colour fetch. `stk` points at this thread's column of the shared stack
 // (entry for level L at stk[L * stride]); levels 1..DEPTH-1 are used.
@@ -120,8 +236,6 @@ template <int DEPTH, bool kVoxel>
 __device__ __forceinline__ RayResult trace_ray(const Octree& o, const RayCam& c, int idx, int idy, int res_x,
                                                int res_y, uint32_t* stk, int stride, uint32_t& fault) {
     constexpr int kScaleMax = 1 << (DEPTH + 1);
-    constexpr int kDepthAnd = (1 << DEPTH) - 1;
-    constexpr int kTopBit = 2 * kDepthAnd + 2;
     const float fscale = (float)kScaleMax;
 
     // delta1 = ((idx-res_x/2+0.5)*fovx/res_y, (idy-res_y/2+0.5)*fovy/res_y, 1)
@@ -148,94 +262,42 @@ __device__ __forceinline__ RayResult trace_ray(const Octree& o, const RayCam& c,
     const float lx = __fsqrt_rn(__fadd_rn(__fadd_rn(1.0f, __fmul_rn(g0y, g0y)), __fmul_rn(g0z, g0z)));
     const float ly = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(g1x, g1x), 1.0f), __fmul_rn(g1z, g1z)));
     const float lz = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(g2x, g2x), __fmul_rn(g2y, g2y)), 1.0f));
+    const float lodswitch = (float)(res_x * 2);  // res_x*LOD_ADJUST*2, kernel.cl:908
 
-    int rix = __float2int_rz(rpx), riy = __float2int_rz(rpy), riz = __float2int_rz(rpz);
-    int rek = DEPTH, lod = 1;
-    float lodswitch = (float)(res_x * 2);  // res_x*LOD_ADJUST*2, kernel.cl:908
-    float distance = 0.0f;
-    const uint32_t root = o.root;
-    uint32_t nodeid = root, nodeid_before = root, local_root = 0, node_test = 0;
-    int x0ry = 0;
-    bool hit = false;
-    int hcx = 0, hcy = 0, hcz = 0;
-    uint32_t steps = 0;
-
-    for (;;) {
-        if (++steps > kStepCap) {
-            fault |= kFaultSteps;
-            break;
-        }
-        const int p0x = rix >> rek, p0y = riy >> rek, p0z = riz >> rek;
-        const uint32_t ni = ((uint32_t)(p0x & 1) | ((uint32_t)(p0y & 1) << 1) | ((uint32_t)(p0z & 1) << 2)) ^ sxyz;
-        node_test = nodeid & (1u << ni);
-        if (node_test) {
-            const uint32_t parent = nodeid;
-            nodeid = fetch_child(o, nodeid, nodeid_before, local_root, ni, node_test, rek, fault);
-            nodeid_before = parent;
-            if (rek <= lod) {
-                hit = true;
-                hcx = p0x;
-                hcy = p0y;
-                hcz = p0z;
-                break;
-            }
-            --rek;
-            stk[rek * stride] = nodeid;
-            continue;
-        }
-        // Distances to the three next cell planes; step along the nearest.
-        const float m0x = __fsub_rn((float)((p0x + 1) << rek), rpx);
-        const float m0y = __fsub_rn((float)((p0y + 1) << rek), rpy);
-        const float m0z = __fsub_rn((float)((p0z + 1) << rek), rpz);
-        float best = __fmul_rn(m0x, lx);
-        const float idy_ = __fmul_rn(m0y, ly), idz_ = __fmul_rn(m0z, lz);
-        float mm = m0x, gx = 1.0f, gy = g0y, gz = g0z;
-        if (idy_ < best) { best = idy_; mm = m0y; gx = g1x; gy = 1.0f; gz = g1z; }
-        if (idz_ < best) { best = idz_; mm = m0z; gx = g2x; gy = g2y; gz = 1.0f; }
-        rpx = __fadd_rn(rpx, __fmul_rn(gx, mm));
-        rpy = __fadd_rn(rpy, __fmul_rn(gy, mm));
-        rpz = __fadd_rn(rpz, __fmul_rn(gz, mm));
-        const int bx = rix, by = riy, bz = riz;
-        rix = __float2int_rz(rpx);
-        riy = __float2int_rz(rpy);
-        riz = __float2int_rz(rpz);
-        distance = __fadd_rn(distance, best);
-        x0ry = by ^ riy;
-        const uint32_t x0r = (uint32_t)(((bx ^ rix) ^ x0ry ^ (bz ^ riz)) & kDepthAnd);
-        const int rek_new = x0r ? 31 - __clz(x0r) : -1;
-        if (distance > kViewDistMax) break;
-        if (rek_new >= rek) {
-            rek = rek_new + 1;
-            if (rek >= DEPTH) {
-                nodeid = nodeid_before = root;
-            } else {
-                nodeid = stk[rek * stride];
-                nodeid_before = (rek + 1 >= DEPTH) ? root : stk[(rek + 1) * stride];
-            }
-            if (distance > lodswitch) {
-                lodswitch = __fmul_rn(lodswitch, 2.0f);
-                ++lod;
-            }
-        }
-        if (x0ry & kTopBit) break;
-    }
+    Walk w;
+    w.rpx = rpx;
+    w.rpy = rpy;
+    w.rpz = rpz;
+    w.hit = false;
+    w.hcx = w.hcy = w.hcz = 0;
+    const float lim = 4194304.0f;  // 2^22
+    const bool fast = rpx >= 0.0f && rpx < lim && rpy >= 0.0f && rpy < lim && rpz >= 0.0f && rpz < lim;
+    if (fast)
+        walk<DEPTH, true>(o, w, sxyz, g0y, g0z, g1x, g1z, g2x, g2y, lx, ly, lz, lodswitch, stk, stride, fault);
+    else
+        walk<DEPTH, false>(o, w, sxyz, g0y, g0z, g1x, g1z, g2x, g2y, lx, ly, lz, lodswitch, stk, stride, fault);
+    rpx = w.rpx;
+    rpy = w.rpy;
+    rpz = w.rpz;
+    const int rek = w.rek;
 
     if (sxyz & 1u) rpx = __fsub_rn(fscale, rpx);
     if (sxyz & 2u) rpy = __fsub_rn(fscale, rpy);
     if (sxyz & 4u) rpz = __fsub_rn(fscale, rpz);
-    const uint32_t before2 = (rek + 1 >= DEPTH) ? root : stk[(rek + 1) * stride];
-    const uint32_t col = fetch_colour(o, nodeid, nodeid_before, before2, local_root, rek, node_test, fault);
+    const uint32_t before2 = (rek + 1 >= DEPTH) ? o.root : stk[(rek + 1) * stride];
+    const uint32_t col = fetch_colour(o, w.nodeid, w.nodeid_before, before2, w.local_root, rek, w.node_test, fault);
 
     RayResult r;
     r.colour = 0xff000000u + col;
-    r.hx = __fdiv_rn(rpx, 16.0f);
-    r.hy = __fdiv_rn(rpy, 16.0f);
-    r.hz = __fdiv_rn(rpz, 16.0f);
-    r.dist = __fdiv_rn(distance, 16.0f);
+    // x/16 is exact as x*0.0625 (a power-of-two scale)
+    r.hx = __fmul_rn(rpx, 0.0625f);
+    r.hy = __fmul_rn(rpy, 0.0625f);
+    r.hz = __fmul_rn(rpz, 0.0625f);
+    r.dist = __fmul_rn(w.distance, 0.0625f);
     r.voxel = 0;
-    if (kVoxel && hit) {
+    if (kVoxel && w.hit) {
         const uint32_t cells = (uint32_t)kScaleMax >> rek;
-        uint32_t cx = (uint32_t)hcx, cy = (uint32_t)hcy, cz = (uint32_t)hcz;
+        uint32_t cx = (uint32_t)w.hcx, cy = (uint32_t)w.hcy, cz = (uint32_t)w.hcz;
         if (sxyz & 1u) cx = cells - 1u - cx;
         if (sxyz & 2u) cy = cells - 1u - cy;
         if (sxyz & 4u) cz = cells - 1u - cz;
