@@ -83,6 +83,13 @@ svo_status svo_synchronize(svo_context* ctx);
 /* Number of kernels this context has launched since creation. */
 uint64_t svo_launch_count(const svo_context* ctx);
 
+/* Tuning switches of the trace kernels (no counterpart in the reference).
+ * SVO_OPT_STAGE_NODES: 1 (default) copies the octree's normal-node region into
+ * each trace block's shared memory (when it fits, <= 160 KiB); 0 reads every
+ * node word from global memory. */
+#define SVO_OPT_STAGE_NODES 1
+svo_status svo_context_set_option(svo_context* ctx, int option, int64_t value);
+
 /* ------------------------------------------------------------ octree -- */
 
 /* Replaces ocl_malloc(size, &octree_array_compact[0]) of src/raycast.h:68

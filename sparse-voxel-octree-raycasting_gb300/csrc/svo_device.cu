@@ -39,6 +39,7 @@ struct svo_context {
     uint32_t* d_counter = nullptr;
     size_t l2_window = 0;
     size_t l2_window_request = ~(size_t)0;  // default: the whole octree
+    bool stage_normal = true;               // stage the normal-node region in shared memory
     uint64_t launches = 0;
     std::string err;
 };
@@ -185,58 +186,98 @@ struct Validator {
     }
 };
 
-template <int DEPTH>
-const void* trace_full_fn(bool vox) {
-    return vox ? (const void*)k_trace_full<DEPTH, true> : (const void*)k_trace_full<DEPTH, false>;
+// Launch geometry of the trace kernels. The normal-node region (words
+// [0, (root>>9)+10), written first by convert_tree_blocks) is staged into
+// shared memory when it fits: 256-thread blocks for a small region, 1024-thread
+// blocks (one per SM, 32 warps) for a large one; otherwise no staging.
+constexpr uint32_t kStageSmallBytes = 48u * 1024u;
+constexpr uint32_t kStageMaxBytes = 160u * 1024u;
+
+struct TraceLaunch {
+    const void* fn;
+    int block;
+    size_t smem;
+    Octree o;
+};
+
+template <int DEPTH, int BLOCK>
+const void* trace_fn(bool warp) {
+    return warp ? (const void*)k_trace_warp<DEPTH, BLOCK> : (const void*)k_trace_full<DEPTH, BLOCK, true>;
 }
 
-svo_status launch_trace_full(svo_context* ctx, FullBatch* d_batch, bool vox) {
-    Octree o{ctx->d_octree, (uint32_t)ctx->n_words, ctx->root};
-    const void* fn = nullptr;
-    switch (ctx->depth) {
-        case 8: fn = trace_full_fn<8>(vox); break;
-        case 9: fn = trace_full_fn<9>(vox); break;
-        case 10: fn = trace_full_fn<10>(vox); break;
-        case 11: fn = trace_full_fn<11>(vox); break;
-        case 12: fn = trace_full_fn<12>(vox); break;
-        default: return fail(ctx, SVO_ERR_NOT_SUPPORTED, "octree depth");
+template <int BLOCK>
+const void* trace_fn_depth(int depth, bool warp) {
+    switch (depth) {
+        case 8: return trace_fn<8, BLOCK>(warp);
+        case 9: return trace_fn<9, BLOCK>(warp);
+        case 10: return trace_fn<10, BLOCK>(warp);
+        case 11: return trace_fn<11, BLOCK>(warp);
+        case 12: return trace_fn<12, BLOCK>(warp);
     }
+    return nullptr;
+}
+
+svo_status plan_trace(svo_context* ctx, bool warp, TraceLaunch& L) {
+    L.o = Octree{ctx->d_octree, (uint32_t)ctx->n_words, ctx->root, 0u, 0u};
+    uint32_t stage_bytes = 0;
+    if (ctx->stage_normal && !(ctx->root & 256u) && (reinterpret_cast<uintptr_t>(ctx->d_octree) & 15u) == 0) {
+        const uint64_t nw = (uint64_t)(ctx->root >> 9) + 10u;
+        const uint64_t bytes = (nw * 4u + 15u) & ~15ull;
+        if (bytes <= kStageMaxBytes && bytes <= (uint64_t)ctx->n_words * 4u) {
+            L.o.n_smem = (uint32_t)nw;
+            stage_bytes = (uint32_t)bytes;
+        }
+    }
+    L.block = stage_bytes > kStageSmallBytes ? 1024 : 256;
+    L.fn = L.block == 1024 ? trace_fn_depth<1024>(ctx->depth, warp) : trace_fn_depth<256>(ctx->depth, warp);
+    if (!L.fn) return fail(ctx, SVO_ERR_NOT_SUPPORTED, "octree depth");
+    L.smem = (size_t)(ctx->depth + 1) * L.block * 4u + stage_bytes;
+    SVO_CUDA(ctx, cudaFuncSetAttribute(L.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
+    return SVO_OK;
+}
+
+// Persistent grid: as many blocks as fit on every SM; the access-policy
+// window travels with the launch so graph-captured launches keep it.
+svo_status launch_trace(svo_context* ctx, const TraceLaunch& L, void** args) {
     int per_sm = 0;
-    SVO_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kTraceBlock, 0));
-    const int grid = std::max(1, per_sm) * ctx->sm_count;
-    void* args[] = {&o, &d_batch, &ctx->d_counter, &ctx->d_fault};
-    SVO_CUDA(ctx, cudaLaunchKernel(fn, dim3(grid), dim3(kTraceBlock), args, 0, ctx->stream));
+    SVO_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, L.fn, L.block, L.smem));
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)(std::max(1, per_sm) * ctx->sm_count));
+    cfg.blockDim = dim3((unsigned)L.block);
+    cfg.dynamicSmemBytes = L.smem;
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute attr[1];
+    if (ctx->l2_window > 0) {
+        attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
+        attr[0].val.accessPolicyWindow.base_ptr = ctx->d_octree;
+        attr[0].val.accessPolicyWindow.num_bytes = ctx->l2_window;
+        attr[0].val.accessPolicyWindow.hitRatio = 1.0f;
+        attr[0].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+        attr[0].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+    }
+    SVO_CUDA(ctx, cudaLaunchKernelExC(&cfg, L.fn, args));
     ++ctx->launches;
     return SVO_OK;
 }
 
-template <int DEPTH>
-const void* trace_warp_fn() {
-    return (const void*)k_trace_warp<DEPTH>;
+svo_status launch_trace_full(svo_context* ctx, FullBatch* d_batch) {
+    TraceLaunch L;
+    svo_status st = plan_trace(ctx, false, L);
+    if (st != SVO_OK) return st;
+    void* args[] = {&L.o, &d_batch, &ctx->d_counter, &ctx->d_fault};
+    return launch_trace(ctx, L, args);
 }
 
 svo_status launch_trace_warp(svo_context* ctx, svo_target* t) {
-    Octree o{ctx->d_octree, (uint32_t)ctx->n_words, ctx->root};
-    const void* fn = nullptr;
-    switch (ctx->depth) {
-        case 8: fn = trace_warp_fn<8>(); break;
-        case 9: fn = trace_warp_fn<9>(); break;
-        case 10: fn = trace_warp_fn<10>(); break;
-        case 11: fn = trace_warp_fn<11>(); break;
-        case 12: fn = trace_warp_fn<12>(); break;
-        default: return fail(ctx, SVO_ERR_NOT_SUPPORTED, "octree depth");
-    }
-    int per_sm = 0;
-    SVO_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kTraceBlock, 0));
-    const int grid = std::max(1, per_sm) * ctx->sm_count;
-    void* args[] = {&o, &t->d_params, &t->B, &ctx->d_fault};
-    SVO_CUDA(ctx, cudaLaunchKernel(fn, dim3(grid), dim3(kTraceBlock), args, 0, ctx->stream));
-    ++ctx->launches;
-    return SVO_OK;
+    TraceLaunch L;
+    svo_status st = plan_trace(ctx, true, L);
+    if (st != SVO_OK) return st;
+    void* args[] = {&L.o, &t->d_params, &t->B, &ctx->d_fault};
+    return launch_trace(ctx, L, args);
 }
 
-// Stage events. Inside a graph capture they must be recorded as external
-// event-record nodes, or they would only order work within the capture.
 void record(svo_target* t, int i) {
     if (!t->profiling) return;
     if (t->capturing)
@@ -365,6 +406,17 @@ void* svo_context_stream(svo_context* ctx) { return ctx ? (void*)ctx->stream : n
 
 uint64_t svo_launch_count(const svo_context* ctx) { return ctx ? ctx->launches : 0; }
 
+svo_status svo_context_set_option(svo_context* ctx, int option, int64_t value) {
+    if (!ctx) return SVO_ERR_INVALID_ARGUMENT;
+    switch (option) {
+        case SVO_OPT_STAGE_NODES:
+            ctx->stage_normal = value != 0;
+            return SVO_OK;
+        default:
+            return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "unknown option");
+    }
+}
+
 svo_status svo_synchronize(svo_context* ctx) {
     if (!ctx) return SVO_ERR_INVALID_ARGUMENT;
     SVO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -374,7 +426,7 @@ svo_status svo_synchronize(svo_context* ctx) {
         SVO_CUDA(ctx, cudaMemset(ctx->d_fault, 0, sizeof(uint32_t)));
         char buf[160];
         std::snprintf(buf, sizeof(buf), "fault flags 0x%x (1: node fetch out of range, 2: ray step limit, "
-                      "4: hole entry outside the frame)", f);
+                      "4: hole entry outside the frame, 8: node staging copy timed out)", f);
         return fail(ctx, SVO_ERR_DEVICE_FAULT, buf);
     }
     return SVO_OK;
@@ -602,7 +654,7 @@ svo_status svo_raycast_full_batch(svo_context* ctx, svo_target* const* targets, 
     SVO_CUDA(ctx, cudaMemcpyAsync(ctx->d_batch[slot], hb, bytes, cudaMemcpyHostToDevice, ctx->stream));
     k_reset_counter<<<1, 1, 0, ctx->stream>>>(ctx->d_counter);
     SVO_LAUNCHED(ctx);
-    svo_status st = launch_trace_full(ctx, ctx->d_batch[slot], true);
+    svo_status st = launch_trace_full(ctx, ctx->d_batch[slot]);
     SVO_CUDA(ctx, cudaEventRecord(ctx->batch_done[slot], ctx->stream));
     if (st != SVO_OK) return st;
     if (t0->profiling) {

@@ -25,7 +25,6 @@
 namespace svo {
 
 constexpr uint64_t kKeyEmpty = ~0ull;
-constexpr int kTraceBlock = 128;
 constexpr int kMaxBatchViews = 256;
 
 // Everything one warp frame needs, written to device memory by k_set_params
@@ -264,13 +263,33 @@ __global__ void __launch_bounds__(256) k_hole_write(TargetBuffers B) {
 // consecutive entries = eight neighbouring 2x2 blocks), then the 8x4 tiles of
 // the refresh rectangle; holes inside the rectangle are left to it (both
 // would store identical values).
-template <int DEPTH, bool kVoxel>
-__global__ void __launch_bounds__(kTraceBlock) k_trace_full(Octree o, const FullBatch* __restrict__ batch,
-                                                          uint32_t* counter, uint32_t* fault_out) {
-    __shared__ uint32_t stack[(DEPTH + 1) * kTraceBlock];
+//
+// Shared memory: the node stack, then (when o.n_smem > 0) a copy of the
+// octree's normal-node region, staged once per block by stage_prefix. The
+// longest rays of a frame -- horizon rays skimming the periodic terrain up to
+// VIEW_DIST_MAX -- fetch nothing else, ~1000 dependent fetches each, so
+// their latency (the kernel's tail) drops from L2-hit to shared-memory
+// latency per fetch.
+template <int DEPTH, int BLOCK>
+__device__ __forceinline__ Octree stage_octree(Octree o, uint64_t* mbar, uint32_t& fault, bool& staged) {
+    staged = false;
+    if (o.n_smem > 0) {
+        o.smem_base = (DEPTH + 1) * BLOCK;
+        staged = stage_prefix(o.words, o.n_smem, o.smem_base, mbar, fault);
+        if (!staged) o.n_smem = 0;
+    }
+    return o;
+}
+
+template <int DEPTH, int BLOCK, bool kVoxel>
+__global__ void __launch_bounds__(BLOCK) k_trace_full(Octree o_in, const FullBatch* __restrict__ batch,
+                                                    uint32_t* counter, uint32_t* fault_out) {
+    __shared__ uint64_t mbar;
     const int lane = threadIdx.x & 31;
-    uint32_t* stk = stack + threadIdx.x;
+    uint32_t* stk = svo_dsmem + threadIdx.x;
     uint32_t fault = 0;
+    bool staged;
+    const Octree o = stage_octree<DEPTH, BLOCK>(o_in, &mbar, fault, staged);
     const uint32_t total = batch->total_packets;
     const int nv = batch->n_views;
     for (;;) {
@@ -293,7 +312,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_full(Octree o, const Full
         const int y = (int)(q / (uint32_t)fv.packets_x) * 4 + (lane >> 3);
         if (x < fv.res_x && y < fv.res_y) {
             const RayCam cam = fv.ray;
-            const RayResult r = trace_ray<DEPTH, kVoxel>(o, cam, x, y, fv.res_x, fv.res_y, stk, kTraceBlock, fault);
+            const RayResult r = trace_ray<DEPTH, kVoxel>(o, cam, x, y, fv.res_x, fv.res_y, stk, BLOCK, fault);
             const size_t ofs = (size_t)y * fv.res_x + x;
             fv.col[ofs] = r.colour;
             fv.xyzw[ofs] = make_float4(r.hx, r.hy, r.hz, r.dist);
@@ -301,16 +320,19 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_full(Octree o, const Full
             fv.bgrx[ofs] = colorize(r.colour);
         }
     }
+    if (o_in.n_smem > 0 && !staged) stage_drain(&mbar);
     if (fault) atomicOr(fault_out, fault);
 }
 
-template <int DEPTH>
-__global__ void __launch_bounds__(kTraceBlock) k_trace_warp(Octree o, const FrameParams* __restrict__ P,
-                                                          TargetBuffers B, uint32_t* fault_out) {
-    __shared__ uint32_t stack[(DEPTH + 1) * kTraceBlock];
+template <int DEPTH, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FrameParams* __restrict__ P,
+                                                    TargetBuffers B, uint32_t* fault_out) {
+    __shared__ uint64_t mbar;
     const int lane = threadIdx.x & 31;
-    uint32_t* stk = stack + threadIdx.x;
+    uint32_t* stk = svo_dsmem + threadIdx.x;
     uint32_t fault = 0;
+    bool staged;
+    const Octree o = stage_octree<DEPTH, BLOCK>(o_in, &mbar, fault, staged);
     const int res_x = B.res_x, res_y = B.res_y;
     const uint32_t tiles = (uint32_t)B.tiles_x * (uint32_t)B.tiles_y;
     const uint32_t holes = B.counters[1];
@@ -346,12 +368,13 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_warp(Octree o, const Fram
             valid = x < xe && y < ye;
         }
         if (valid) {
-            const RayResult r = trace_ray<DEPTH, false>(o, cam, x, y, res_x, res_y, stk, kTraceBlock, fault);
+            const RayResult r = trace_ray<DEPTH, false>(o, cam, x, y, res_x, res_y, stk, BLOCK, fault);
             const size_t ofs = (size_t)y * res_x + x;
             col[ofs] = r.colour;
             xyz[ofs] = make_float4(r.hx, r.hy, r.hz, r.dist);
         }
     }
+    if (o_in.n_smem > 0 && !staged) stage_drain(&mbar);
     if (fault) atomicOr(fault_out, fault);
 }
 

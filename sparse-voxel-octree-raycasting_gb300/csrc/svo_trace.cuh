@@ -30,11 +30,19 @@ constexpr uint32_t kStepCap = 1u << 20;
 constexpr uint32_t kFaultFetch = 1u;       // node word index outside the octree
 constexpr uint32_t kFaultSteps = 2u;       // a ray exceeded kStepCap steps
 constexpr uint32_t kFaultHoleEntry = 4u;   // hole list entry outside the frame
+constexpr uint32_t kFaultStage = 8u;       // staging copy of the node prefix did not complete
+
+// Dynamic shared memory of the trace kernels: the per-thread node stack
+// ([level][thread]) followed by a staged copy of the octree's first words
+// (the normal-node region, see stage_prefix).
+extern __shared__ __align__(16) uint32_t svo_dsmem[];
 
 struct Octree {
     const uint32_t* __restrict__ words;
     uint32_t n_words;
     uint32_t root;
+    uint32_t n_smem;     // words [0, n_smem) are also in svo_dsmem[smem_base ...]
+    uint32_t smem_base;  // word offset of that copy in svo_dsmem
 };
 
 // Camera as the ray kernels consume it: position and the rows of m^T.
@@ -53,11 +61,81 @@ struct RayResult {
     uint64_t voxel;    // packed hit cell (bit 63 = hit)
 };
 
+// Node word fetch: the staged prefix from shared memory, the rest through the
+// read-only path, everything bounds-checked against the uploaded word count.
 __device__ __forceinline__ uint32_t load_word(const Octree& o, uint32_t i, uint32_t& fault) {
+    if (i < o.n_smem) return svo_dsmem[o.smem_base + i];
     if (i < o.n_words) return __ldg(o.words + i);
     fault |= kFaultFetch;
     return 0u;
 }
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait on phase 0 of an mbarrier: gives up after ~0.5 s.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar) {
+    if (mbar_try_wait(bar, 0)) return true;
+    const uint64_t t0 = global_ns();
+    for (;;) {
+        if (mbar_try_wait(bar, 0)) return true;
+        if (global_ns() - t0 > 500000000ull) return false;
+    }
+}
+
+// Copies octree words [0, n) into svo_dsmem[base ...] with bulk asynchronous
+// copies (the TMA engine), completing on an mbarrier. n*4 rounded up to 16
+// bytes must lie inside the octree allocation (checked by the host), the
+// source is the 256-byte aligned allocation start and base is a multiple of 4
+// words. Every thread of the block must call it. Returns false (and the
+// block must not use the copy) if the copy did not complete in time.
+__device__ __forceinline__ bool stage_prefix(const uint32_t* src, uint32_t n, uint32_t base, uint64_t* mbar,
+                                             uint32_t& fault) {
+    const uint32_t bytes = (n * 4u + 15u) & ~15u;
+    const uint32_t bar = smem_addr(mbar);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+        const uint32_t dst = smem_addr(svo_dsmem + base);
+        for (uint32_t off = 0; off < bytes; off += 16384u) {
+            const uint32_t chunk = min(16384u, bytes - off);
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    dst + off),
+                "l"(reinterpret_cast<const char*>(src) + off), "r"(chunk), "r"(bar)
+                : "memory");
+        }
+    }
+    const bool ok = __syncthreads_and(mbar_wait_bounded(bar) ? 1 : 0) != 0;
+    if (!ok) fault |= kFaultStage;
+    return ok;
+}
+
+// Before a block that gave up on its staging copy exits: wait (bounded) for
+// the copy still in flight so it never lands in released shared memory.
+__device__ __forceinline__ void stage_drain(uint64_t* mbar) { (void)mbar_wait_bounded(smem_addr(mbar)); }
 
 __device__ __forceinline__ uint32_t popc8(uint32_t v) { return __popc(v & 0xffu); }
 

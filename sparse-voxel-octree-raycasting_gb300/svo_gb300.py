@@ -19,6 +19,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libsvo_gb300.so")
 
 EMPTY_PIXEL = 0xFFFFFF00
+OPT_STAGE_NODES = 1
 DEFAULT_INITIAL_WORDS = 2097152
 STATUS = {
     0: "SVO_OK", 1: "SVO_ERR_INVALID_ARGUMENT", 2: "SVO_ERR_CUDA", 3: "SVO_ERR_NO_OCTREE",
@@ -29,7 +30,7 @@ STATUS = {
 # Every symbol include/svo_gb300.h declares.
 EXPORTS = [
     "svo_context_create", "svo_context_destroy", "svo_last_error", "svo_context_stream", "svo_synchronize",
-    "svo_launch_count", "svo_octree_upload", "svo_octree_upload_device", "svo_octree_set_l2_window",
+    "svo_launch_count", "svo_context_set_option", "svo_octree_upload", "svo_octree_upload_device", "svo_octree_set_l2_window",
     "svo_target_create", "svo_target_destroy", "svo_raycast_full", "svo_raycast_full_batch", "svo_warp_frame",
     "svo_target_use_graph", "svo_target_set_profiling", "svo_target_stage_times", "svo_read_colour",
     "svo_read_coords", "svo_read_holes", "svo_read_bgrx", "svo_read_full", "svo_read_voxels",
@@ -99,6 +100,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "svo_context_stream": (_P, [_P]),
         "svo_synchronize": (i, [_P]),
         "svo_launch_count": (ctypes.c_uint64, [_P]),
+        "svo_context_set_option": (i, [_P, i, ctypes.c_int64]),
         "svo_octree_upload": (i, [_P, _P, sz, u32, i, i]),
         "svo_octree_upload_device": (i, [_P, _P, sz, u32, i]),
         "svo_octree_set_l2_window": (i, [_P, sz]),
@@ -277,6 +279,9 @@ class Context:
 
     def upload_device(self, d_words: int, n_words: int, root: int, depth: int) -> None:
         _check(self._lib.svo_octree_upload_device(self._h, _P(d_words), n_words, root, depth), self)
+
+    def set_option(self, option: int, value: int) -> None:
+        _check(self._lib.svo_context_set_option(self._h, option, value), self)
 
     def set_l2_window(self, nbytes: int) -> None:
         _check(self._lib.svo_octree_set_l2_window(self._h, nbytes), self)
