@@ -139,29 +139,6 @@ __device__ __forceinline__ void stage_drain(uint64_t* mbar) { (void)mbar_wait_bo
 
 __device__ __forceinline__ uint32_t popc8(uint32_t v) { return __popc(v & 0xffu); }
 
-// fetchChildOffset (kernel.cl:32-62). At rekursion 1 the walk always stops
-// right after this call and never reads the returned word (kernel.cl:79 reads
-// the colour through the parent words), so that load is skipped.
-__device__ __forceinline__ uint32_t fetch_child(const Octree& o, uint32_t node, uint32_t before, uint32_t& local_root,
-                                                uint32_t child, uint32_t child_test, int rek, uint32_t& fault) {
-    uint32_t n = node >> 9;
-    if (node & 256u) {
-        if (!(before & 256u)) {
-            local_root = n << 6;
-            n = 0;
-        }
-        n += local_root;
-        const uint32_t nadd = __popc(node & ((child_test << 1) - 1u));
-        if (rek == 2) {
-            const uint32_t w = load_word(o, n + (nadd >> 2), fault);
-            return ((w >> ((nadd & 3u) << 3)) & 255u) + 256u + (nadd << 9);
-        }
-        if (rek == 1) return 0u;
-        return load_word(o, n + nadd, fault);
-    }
-    return load_word(o, n + child, fault);
-}
-
 // fetchColor (kernel.cl:64-112).
 __device__ __forceinline__ uint32_t fetch_colour(const Octree& o, uint32_t node, uint32_t before, uint32_t before2,
                                                  uint32_t local_root, int rek, uint32_t child_test, uint32_t& fault) {
@@ -219,10 +196,30 @@ struct Walk {
     int hcx, hcy, hcz;
 };
 
-// CAST_RAY's loop (kernel.cl:152-211). kFast: every coordinate of the walk
-// stays in [0, 2^23), checked by the caller from the mirrored start point
-// (each step moves a coordinate by at most the distance it adds, and the walk
-// stops once the distance passes VIEW_DIST_MAX).
+// load_word written as a select chain (no early returns) for the descent loop.
+__device__ __forceinline__ uint32_t load_word_sel(const Octree& o, uint32_t i, uint32_t& fault) {
+    const bool in_smem = i < o.n_smem;
+    const bool in_range = i < o.n_words;
+    uint32_t v = 0;
+    if (in_smem) v = svo_dsmem[o.smem_base + i];
+    else if (in_range) v = __ldg(o.words + i);
+    else fault |= kFaultFetch;
+    return v;
+}
+
+// CAST_RAY's loop (kernel.cl:152-211), arranged for SIMT execution:
+//   * descents run in an inner loop, so the lanes of a warp that descend do so
+//     together and then all lanes step together (a loop iteration no longer
+//     runs both the descend and the step path);
+//   * the next level's child index is computed while the node load is in
+//     flight; block-node addressing uses selects instead of nested branches;
+//   * the descent loop needs no step cap (rek strictly decreases); the view
+//     distance and y-exit tests share one branch.
+// The state changes are those of the reference loop, in the same order.
+// kFast: every coordinate of the walk stays in [0, 2^23), checked by the
+// caller from the mirrored start point (each step moves a coordinate by at
+// most the distance it adds, and the walk stops once the distance passes
+// VIEW_DIST_MAX).
 template <int DEPTH, bool kFast>
 __device__ __forceinline__ void walk(const Octree& o, Walk& w, uint32_t sxyz, float g0y, float g0z, float g1x,
                                      float g1z, float g2x, float g2y, float lx, float ly, float lz, float lodswitch,
@@ -236,30 +233,55 @@ __device__ __forceinline__ void walk(const Octree& o, Walk& w, uint32_t sxyz, fl
     const uint32_t root = o.root;
     uint32_t nodeid = root, nodeid_before = root, local_root = 0, node_test = 0;
     uint32_t steps = 0;
+    auto child_index = [&](int r) -> uint32_t {
+        return ((uint32_t)((rix >> r) & 1) | ((uint32_t)((riy >> r) & 1) << 1) | ((uint32_t)((riz >> r) & 1) << 2)) ^
+               sxyz;
+    };
+    uint32_t ni = child_index(rek);
     for (;;) {
+        node_test = nodeid & (1u << ni);
+        bool hit = false;
+        while (node_test) {
+            const uint32_t parent = nodeid;
+            const uint32_t n = nodeid >> 9;
+            if (!(nodeid & 256u)) {
+                nodeid = load_word_sel(o, n + ni, fault);
+            } else {
+                const bool enter = !(nodeid_before & 256u);
+                local_root = enter ? (n << 6) : local_root;
+                const uint32_t base = enter ? local_root : local_root + n;
+                const uint32_t nadd = __popc(nodeid & ((node_test << 1) - 1u));
+                if (rek > 2) {
+                    nodeid = load_word_sel(o, base + nadd, fault);
+                } else if (rek == 2) {
+                    const uint32_t wd = load_word_sel(o, base + (nadd >> 2), fault);
+                    nodeid = ((wd >> ((nadd & 3u) << 3)) & 255u) + 256u + (nadd << 9);
+                } else {
+                    nodeid = 0u;
+                }
+            }
+            nodeid_before = parent;
+            if (rek <= lod) {
+                hit = true;
+                break;
+            }
+            --rek;
+            ni = child_index(rek);
+            stk[rek * stride] = nodeid;
+            node_test = nodeid & (1u << ni);
+        }
+        if (hit) {
+            w.hit = true;
+            w.hcx = rix >> rek;
+            w.hcy = riy >> rek;
+            w.hcz = riz >> rek;
+            break;
+        }
         if (++steps > kStepCap) {
             fault |= kFaultSteps;
             break;
         }
         const int p0x = rix >> rek, p0y = riy >> rek, p0z = riz >> rek;
-        const uint32_t ni = ((uint32_t)(p0x & 1) | ((uint32_t)(p0y & 1) << 1) | ((uint32_t)(p0z & 1) << 2)) ^ sxyz;
-        node_test = nodeid & (1u << ni);
-        if (node_test) {
-            const uint32_t parent = nodeid;
-            nodeid = fetch_child(o, nodeid, nodeid_before, local_root, ni, node_test, rek, fault);
-            nodeid_before = parent;
-            if (rek <= lod) {
-                w.hit = true;
-                w.hcx = p0x;
-                w.hcy = p0y;
-                w.hcz = p0z;
-                break;
-            }
-            --rek;
-            stk[rek * stride] = nodeid;
-            continue;
-        }
-        // Distances to the three next cell planes; step along the nearest.
         const float m0x = __fsub_rn(int_to_float<kFast>((p0x + 1) << rek), rpx);
         const float m0y = __fsub_rn(int_to_float<kFast>((p0y + 1) << rek), rpy);
         const float m0z = __fsub_rn(int_to_float<kFast>((p0z + 1) << rek), rpz);
@@ -278,23 +300,21 @@ __device__ __forceinline__ void walk(const Octree& o, Walk& w, uint32_t sxyz, fl
         distance = __fadd_rn(distance, best);
         const int x0ry = by ^ riy;
         const uint32_t x0r = (uint32_t)(((bx ^ rix) ^ x0ry ^ (bz ^ riz)) & kDepthAnd);
-        if (distance > kViewDistMax) break;
-        // log2(x0r) >= rek <=> some bit at or above rek changed: pop to the
-        // level above the highest changed bit.
-        if (x0r >> rek) {
+        const bool far = distance > kViewDistMax;
+        if (!far && (x0r >> rek)) {
             rek = 32 - __clz(x0r);
-            if (rek >= DEPTH) {
-                nodeid = nodeid_before = root;
-            } else {
-                nodeid = stk[rek * stride];
-                nodeid_before = (rek + 1 >= DEPTH) ? root : stk[(rek + 1) * stride];
-            }
+            const bool at_root = rek >= DEPTH;
+            const uint32_t s0 = at_root ? root : stk[rek * stride];
+            const uint32_t s1 = (rek + 1 >= DEPTH) ? root : stk[(rek + 1) * stride];
+            nodeid = s0;
+            nodeid_before = at_root ? root : s1;
             if (distance > lodswitch) {
                 lodswitch = __fmul_rn(lodswitch, 2.0f);
                 ++lod;
             }
         }
-        if (x0ry & kTopBit) break;
+        if (far || (x0ry & kTopBit)) break;
+        ni = child_index(rek);
     }
     w.rpx = rpx;
     w.rpy = rpy;
