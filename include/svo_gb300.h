@@ -192,6 +192,37 @@ typedef struct svo_device_outputs {
 } svo_device_outputs;
 svo_status svo_target_device_outputs(svo_target* t, svo_device_outputs* out);
 
+/* ----------------------------------------------- allocation-free call -- */
+/* No counterpart in the reference. A full raycast (as svo_raycast_full, one
+ * or more views) that allocates nothing, for callers that cannot let this
+ * library allocate device memory: engines that hand out all GPU memory from
+ * their own allocator or pool, frame loops that may not allocate after
+ * start-up, plugins that may not create a context or grow its footprint.
+ * The caller passes the octree words already on the current device and, per
+ * view, device buffers of res_x*res_y elements for every output. The little
+ * scratch the trace needs -- work-queue counter, fault flags and the table
+ * of views, 7 KiB -- is a static device array that exists once per device
+ * while the library is loaded; the views beyond SVO_NOALLOC_MAX_VIEWS do not
+ * fit in it and are rejected with SVO_ERR_CAPACITY.
+ * The first call on a device looks up that array's device address; make the
+ * first call before any stream capture. Every call shares the array (it keeps
+ * the last call's contents; the counter and fault flags are cleared at the
+ * start of each call), so calls that overlap on the GPU -- from two host
+ * threads or on two streams at once -- race; issue them one after another.
+ * The call runs on `stream` (null = the default stream) and returns when the
+ * rays are written, with SVO_ERR_DEVICE_FAULT if a kernel flagged an
+ * out-of-range node word. */
+#define SVO_NOALLOC_MAX_VIEWS 64
+typedef struct svo_frame_buffers {
+    uint32_t* colour; /* 0xff000000 + colour word */
+    float* xyzw;      /* 4 floats per pixel: hit xyz, hit distance (world units) */
+    uint64_t* voxel;  /* packed hit voxel, as svo_read_voxels */
+    uint32_t* bgrx;   /* colourised BGRX8 */
+} svo_frame_buffers;
+svo_status svo_raycast_full_noalloc(const uint32_t* d_words, size_t n_words, uint32_t root_word, int depth,
+                                    const svo_view* views, const svo_frame_buffers* outputs, int n_views,
+                                    void* stream);
+
 /* ------------------------------------------------- host octree builder -- */
 /* Replaces set_voxel / convert_tree_blocks (src/octree/octree.h:32-89,
  * 232-293) and octree_init (src/raycast.h:13-46). Produces the same compact

@@ -9,8 +9,10 @@
 // persistent trace launch's work queue.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -814,3 +816,153 @@ svo_status svo_target_device_outputs(svo_target* t, svo_device_outputs* out) {
 }
 
 }  // extern "C"
+
+// ======================================================================
+// A full raycast entry point that allocates no memory.
+//
+// For callers that cannot allocate device memory through this library: host
+// engines that hand out all GPU memory from their own allocator or pool, code
+// paths that run after start-up in a no-allocation frame budget, and plugins
+// that may not create a context or grow its footprint. The caller passes the
+// octree words and every output buffer; the only memory the call needs
+// besides them -- the trace kernel's work-queue counter, its fault flags and
+// the table of views -- lives in the file-scope array below, which exists
+// once per device for as long as the library is loaded.
+namespace {
+
+// Layout of the scratch array: the counter and fault word in the first 256
+// bytes, then a FullBatch header with room for SVO_NOALLOC_MAX_VIEWS views.
+constexpr size_t kNoAllocTableOffset = 256;
+constexpr size_t kNoAllocTableBytes = offsetof(FullBatch, v) + sizeof(FullView) * SVO_NOALLOC_MAX_VIEWS;
+constexpr size_t kNoAllocScratchBytes = kNoAllocTableOffset + kNoAllocTableBytes;
+static_assert(SVO_NOALLOC_MAX_VIEWS <= kMaxBatchViews, "view table larger than the kernel's batch layout");
+
+// Device copy of the scratch. In host code this name is only a stand-in for
+// the symbol; its device address comes from cudaGetSymbolAddress.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_setup_mutex;
+unsigned char* g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device, looked up once
+// per device.
+svo_status scratch_address(int device, unsigned char** out) {
+    std::lock_guard<std::mutex> lock(g_setup_mutex);
+    if (!g_scratch_ptr[device]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return SVO_ERR_CUDA;
+        g_scratch_ptr[device] = static_cast<unsigned char*>(p);
+    }
+    *out = g_scratch_ptr[device];
+    return SVO_OK;
+}
+
+template <int BLOCK>
+const void* noalloc_kernel(int depth) {
+    switch (depth) {
+        case 8: return (const void*)k_trace_full<8, BLOCK, true>;
+        case 9: return (const void*)k_trace_full<9, BLOCK, true>;
+        case 10: return (const void*)k_trace_full<10, BLOCK, true>;
+        case 11: return (const void*)k_trace_full<11, BLOCK, true>;
+        case 12: return (const void*)k_trace_full<12, BLOCK, true>;
+    }
+    return nullptr;
+}
+
+}  // namespace
+
+extern "C" svo_status svo_raycast_full_noalloc(const uint32_t* d_words, size_t n_words, uint32_t root_word, int depth,
+                                               const svo_view* views, const svo_frame_buffers* outputs, int n_views,
+                                               void* stream) {
+    if (!d_words || n_words < 10 || n_words >= 0xffffffc0ull || !views || !outputs || n_views < 1)
+        return SVO_ERR_INVALID_ARGUMENT;
+    if (depth < SVO_MIN_DEPTH || depth > SVO_MAX_DEPTH) return SVO_ERR_INVALID_ARGUMENT;
+    if (n_views > SVO_NOALLOC_MAX_VIEWS) return SVO_ERR_CAPACITY;
+    for (int i = 0; i < n_views; ++i) {
+        const svo_view& v = views[i];
+        const svo_frame_buffers& o = outputs[i];
+        if (v.res_x < 1 || v.res_y < 1 || v.res_x > 65535 || v.res_y > 65535) return SVO_ERR_INVALID_ARGUMENT;
+        if (!o.colour || !o.xyzw || !o.voxel || !o.bgrx) return SVO_ERR_INVALID_ARGUMENT;
+    }
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= kMaxDevices) return SVO_ERR_CUDA;
+    unsigned char* scratch = nullptr;
+    svo_status st = scratch_address(device, &scratch);
+    if (st != SVO_OK) return st;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+    // View table, built on the host stack and copied into the scratch array.
+    struct alignas(16) Table {
+        unsigned char bytes[kNoAllocTableBytes];
+    } table;
+    std::memset(&table, 0, sizeof(table));
+    FullBatch* hb = reinterpret_cast<FullBatch*>(table.bytes);
+    hb->n_views = n_views;
+    uint32_t packets = 0;
+    for (int i = 0; i < n_views; ++i) {
+        const svo_view& v = views[i];
+        FullView& fv = hb->v[i];
+        fv.ray.px = v.pos[0];
+        fv.ray.py = v.pos[1];
+        fv.ray.pz = v.pos[2];
+        fv.ray.mxx = v.m[0];
+        fv.ray.mxy = v.m[4];
+        fv.ray.mxz = v.m[8];
+        fv.ray.myx = v.m[1];
+        fv.ray.myy = v.m[5];
+        fv.ray.myz = v.m[9];
+        fv.ray.mzx = v.m[2];
+        fv.ray.mzy = v.m[6];
+        fv.ray.mzz = v.m[10];
+        fv.ray.fovx = v.fovx;
+        fv.ray.fovy = v.fovy;
+        fv.res_x = v.res_x;
+        fv.res_y = v.res_y;
+        fv.packets_x = (v.res_x + 7) / 8;
+        fv.packet_begin = packets;
+        packets += (uint32_t)fv.packets_x * (uint32_t)((v.res_y + 3) / 4);
+        fv.col = outputs[i].colour;
+        fv.xyzw = reinterpret_cast<float4*>(outputs[i].xyzw);
+        fv.vox = outputs[i].voxel;
+        fv.bgrx = outputs[i].bgrx;
+    }
+    hb->total_packets = packets;
+
+    // Launch geometry as for the context path: stage the normal-node region in
+    // shared memory when it fits and the words are 16-byte aligned.
+    Octree o{d_words, (uint32_t)n_words, root_word, 0u, 0u};
+    uint32_t stage_bytes = 0;
+    if (!(root_word & 256u) && (reinterpret_cast<uintptr_t>(d_words) & 15u) == 0) {
+        const uint64_t nw = (uint64_t)(root_word >> 9) + 10u;
+        const uint64_t bytes = (nw * 4u + 15u) & ~15ull;
+        if (bytes <= 160u * 1024u && bytes <= (uint64_t)n_words * 4u) {
+            o.n_smem = (uint32_t)nw;
+            stage_bytes = (uint32_t)bytes;
+        }
+    }
+    const int block = stage_bytes > 48u * 1024u ? 1024 : 256;
+    const void* fn = block == 1024 ? noalloc_kernel<1024>(depth) : noalloc_kernel<256>(depth);
+    const size_t smem = (size_t)(depth + 1) * block * 4u + stage_bytes;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return SVO_ERR_CUDA;
+    int per_sm = 0, sms = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, smem) != cudaSuccess) return SVO_ERR_CUDA;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return SVO_ERR_CUDA;
+
+    // The counter and the fault word must start at zero on every call.
+    uint32_t* counter = reinterpret_cast<uint32_t*>(scratch);
+    uint32_t* fault = counter + 1;
+    FullBatch* d_batch = reinterpret_cast<FullBatch*>(scratch + kNoAllocTableOffset);
+    if (cudaMemsetAsync(scratch, 0, 8, s) != cudaSuccess) return SVO_ERR_CUDA;
+    if (cudaMemcpyAsync(d_batch, table.bytes, kNoAllocTableBytes, cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return SVO_ERR_CUDA;
+    void* args[] = {&o, &d_batch, &counter, &fault};
+    if (cudaLaunchKernel(fn, dim3((unsigned)(std::max(1, per_sm) * sms)), dim3((unsigned)block), args, smem, s) !=
+        cudaSuccess)
+        return SVO_ERR_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return SVO_ERR_CUDA;
+    uint32_t flags = 0;
+    if (cudaMemcpy(&flags, fault, sizeof(flags), cudaMemcpyDeviceToHost) != cudaSuccess) return SVO_ERR_CUDA;
+    return flags ? SVO_ERR_DEVICE_FAULT : SVO_OK;
+}

@@ -20,6 +20,7 @@ LIB_PATH = os.path.join(HERE, "libsvo_gb300.so")
 
 EMPTY_PIXEL = 0xFFFFFF00
 OPT_STAGE_NODES = 1
+NOALLOC_MAX_VIEWS = 64
 DEFAULT_INITIAL_WORDS = 2097152
 STATUS = {
     0: "SVO_OK", 1: "SVO_ERR_INVALID_ARGUMENT", 2: "SVO_ERR_CUDA", 3: "SVO_ERR_NO_OCTREE",
@@ -38,6 +39,7 @@ EXPORTS = [
     "svo_builder_set_voxels", "svo_builder_finish", "svo_builder_copy_words", "svo_builder_stats",
     "svo_octree_save", "svo_octree_load_header", "svo_octree_load_words", "svo_terrain_build",
     "svo_terrain_voxels", "svo_view_from_euler", "svo_view_look_at", "svo_wrap_position", "svo_camera_path",
+    "svo_raycast_full_noalloc",
 ]
 
 
@@ -64,6 +66,12 @@ class View(ctypes.Structure):
 class TerrainSpec(ctypes.Structure):
     _fields_ = [("seed", ctypes.c_uint32), ("depth", ctypes.c_int32), ("shell", ctypes.c_int32),
                 ("boxes", ctypes.c_int32)]
+
+
+class FrameBuffers(ctypes.Structure):
+    """svo_frame_buffers: device output buffers of one view of svo_raycast_full_noalloc."""
+    _fields_ = [("colour", ctypes.c_void_p), ("xyzw", ctypes.c_void_p), ("voxel", ctypes.c_void_p),
+                ("bgrx", ctypes.c_void_p)]
 
 
 class DeviceOutputs(ctypes.Structure):
@@ -137,6 +145,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "svo_view_look_at": (i, [_P, _P, i, i, ctypes.c_float, ctypes.POINTER(View)]),
         "svo_wrap_position": (i, [_P, i]),
         "svo_camera_path": (i, [i, i, i, u32, i, i, ctypes.c_float, ctypes.POINTER(View)]),
+        "svo_raycast_full_noalloc": (i, [_P, sz, u32, i, _P, _P, i, _P]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
