@@ -251,6 +251,24 @@ svo_status svo_octree_save(const char* path, const uint32_t* words, size_t n_wor
 svo_status svo_octree_load_header(const char* path, size_t* n_words, uint32_t* root_word, int* depth);
 svo_status svo_octree_load_words(const char* path, uint32_t* words, size_t n_words);
 
+/* --------------------------------------------------------- .rle4 files -- */
+/* The reference's volume loader RLE4::load (src/octree/Rle4.cpp:8-165): the
+ * voxels of map 0 of an .rle4 file with the same colour words and the same
+ * insertion order (z outer, x inner, top of each column first), offset by
+ * (addx, addy, addz). palette selects the material/intensity colour byte
+ * (Rle4.cpp:146); 0 is the reference's default (octree_init passes 0).
+ * Malformed files fail with SVO_ERR_IO (the reference reads out of bounds). */
+svo_status svo_rle4_voxels(const char* path, int palette, uint32_t addx, uint32_t addy, uint32_t addz, uint32_t* x,
+                           uint32_t* y, uint32_t* z, uint32_t* rgba, size_t cap, size_t* n);
+/* Inserts those voxels into a builder (SVO_ERR_CAPACITY if one falls outside
+ * the builder's 2^depth cube). */
+svo_status svo_rle4_build(svo_builder* b, const char* path, int palette, uint32_t addx, uint32_t addy, uint32_t addz);
+
+/* 32-bit BMP of a BGRX8 frame, top row first in the frame (replaces the dead
+ * frame dump of src/raycast.h:496-509 and Bmp::save, src/Bmp.cpp:30-60, with
+ * a complete header). */
+svo_status svo_write_bmp(const char* path, const uint32_t* bgrx, int width, int height);
+
 /* --------------------------------------------------- synthetic scenes -- */
 /* Seeded value-noise fBm terrain (6 octaves, lacunarity 2, gain 0.5,
  * amplitude 0.3*extent, base 0.35*extent). shell = 0 inserts every voxel

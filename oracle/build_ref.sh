@@ -1,6 +1,7 @@
 #!/usr/bin/env bash
-# Builds oracle/_ref/libsvo_ref.so: the reference's own kernel/kernel.cl and
-# src/octree/octree.h compiled for the host CPU behind oracle/ref_shim.h, one
+# Builds oracle/_ref/libsvo_ref.so: the reference's own kernel/kernel.cl,
+# src/octree/octree.h and src/octree/Rle4.cpp (behind oracle/ref_win/windows.h)
+# compiled for the host CPU behind oracle/ref_shim.h, one
 # copy per octree depth 8..12 (OCTREE_DEPTH is hard-coded at kernel.cl:12 and
 # octree.h:2, so the sources are streamed through sed into the compiler; no
 # copy of them is written anywhere). TEST INFRASTRUCTURE ONLY: the library is
@@ -39,8 +40,12 @@ mkdir -p "$OUT"
         echo '#include "ref_driver.inc"'
         echo '}'
     done
+    if [ -f "$REF/src/octree/Rle4.cpp" ]; then
+        echo '#line 1 "src/octree/Rle4.cpp"'
+        cat "$REF/src/octree/Rle4.cpp"
+    fi
     echo '#include "ref_capi.inc"'
 } | g++ -x c++ -std=c++17 -O2 -ffp-contract=off -fno-strict-aliasing -fPIC -shared -w \
-        -I"$HERE" -I"$REF/src/octree" -I"$REF/src" -o "$OUT/libsvo_ref.so.tmp" -
+        -I"$HERE" -I"$HERE/ref_win" -I"$REF/src/octree" -I"$REF/src" -o "$OUT/libsvo_ref.so.tmp" -
 mv "$OUT/libsvo_ref.so.tmp" "$OUT/libsvo_ref.so"
 echo "build_ref: built $OUT/libsvo_ref.so"

@@ -385,6 +385,96 @@ void fill_view(svo_view* out, const float pos[3], const float* m, int res_x, int
     out->res_y = res_y;
 }
 
+// --------------------------------------------------------------- .rle4 ----
+// The reference's mip-volume format (src/octree/Rle4.cpp:8-165): int32 map
+// count, then per map sx, sy, sz, slabs_size and slabs_size uint16 words. A
+// map is sx*sz columns, x fastest; a column is [count, texels, count slab
+// words, texels texel words]; a slab word skips (slab & 1023) empty voxels
+// and then fills (slab >> 10) voxels, one texel each. Only map 0 is turned
+// into voxels (Rle4.cpp:91), column by column (z outer, x inner), top of the
+// volume first in y (y = sy-1-y1).
+struct Rle4Map {
+    int32_t sx = 0, sy = 0, sz = 0;
+    std::vector<uint16_t> slabs;
+    std::vector<uint32_t> column;  // slab offset of every column
+};
+
+bool rle4_read(const char* path, Rle4Map& m0, std::string& why) {
+    FILE* f = std::fopen(path, "rb");
+    if (!f) {
+        why = "cannot open";
+        return false;
+    }
+    auto rd = [&](void* p, size_t bytes) { return std::fread(p, 1, bytes, f) == bytes; };
+    int32_t nummaps = 0;
+    bool ok = rd(&nummaps, 4) && nummaps >= 1 && nummaps <= 16;
+    for (int m = 0; ok && m < nummaps; ++m) {
+        int32_t hdr[4];
+        ok = rd(hdr, 16) && hdr[0] > 0 && hdr[1] > 0 && hdr[2] > 0 && hdr[3] > 0 &&
+             (int64_t)hdr[0] * hdr[2] <= (1ll << 28) && hdr[3] <= (1 << 30);
+        if (!ok) break;
+        Rle4Map map;
+        map.sx = hdr[0];
+        map.sy = hdr[1];
+        map.sz = hdr[2];
+        map.slabs.resize((size_t)hdr[3]);
+        ok = rd(map.slabs.data(), map.slabs.size() * 2);
+        if (!ok) break;
+        // Column offsets (Rle4.cpp:50-73), bounds-checked.
+        const size_t cols = (size_t)map.sx * map.sz;
+        map.column.resize(cols);
+        size_t ofs = 0;
+        for (size_t c = 0; c < cols && ok; ++c) {
+            if (ofs + 2 > map.slabs.size()) {
+                ok = false;
+                break;
+            }
+            map.column[c] = (uint32_t)ofs;
+            const size_t count = map.slabs[ofs], texels = map.slabs[ofs + 1];
+            if (ofs + 2 + count + texels > map.slabs.size()) ok = false;
+            ofs += count + texels + 2;
+        }
+        if (ok && m == 0) m0 = std::move(map);
+    }
+    std::fclose(f);
+    if (!ok && why.empty()) why = "malformed .rle4 file";
+    return ok;
+}
+
+// Voxels of map 0 with the reference's colour word (Rle4.cpp:116-160).
+template <class F>
+void rle4_voxels(const Rle4Map& m, int palette, uint32_t addx, uint32_t addy, uint32_t addz, F&& emit) {
+    for (int32_t slice = 0; slice < m.sz; ++slice)
+        for (int32_t x = 0; x < m.sx; ++x) {
+            const size_t ofs = m.column[(size_t)x + (size_t)m.sx * slice];
+            const uint32_t count = m.slabs[ofs];
+            const uint32_t texels = m.slabs[ofs + 1];
+            const uint16_t* p = m.slabs.data() + ofs + 2;
+            const uint16_t* pt = p + count;
+            const uint16_t* pt_end = pt + texels;
+            uint32_t y1 = 0, y2 = 0;
+            for (uint32_t s = 0; s < count; ++s) {
+                const uint16_t slab = p[s];
+                y1 += slab & 1023u;
+                y2 = y1 + (slab >> 10);
+                for (; y1 < y2; ++y1, ++pt) {
+                    if (y1 >= (uint32_t)m.sy || pt >= pt_end) continue;
+                    const uint32_t tcol = *pt;
+                    const int material = (int)((tcol >> 8) & 3u);
+                    int intensity = (int)((tcol & 255u) * (tcol & 255u) / 255u);
+                    if (intensity < 2) intensity = 2;
+                    if (intensity > 255) intensity = 255;
+                    uint32_t rx = (uint32_t)(material + ((intensity >> 3) << 3)) & 0xffu;
+                    if (!palette) rx = (1u + ((255u - (tcol & 255u)) & 0xfcu)) & 0xffu;
+                    const uint32_t ry = ((tcol >> 5) << 3) & 0xffu;
+                    const uint32_t rz = ((tcol >> 10) << 3) & 0xffu;
+                    emit((uint32_t)x + addx, (uint32_t)m.sy - 1u - y1 + addy, (uint32_t)slice + addz,
+                         rx | (ry << 8) | (rz << 16));
+                }
+            }
+        }
+}
+
 }  // namespace
 
 // ================================================================ C ABI ==
@@ -707,6 +797,71 @@ svo_status svo_camera_path(int kind, int depth, int frame, uint32_t seed, int re
     // The reference keeps the camera inside the periodic volume (src/raycast.h:136-145).
     svo_wrap_position(out->pos, depth);
     return SVO_OK;
+}
+
+svo_status svo_rle4_voxels(const char* path, int palette, uint32_t addx, uint32_t addy, uint32_t addz, uint32_t* x,
+                           uint32_t* y, uint32_t* z, uint32_t* rgba, size_t cap, size_t* n) {
+    if (!path || !n) return SVO_ERR_INVALID_ARGUMENT;
+    Rle4Map m;
+    std::string why;
+    if (!rle4_read(path, m, why)) return SVO_ERR_IO;
+    size_t k = 0;
+    const bool write = x && y && z && rgba;
+    rle4_voxels(m, palette, addx, addy, addz, [&](uint32_t vx, uint32_t vy, uint32_t vz, uint32_t c) {
+        if (write && k < cap) {
+            x[k] = vx;
+            y[k] = vy;
+            z[k] = vz;
+            rgba[k] = c;
+        }
+        ++k;
+    });
+    *n = k;
+    return (write && k > cap) ? SVO_ERR_CAPACITY : SVO_OK;
+}
+
+svo_status svo_rle4_build(svo_builder* b, const char* path, int palette, uint32_t addx, uint32_t addy, uint32_t addz) {
+    if (!b || !path || b->finished) return SVO_ERR_INVALID_ARGUMENT;
+    Rle4Map m;
+    std::string why;
+    if (!rle4_read(path, m, why)) return SVO_ERR_IO;
+    const uint32_t D = 1u << b->depth;
+    bool inside = true;
+    rle4_voxels(m, palette, addx, addy, addz, [&](uint32_t vx, uint32_t vy, uint32_t vz, uint32_t c) {
+        if (vx >= D || vy >= D || vz >= D) {
+            inside = false;
+            return;
+        }
+        b->keys.push_back(morton3(vx, vy, vz));
+        b->rgba.push_back(c);
+    });
+    return inside ? SVO_OK : SVO_ERR_CAPACITY;
+}
+
+svo_status svo_write_bmp(const char* path, const uint32_t* bgrx, int width, int height) {
+    if (!path || !bgrx || width < 1 || height < 1 || (int64_t)width * height > (1ll << 28))
+        return SVO_ERR_INVALID_ARGUMENT;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return SVO_ERR_IO;
+    const uint32_t image = (uint32_t)width * (uint32_t)height * 4u;
+    unsigned char h[54] = {'B', 'M'};
+    auto put32 = [&](int at, uint32_t v) {
+        for (int i = 0; i < 4; ++i) h[at + i] = (unsigned char)(v >> (8 * i));
+    };
+    put32(2, 54u + image);
+    put32(10, 54u);
+    put32(14, 40u);
+    put32(18, (uint32_t)width);
+    put32(22, (uint32_t)height);
+    h[26] = 1;
+    h[28] = 32;
+    put32(34, image);
+    bool ok = std::fwrite(h, 1, 54, f) == 54;
+    // BMP rows run bottom-up; the frame's row 0 is the top of the image.
+    for (int yy = height - 1; ok && yy >= 0; --yy)
+        ok = std::fwrite(bgrx + (size_t)yy * width, 4, (size_t)width, f) == (size_t)width;
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? SVO_OK : SVO_ERR_IO;
 }
 
 }  // extern "C"

@@ -39,7 +39,7 @@ EXPORTS = [
     "svo_builder_set_voxels", "svo_builder_finish", "svo_builder_copy_words", "svo_builder_stats",
     "svo_octree_save", "svo_octree_load_header", "svo_octree_load_words", "svo_terrain_build",
     "svo_terrain_voxels", "svo_view_from_euler", "svo_view_look_at", "svo_wrap_position", "svo_camera_path",
-    "svo_raycast_full_noalloc",
+    "svo_raycast_full_noalloc", "svo_rle4_voxels", "svo_rle4_build", "svo_write_bmp",
 ]
 
 
@@ -146,6 +146,9 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "svo_wrap_position": (i, [_P, i]),
         "svo_camera_path": (i, [i, i, i, u32, i, i, ctypes.c_float, ctypes.POINTER(View)]),
         "svo_raycast_full_noalloc": (i, [_P, sz, u32, i, _P, _P, i, _P]),
+        "svo_rle4_voxels": (i, [ctypes.c_char_p, i, u32, u32, u32, _P, _P, _P, _P, sz, ctypes.POINTER(sz)]),
+        "svo_rle4_build": (i, [_P, ctypes.c_char_p, i, u32, u32, u32]),
+        "svo_write_bmp": (i, [ctypes.c_char_p, _P, i, i]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -174,6 +177,24 @@ def terrain_voxels(seed: int, depth: int, shell: bool, boxes: int = 0):
     y, z, c = np.empty_like(x), np.empty_like(x), np.empty_like(x)
     _check(lib.svo_terrain_voxels(ctypes.byref(spec), _ptr(x), _ptr(y), _ptr(z), _ptr(c), n.value, ctypes.byref(n)))
     return x, y, z, c
+
+
+def rle4_voxels(path: str, palette: int = 0, add=(0, 0, 0)):
+    """Voxels of map 0 of an .rle4 file in the reference loader's order: (x, y, z, rgba)."""
+    lib = load()
+    n = ctypes.c_size_t()
+    _check(lib.svo_rle4_voxels(path.encode(), palette, add[0], add[1], add[2], None, None, None, None, 0,
+                               ctypes.byref(n)), None, f"cannot read {path}")
+    x = np.empty(n.value, np.uint32)
+    y, z, c = np.empty_like(x), np.empty_like(x), np.empty_like(x)
+    _check(lib.svo_rle4_voxels(path.encode(), palette, add[0], add[1], add[2], _ptr(x), _ptr(y), _ptr(z), _ptr(c),
+                               n.value, ctypes.byref(n)))
+    return x, y, z, c
+
+
+def write_bmp(path: str, bgrx: np.ndarray, width: int, height: int) -> None:
+    img = np.ascontiguousarray(bgrx, np.uint32)
+    _check(load().svo_write_bmp(path.encode(), _ptr(img), width, height), None, f"cannot write {path}")
 
 
 class Octree:
@@ -214,6 +235,10 @@ class Builder:
     def set_voxels(self, x, y, z, rgba) -> None:
         arrs = [np.ascontiguousarray(a, dtype=np.uint32) for a in (x, y, z, rgba)]
         _check(self._lib.svo_builder_set_voxels(self._h, *[_ptr(a) for a in arrs], arrs[0].size))
+
+    def add_rle4(self, path: str, palette: int = 0, add=(0, 0, 0)) -> None:
+        _check(self._lib.svo_rle4_build(self._h, path.encode(), palette, add[0], add[1], add[2]), None,
+               f"cannot load {path}")
 
     def add_terrain(self, seed: int, shell: bool, boxes: int = 0) -> None:
         spec = TerrainSpec(seed, self.depth, 1 if shell else 0, boxes)
