@@ -57,7 +57,7 @@ def oracle() -> ctypes.CDLL:
         lib.orc_warp_create.restype = _P
         lib.orc_warp_create.argtypes = [i, i]
         lib.orc_warp_free.argtypes = [_P]
-        lib.orc_warp_frame.argtypes = [_P, i, _P, sz, u32, _P, _P, i, i]
+        lib.orc_warp_frame.argtypes = [_P, i, _P, sz, u32, _P, _P, i, i, i]
         for name in ("screen", "ids", "tex", "prefill"):
             f = getattr(lib, "orc_warp_" + name)
             f.restype = ctypes.POINTER(ctypes.c_uint32)
@@ -95,7 +95,7 @@ def reference() -> ctypes.CDLL:
         lib.ref_warp_create.restype = _P
         lib.ref_warp_create.argtypes = [i, i, i]
         lib.ref_warp_free.argtypes = [_P]
-        lib.ref_warp_frame.argtypes = [_P, _P, sz, u32, _P, _P, i]
+        lib.ref_warp_frame.argtypes = [_P, _P, sz, u32, _P, _P, i, i]
         for name in ("screen", "ids", "tex", "prefill"):
             f = getattr(lib, "ref_warp_" + name)
             f.restype = ctypes.POINTER(ctypes.c_uint32)
@@ -169,15 +169,16 @@ class Warp:
         if not self._h:
             raise ValueError("warp state: resolution must be at least 16x16")
 
-    def frame(self, words, root, pos, m, frame: int, threads: int = 0) -> None:
+    def frame(self, words, root, pos, m, frame: int, threads: int = 0, cache_mode: int = 0) -> None:
         words = np.ascontiguousarray(words, np.uint32)
         pos = np.ascontiguousarray(pos, np.float32)
         m = np.ascontiguousarray(m, np.float32)
         if self.which == "oracle":
             rc = self._lib.orc_warp_frame(self._h, self.depth, _ptr(words), words.size, root, _ptr(pos), _ptr(m),
-                                          frame, threads)
+                                          frame, threads, cache_mode)
         else:
-            rc = self._lib.ref_warp_frame(self._h, _ptr(words), words.size, root, _ptr(pos), _ptr(m), frame)
+            rc = self._lib.ref_warp_frame(self._h, _ptr(words), words.size, root, _ptr(pos), _ptr(m), frame,
+                                          cache_mode)
         if rc != 0:
             raise RuntimeError(f"{self._pre}_warp_frame failed: {rc}")
 

@@ -436,10 +436,13 @@ inline int proj_coord(float num, float z, float half) {
     return (int)(float)v;
 }
 
+// raycast_proj over one cache plane (kernel.cl:472-592). Rejected source
+// pixels (behind the camera or off screen) are cleared in that cache plane
+// (kernel.cl:549-562), which matters for a plane that is not the copy target.
 void proj_plane(Warp& w, const View& v, uint32_t plane) {
     const int res_x = w.res_x, res_y = w.res_y;
     const size_t N = w.N;
-    const uint32_t* src = w.screen.data() + plane * N;
+    uint32_t* src = w.screen.data() + plane * N;
     const float* sb = w.back.data() + plane * N * 4;
     std::atomic<uint64_t>* keys = reinterpret_cast<std::atomic<uint64_t>*>(w.keys.data());
 #pragma omp parallel for schedule(static)
@@ -448,10 +451,16 @@ void proj_plane(Warp& w, const View& v, uint32_t plane) {
         if (col == kEmpty) continue;
         float p[3] = {sb[s * 4 + 0] - v.pos[0], sb[s * 4 + 1] - v.pos[1], sb[s * 4 + 2] - v.pos[2]};
         float ph[3] = {dot3(p, v.vx), dot3(p, v.vy), dot3(p, v.vz)};
-        if (ph[2] < 0.05f) continue;  // (double)z < 0.05 <=> z < 0.05f for binary32 z
+        if (ph[2] < 0.05f) {  // (double)z < 0.05 <=> z < 0.05f for binary32 z
+            src[s] = kEmpty;
+            continue;
+        }
         int sx = proj_coord(ph[0] * (float)res_y, ph[2], (float)res_x / 2);
         int sy = proj_coord(ph[1] * (float)res_y, ph[2], (float)res_y / 2);
-        if (sx >= res_x - 1 || sx < 0 || sy >= res_y - 1 || sy < 0) continue;
+        if (sx >= res_x - 1 || sx < 0 || sy >= res_y - 1 || sy < 0) {
+            src[s] = kEmpty;
+            continue;
+        }
         size_t t = (size_t)sy * res_x + sx;
         uint32_t sz = (uint32_t)(int)(ph[2] * 1000.0f) << 8;
         if (sz >= kEmpty) continue;  // cannot beat the cleared value (kernel.cl:571)
@@ -659,9 +668,11 @@ void* orc_warp_create(int res_x, int res_y) {
 }
 void orc_warp_free(void* h) { delete static_cast<Warp*>(h); }
 
-// One raycast_draw (raycast.h:147-441) minus the GL display.
+// One raycast_draw (raycast.h:147-441) minus the GL display. cache_mode 0:
+// the shipped copy target 2 (raycast.h:395); 1: the commented-out
+// alternating target ((frame>>4)%2)+1.
 int orc_warp_frame(void* h, int depth, const uint32_t* words, size_t n_words, uint32_t root, const float* pos4,
-                   const float* m16, int frame, int threads) {
+                   const float* m16, int frame, int threads, int cache_mode) {
     Warp& w = *static_cast<Warp*>(h);
     if (threads > 0) omp_set_num_threads(threads);
     const int res_x = w.res_x, res_y = w.res_y;
@@ -711,12 +722,13 @@ int orc_warp_frame(void* h, int depth, const uint32_t* words, size_t n_words, ui
     w.child_fetches = child;
     w.colour_fetches = col;
     w.boundary_rays = bnd;
-    // raycast.h:394-405: copy plane 0 to cache plane 2
-    std::memcpy(w.screen.data() + 2 * N, w.screen.data(), N * 4);
-    std::memcpy(w.back.data() + 2 * N * 4, w.back.data(), N * 16);
+    // raycast.h:394-405: copy plane 0 to the cache target plane
+    const int target = cache_mode ? ((frame >> 4) % 2) + 1 : 2;
+    std::memcpy(w.screen.data() + (size_t)target * N, w.screen.data(), N * 4);
+    std::memcpy(w.back.data() + (size_t)target * N * 4, w.back.data(), N * 16);
     std::memcpy(w.prefill.data(), w.screen.data(), N * 4);
     // raycast.h:411-422 and 429-437
-    const uint32_t* snap = w.screen.data() + 2 * N;  // identical to plane 0 here
+    const uint32_t* snap = w.screen.data();
     std::vector<uint32_t> lin(2 * N);
     std::memcpy(lin.data(), snap, N * 4);
     std::memcpy(lin.data() + N, w.screen.data() + N, N * 4);  // plane 1 follows plane 0 in memory

@@ -167,3 +167,20 @@ def test_oracle_warp_frames_match_reference(svo, orc, depth, seed, shell, kind, 
         rb, mb = ref.back(), mine.back()
         assert np.array_equal(np.ascontiguousarray(rb[2][ne][:, :3]).view(np.uint32),
                               np.ascontiguousarray(mb[2][ne][:, :3]).view(np.uint32)), f"frame {f}: coords"
+
+
+@needs_ref
+def test_oracle_alternating_cache_target_matches_reference(svo, orc):
+    # raycast.h:395's commented-out target ((frame>>4)%2)+1: both cache planes
+    # are projected and the one not copied into keeps its cleared sources.
+    depth, W, H = 9, 96, 64
+    x, y, z, c = svo.terrain_voxels(41, depth, True)
+    words, root = orc.build_octree(depth, x, y, z, c)
+    ref = orc.Warp(depth, W, H, which="reference")
+    mine = orc.Warp(depth, W, H)
+    for f in range(36):
+        v = svo.camera_path(2, depth, f, W, H)
+        ref.frame(words, root, v.pos_array, v.m_array, f, cache_mode=1)
+        mine.frame(words, root, v.pos_array, v.m_array, f, cache_mode=1)
+        assert np.array_equal(ref.screen(), mine.screen()), f"frame {f}"
+        assert np.array_equal(ref.ids(), mine.ids()) and np.array_equal(ref.tex(), mine.tex())
