@@ -327,138 +327,6 @@ __device__ __forceinline__ void walk(const Octree& o, Walk& w, uint32_t sxyz, fl
     w.rek = rek;
 }
 
-#if SVO_WALK_VARIANT == 3
-template <int DEPTH, bool kFast>
-__device__ __forceinline__ void walk_v3(const Octree& o, Walk& w, uint32_t sxyz, float g0y, float g0z, float g1x,
-                                     float g1z, float g2x, float g2y, float lx, float ly, float lz, float lodswitch,
-                                     uint32_t* stk, int stride, uint32_t& fault) {
-    constexpr int kDepthAnd = (1 << DEPTH) - 1;
-    constexpr int kTopBit = 2 * kDepthAnd + 2;
-    float rpx = w.rpx, rpy = w.rpy, rpz = w.rpz;
-    int rix = float_to_int<kFast>(rpx), riy = float_to_int<kFast>(rpy), riz = float_to_int<kFast>(rpz);
-    int rek = DEPTH, lod = 1;
-    float distance = 0.0f;
-    const uint32_t root = o.root;
-    uint32_t nodeid = root, nodeid_before = root, local_root = 0, node_test = 0;
-    uint32_t steps = 0;
-    auto child_index = [&](int r) -> uint32_t {
-        return ((uint32_t)((rix >> r) & 1) | ((uint32_t)((riy >> r) & 1) << 1) | ((uint32_t)((riz >> r) & 1) << 2)) ^
-               sxyz;
-    };
-    constexpr int kRegLo = 7;
-    constexpr int kRegN = DEPTH - kRegLo > 0 ? DEPTH - kRegLo : 1;
-    uint32_t rs[kRegN];
-#pragma unroll
-    for (int k = 0; k < kRegN; ++k) rs[k] = root;
-    auto push = [&](int level, uint32_t v) {
-        if (level >= kRegLo) {
-#pragma unroll
-            for (int k = 0; k < kRegN; ++k)
-                if (level == kRegLo + k) rs[k] = v;
-        } else {
-            stk[level * stride] = v;
-        }
-    };
-    auto peek = [&](int level) -> uint32_t {
-        if (level >= DEPTH) return root;
-        if (level >= kRegLo) {
-            uint32_t v = root;
-#pragma unroll
-            for (int k = 0; k < kRegN; ++k) v = (level == kRegLo + k) ? rs[k] : v;
-            return v;
-        }
-        return stk[level * stride];
-    };
-    uint32_t ni = child_index(rek);
-    for (;;) {
-        node_test = nodeid & (1u << ni);
-        bool hit = false;
-        while (node_test) {
-            const uint32_t parent = nodeid;
-            const uint32_t n = nodeid >> 9;
-            if (!(nodeid & 256u)) {
-                nodeid = load_word_sel(o, n + ni, fault);
-            } else {
-                const bool enter = !(nodeid_before & 256u);
-                local_root = enter ? (n << 6) : local_root;
-                const uint32_t base = enter ? local_root : local_root + n;
-                const uint32_t nadd = __popc(nodeid & ((node_test << 1) - 1u));
-                if (rek > 2) {
-                    nodeid = load_word_sel(o, base + nadd, fault);
-                } else if (rek == 2) {
-                    const uint32_t wd = load_word_sel(o, base + (nadd >> 2), fault);
-                    nodeid = ((wd >> ((nadd & 3u) << 3)) & 255u) + 256u + (nadd << 9);
-                } else {
-                    nodeid = 0u;
-                }
-            }
-            nodeid_before = parent;
-            if (rek <= lod) {
-                hit = true;
-                break;
-            }
-            --rek;
-            ni = child_index(rek);
-            push(rek, nodeid);
-            node_test = nodeid & (1u << ni);
-        }
-        if (hit) {
-            w.hit = true;
-            w.hcx = rix >> rek;
-            w.hcy = riy >> rek;
-            w.hcz = riz >> rek;
-            break;
-        }
-        if (++steps > kStepCap) {
-            fault |= kFaultSteps;
-            break;
-        }
-        const int p0x = rix >> rek, p0y = riy >> rek, p0z = riz >> rek;
-        const float m0x = __fsub_rn(int_to_float<kFast>((p0x + 1) << rek), rpx);
-        const float m0y = __fsub_rn(int_to_float<kFast>((p0y + 1) << rek), rpy);
-        const float m0z = __fsub_rn(int_to_float<kFast>((p0z + 1) << rek), rpz);
-        float best = __fmul_rn(m0x, lx);
-        const float idy_ = __fmul_rn(m0y, ly), idz_ = __fmul_rn(m0z, lz);
-        float mm = m0x, gx = 1.0f, gy = g0y, gz = g0z;
-        if (idy_ < best) { best = idy_; mm = m0y; gx = g1x; gy = 1.0f; gz = g1z; }
-        if (idz_ < best) { best = idz_; mm = m0z; gx = g2x; gy = g2y; gz = 1.0f; }
-        rpx = __fadd_rn(rpx, __fmul_rn(gx, mm));
-        rpy = __fadd_rn(rpy, __fmul_rn(gy, mm));
-        rpz = __fadd_rn(rpz, __fmul_rn(gz, mm));
-        const int bx = rix, by = riy, bz = riz;
-        rix = float_to_int<kFast>(rpx);
-        riy = float_to_int<kFast>(rpy);
-        riz = float_to_int<kFast>(rpz);
-        distance = __fadd_rn(distance, best);
-        const int x0ry = by ^ riy;
-        const uint32_t x0r = (uint32_t)(((bx ^ rix) ^ x0ry ^ (bz ^ riz)) & kDepthAnd);
-        const bool far = distance > kViewDistMax;
-        if (!far && (x0r >> rek)) {
-            // bit length of x0r (< 2^23) from its exact float exponent
-            rek = (__float_as_int(u23_to_float((int)x0r)) >> 23) - 126;
-            nodeid = peek(rek);
-            nodeid_before = peek(rek + 1);
-            if (distance > lodswitch) {
-                lodswitch = __fmul_rn(lodswitch, 2.0f);
-                ++lod;
-            }
-        }
-        if (far || (x0ry & kTopBit)) break;
-        ni = child_index(rek);
-    }
-    w.rpx = rpx;
-    w.rpy = rpy;
-    w.rpz = rpz;
-    w.distance = distance;
-    w.nodeid = nodeid;
-    w.nodeid_before = nodeid_before;
-    w.local_root = local_root;
-    w.node_test = node_test;
-    w.rek = rek;
-}
-
-#endif
-
 // Ray setup of raycast_fine_2/raycast_holes (kernel.cl:883-899) + CAST_RAY +
 // the colour fetch. `stk` points at this thread's column of the shared stack
 // (entry for level L at stk[L * stride]); levels 1..DEPTH-1 are used.
@@ -502,17 +370,10 @@ __device__ __forceinline__ RayResult trace_ray(const Octree& o, const RayCam& c,
     w.hcx = w.hcy = w.hcz = 0;
     const float lim = 4194304.0f;  // 2^22
     const bool fast = rpx >= 0.0f && rpx < lim && rpy >= 0.0f && rpy < lim && rpz >= 0.0f && rpz < lim;
-#if SVO_WALK_VARIANT == 3
-    if (fast)
-        walk_v3<DEPTH, true>(o, w, sxyz, g0y, g0z, g1x, g1z, g2x, g2y, lx, ly, lz, lodswitch, stk, stride, fault);
-    else
-        walk_v3<DEPTH, false>(o, w, sxyz, g0y, g0z, g1x, g1z, g2x, g2y, lx, ly, lz, lodswitch, stk, stride, fault);
-#else
     if (fast)
         walk<DEPTH, true>(o, w, sxyz, g0y, g0z, g1x, g1z, g2x, g2y, lx, ly, lz, lodswitch, stk, stride, fault);
     else
         walk<DEPTH, false>(o, w, sxyz, g0y, g0z, g1x, g1z, g2x, g2y, lx, ly, lz, lodswitch, stk, stride, fault);
-#endif
     rpx = w.rpx;
     rpy = w.rpy;
     rpz = w.rpz;
