@@ -53,6 +53,7 @@ def parse_args(argv=None):
     ap.add_argument("--cpu-frames", type=int, default=-1, help="oracle frames for the CPU baseline (-1: all)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (for profiling runs)")
     ap.add_argument("--graph", type=int, default=1, help="replay each warp frame as a CUDA graph")
+    ap.add_argument("--views", type=int, default=8, help="camera streams of the concurrent multi-view measurement")
     return ap.parse_args(argv)
 
 
@@ -323,6 +324,51 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     tgt4.close()
     psnr_mean = float(np.mean([p for p in psnr if np.isfinite(p)])) if psnr else None
 
+    # ---- several camera streams at once: one context (stream) per view, the
+    # octree words shared; the warp frames of all views are in flight together
+    # so one view's latency tail overlaps the others' work.
+    multiview = None
+    if args.views > 1:
+        d_words = torch.from_numpy(octree.words.view(np.int32)).to(device)
+        torch.cuda.synchronize(device)
+        ctxs, tgts = [], []
+        for k in range(args.views):
+            c = svo.Context(local_rank)
+            c.upload_device(d_words.data_ptr(), octree.words.size, octree.root, octree.depth)
+            t = c.target(W, H)
+            if args.graph:
+                t.use_graph(True)
+            ctxs.append(c)
+            tgts.append(t)
+
+        def mv_view(k, f):
+            return svo.camera_path(1, depth, frame_offset + 37 * k + f, W, H)
+
+        for f in range(args.warmup):
+            for k in range(args.views):
+                ctxs[k].warp_frame(tgts[k], mv_view(k, f), f)
+        for c in ctxs:
+            c.synchronize()
+        mv_s = 0.0
+        for i in range(args.steps):
+            f = args.warmup + i
+            views = [mv_view(k, f) for k in range(args.views)]
+            flush_l2()
+            t0 = time.perf_counter()
+            for k in range(args.views):
+                ctxs[k].warp_frame(tgts[k], views[k], f)
+            for c in ctxs:
+                c.synchronize()
+            mv_s += time.perf_counter() - t0
+        multiview = {"views": args.views, "frames_per_s": args.views * args.steps / mv_s,
+                     "ms_per_step": 1000.0 * mv_s / args.steps,
+                     "note": "host-timed: all views' warp frames launched, then every stream synchronised"}
+        for t in tgts:
+            t.close()
+        for c in ctxs:
+            c.close()
+        del d_words
+
     # ---- CPU oracle on the same frames: parity of the last frame, fetch
     # counts for the roofline's algorithmic bytes, and the CPU baseline.
     cpu = None
@@ -391,6 +437,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
             "psnr_db_vs_full": psnr_mean,
             "hole_pixel_fraction": float(np.mean(traced_frac)) if traced_frac else None,
             "stage_ms": stage_ms,
+            "multiview": multiview,
             "parity_last_frame_vs_oracle": parity,
             "octree_build_s": t_build,
         }

@@ -71,7 +71,9 @@ typedef struct svo_builder svo_builder;
 /* Replaces ocl_init (src/ocl.h:57-146) and the device half of raycast_init
  * (src/raycast.h:61-91). Creates a stream on `device`. */
 svo_status svo_context_create(int device, svo_context** out);
-/* Replaces raycast_exit (src/raycast.h:511-517) and ocl_exit (src/ocl.h:168-174). */
+/* Replaces raycast_exit (src/raycast.h:511-517) and ocl_exit (src/ocl.h:168-174).
+ * Also destroys every render target of the context still alive; their
+ * handles are invalid afterwards. */
 svo_status svo_context_destroy(svo_context* ctx);
 /* Human-readable text of the last failure on this context (never null). */
 const char* svo_last_error(const svo_context* ctx);
@@ -119,6 +121,8 @@ svo_status svo_octree_set_l2_window(svo_context* ctx, size_t bytes);
  * displayed colour plane and the BGRX8 image that replaces the PBO
  * (mem_screenbuffer_tex, :88-89). res_x, res_y <= 65535. */
 svo_status svo_target_create(svo_context* ctx, int res_x, int res_y, svo_target** out);
+/* Destroy a target before its context (svo_context_destroy destroys the
+ * targets left over). */
 svo_status svo_target_destroy(svo_target* t);
 
 /* ----------------------------------------------------------- frames ---- */

@@ -43,6 +43,7 @@ struct svo_context {
     size_t l2_window_request = ~(size_t)0;  // default: the whole octree
     bool stage_normal = true;               // stage the normal-node region in shared memory
     uint64_t launches = 0;
+    std::vector<svo_target*> targets;  // live targets, destroyed with the context
     std::string err;
 };
 
@@ -73,6 +74,25 @@ struct svo_target {
 };
 
 namespace {
+
+// The persisting-L2 set-aside is one setting of the CUDA context, which every
+// svo_context on a device shares; it is released only when the last context
+// holding a window gives it up.
+std::mutex g_l2_mutex;
+int g_l2_users[64] = {};
+
+void l2_window_acquire(int device) {
+    std::lock_guard<std::mutex> lock(g_l2_mutex);
+    if (device >= 0 && device < 64) ++g_l2_users[device];
+}
+void l2_window_release(int device) {
+    std::lock_guard<std::mutex> lock(g_l2_mutex);
+    if (device < 0 || device >= 64 || g_l2_users[device] <= 0) return;
+    if (--g_l2_users[device] == 0) {
+        cudaCtxResetPersistingL2Cache();
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
+    }
+}
 
 const char* status_text(svo_status s) {
     switch (s) {
@@ -383,12 +403,10 @@ svo_status svo_context_create(int device, svo_context** out) {
 
 svo_status svo_context_destroy(svo_context* ctx) {
     if (!ctx) return SVO_OK;
+    while (!ctx->targets.empty()) svo_target_destroy(ctx->targets.back());
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    if (ctx->l2_window > 0) {
-        cudaCtxResetPersistingL2Cache();
-        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
-    }
+    if (ctx->l2_window > 0) l2_window_release(ctx->device);
     if (ctx->owns_octree && ctx->d_octree) cudaFree(ctx->d_octree);
     if (ctx->d_fault) cudaFree(ctx->d_fault);
     if (ctx->d_counter) cudaFree(ctx->d_counter);
@@ -495,10 +513,8 @@ svo_status svo_octree_set_l2_window(svo_context* ctx, size_t bytes) {
         attr.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
     }
     SVO_CUDA(ctx, cudaStreamSetAttribute(ctx->stream, cudaStreamAttributeAccessPolicyWindow, &attr));
-    if (bytes == 0 && ctx->l2_window > 0) {
-        SVO_CUDA(ctx, cudaCtxResetPersistingL2Cache());
-        SVO_CUDA(ctx, cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0));
-    }
+    if (bytes > 0 && ctx->l2_window == 0) l2_window_acquire(ctx->device);
+    if (bytes == 0 && ctx->l2_window > 0) l2_window_release(ctx->device);
     ctx->l2_window = bytes;
     return SVO_OK;
 }
@@ -553,6 +569,7 @@ svo_status svo_target_create(svo_context* ctx, int res_x, int res_y, svo_target*
     SVO_CUDA(ctx, cudaMemsetAsync(t->B.disp, 0xff, N * 4, s));
     for (auto& e : t->ev) SVO_CUDA(ctx, cudaEventCreate(&e));
     SVO_CUDA(ctx, cudaStreamSynchronize(s));
+    ctx->targets.push_back(t);
     *out = t;
     return SVO_OK;
 }
@@ -570,6 +587,8 @@ svo_status svo_target_destroy(svo_target* t) {
         if (p) cudaFree(p);
     for (auto& e : t->ev)
         if (e) cudaEventDestroy(e);
+    auto it = std::find(ctx->targets.begin(), ctx->targets.end(), t);
+    if (it != ctx->targets.end()) ctx->targets.erase(it);
     delete t;
     return SVO_OK;
 }

@@ -9,8 +9,10 @@ library (or without a GPU for the device calls) the calls fail loudly.
 """
 from __future__ import annotations
 
+import atexit
 import ctypes
 import os
+import weakref
 from typing import Sequence
 
 import numpy as np
@@ -294,9 +296,11 @@ class Context:
     def __init__(self, device: int = 0):
         self._lib = load()
         self._h = _P()
+        self._targets: "weakref.WeakSet[Target]" = weakref.WeakSet()
         _check(self._lib.svo_context_create(device, ctypes.byref(self._h)), None,
                f"svo_context_create(device={device}) failed")
         self.octree: Octree | None = None
+        _LIVE_CONTEXTS.add(self)
 
     @property
     def handle(self):
@@ -342,12 +346,26 @@ class Context:
         _check(self._lib.svo_warp_frame(self._h, target._h, ctypes.byref(view), frame), self)
 
     def close(self) -> None:
+        """Destroy the context; its targets still open are closed first."""
         if getattr(self, "_h", None):
+            for t in list(getattr(self, "_targets", ())):
+                t.close()
             self._lib.svo_context_destroy(self._h)
             self._h = None
 
     def __del__(self):
         self.close()
+
+
+# Contexts still open at interpreter exit are closed while every module is
+# intact, whatever order the interpreter would finalise the objects in.
+_LIVE_CONTEXTS: "weakref.WeakSet[Context]" = weakref.WeakSet()
+
+
+@atexit.register
+def _close_live_contexts() -> None:
+    for c in list(_LIVE_CONTEXTS):
+        c.close()
 
 
 class Target:
@@ -358,6 +376,7 @@ class Target:
         self._lib = ctx._lib
         self._h = _P()
         _check(self._lib.svo_target_create(ctx._h, res_x, res_y, ctypes.byref(self._h)), ctx)
+        ctx._targets.add(self)
         self.res_x, self.res_y = res_x, res_y
         self.n = res_x * res_y
         self.tiles = (res_x // 16) * (res_y // 16)
@@ -416,7 +435,8 @@ class Target:
 
     def close(self) -> None:
         if getattr(self, "_h", None):
-            self._lib.svo_target_destroy(self._h)
+            if getattr(self.ctx, "_h", None):  # a closed context already destroyed its targets
+                self._lib.svo_target_destroy(self._h)
             self._h = None
 
     def __del__(self):

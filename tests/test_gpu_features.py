@@ -188,3 +188,55 @@ def test_reference_named_cpp_interface(svo, tmp_path):
     assert "frames=6" in out.stdout
     nonblack = int(out.stdout.split("nonblack=")[1])
     assert nonblack > 256 * 160 // 4
+
+
+def test_concurrent_camera_streams_share_one_octree(svo, scene, gpu_ctx):
+    # One context per camera stream, the octree words uploaded once and shared;
+    # frames of all streams in flight together give the same images as one
+    # stream at a time.
+    torch = pytest.importorskip("torch")
+    octree = scene(9, 5, True)
+    d_words = torch.from_numpy(octree.words.view(np.int32)).cuda()
+    torch.cuda.synchronize()
+    ctxs = [svo.Context(0) for _ in range(3)]
+    for c in ctxs:
+        c.upload_device(d_words.data_ptr(), octree.words.size, octree.root, octree.depth)
+    tgts = [c.target(128, 96) for c in ctxs]
+    gpu_ctx.upload(octree)
+    for f in range(12):
+        for k, (c, t) in enumerate(zip(ctxs, tgts)):
+            c.warp_frame(t, svo.camera_path(2, 9, 5 * k + f, 128, 96), f)
+        for c in ctxs:
+            c.synchronize()
+    for k, t in enumerate(tgts):
+        s2 = gpu_ctx.target(128, 96)
+        for f in range(12):
+            gpu_ctx.warp_frame(s2, svo.camera_path(2, 9, 5 * k + f, 128, 96), f)
+        gpu_ctx.synchronize()
+        assert np.array_equal(t.bgrx(), s2.bgrx()) and np.array_equal(t.colour(2), s2.colour(2))
+        s2.close()
+    for t in tgts:
+        t.close()
+    for c in ctxs:
+        c.close()
+
+
+def test_context_close_destroys_live_targets(svo, scene):
+    # Closing a context first destroys the targets it still owns; closing such
+    # a target afterwards is a no-op, and so is the C-level destroy order
+    # context-then-nothing.
+    octree = scene(8, 99, True)
+    ctx = svo.Context(0)
+    ctx.upload(octree)
+    t = ctx.target(64, 32)
+    ctx.raycast_full(t, svo.camera_path(1, 8, 3, 64, 32))
+    ctx.synchronize()
+    ctx.close()
+    t.close()
+    lib = svo.load()
+    import ctypes
+    h, th = ctypes.c_void_p(), ctypes.c_void_p()
+    assert lib.svo_context_create(0, ctypes.byref(h)) == 0
+    assert lib.svo_target_create(h, 32, 16, ctypes.byref(th)) == 0
+    assert lib.svo_context_destroy(h) == 0
+
