@@ -65,6 +65,7 @@ typedef struct svo_view {
 typedef struct svo_context svo_context;
 typedef struct svo_target svo_target;
 typedef struct svo_builder svo_builder;
+typedef struct svo_net svo_net;
 
 /* ----------------------------------------------------------- context -- */
 
@@ -72,8 +73,8 @@ typedef struct svo_builder svo_builder;
  * (src/raycast.h:61-91). Creates a stream on `device`. */
 svo_status svo_context_create(int device, svo_context** out);
 /* Replaces raycast_exit (src/raycast.h:511-517) and ocl_exit (src/ocl.h:168-174).
- * Also destroys every render target of the context still alive; their
- * handles are invalid afterwards. */
+ * Also destroys every render target and net of the context still alive;
+ * their handles are invalid afterwards. */
 svo_status svo_context_destroy(svo_context* ctx);
 /* Human-readable text of the last failure on this context (never null). */
 const char* svo_last_error(const svo_context* ctx);
@@ -147,8 +148,9 @@ svo_status svo_raycast_full_batch(svo_context* ctx, svo_target* const* targets, 
 svo_status svo_warp_frame(svo_context* ctx, svo_target* t, const svo_view* view, int frame);
 
 /* Capture the warp frame of this target as a CUDA graph on first use and
- * replay it on later calls (per-frame parameters travel through one small
- * host-to-device copy inside the graph). enable = 0 returns to direct launches. */
+ * replay it on later calls (the per-frame parameters are the arguments of
+ * the graph's first kernel node, updated before each replay). Plain and
+ * learned frames keep one graph each. enable = 0 returns to direct launches. */
 svo_status svo_target_use_graph(svo_target* t, int enable);
 
 /* Per-stage CUDA-event timing of the next frames on this target (replaces
@@ -156,7 +158,8 @@ svo_status svo_target_use_graph(svo_target* t, int enable);
 svo_status svo_target_set_profiling(svo_target* t, int enable);
 /* Milliseconds of each stage of the last profiled frame. Warp frames fill
  * [0] project, [1] resolve+gather, [2] scan, [3] hole list, [4] trace,
- * [5] filter+colourise; full raycasts fill [4] trace and [5] colourise.
+ * [5] filter+colourise; full raycasts fill [4] trace and [5] colourise;
+ * learned frames fill [0] project, [1] resolve, [2] net, [3] trace.
  * Synchronises the stream. Returns the number of stages written. */
 int svo_target_stage_times(svo_target* t, float* ms, int cap);
 
@@ -195,6 +198,58 @@ typedef struct svo_device_outputs {
     uint64_t* full_voxel;  /* full raycast packed hit voxels */
 } svo_device_outputs;
 svo_status svo_target_device_outputs(svo_target* t, svo_device_outputs* out);
+
+/* ------------------------------------------- learned reconstruction -- */
+/* No counterpart in the reference, which fills reprojection holes with a
+ * fixed filter (raycast_fillhole2, kernel/kernel.cl:404-470) and traces every
+ * 2x2 hole block (raycast_counthole/writeids/holes, :234-340,594-694). A
+ * learned frame reprojects like svo_warp_frame, then a small convolutional
+ * net (inputs: warped colour, depth, hole mask, reprojection motion; outputs:
+ * colour and a confidence) runs on the tensor cores over the whole frame;
+ * pixels whose confidence is below `threshold` (0..1, e.g. 0.5) are traced,
+ * together with the 8x4 refresh tile, and show the traced colour; the others
+ * show the net's colour. The current plane (reprojected + traced pixels)
+ * becomes the next frame's cache. Output: the target's BGRX image.
+ * Asynchronous on the context stream. */
+svo_status svo_warp_frame_learned(svo_context* ctx, svo_target* t, const svo_view* view, int frame,
+                                  const svo_net* net, float threshold);
+/* Rays the net requested in the target's last learned frame (synchronises). */
+svo_status svo_read_requested(svo_target* t, uint32_t* count);
+/* Training tap: when d_features is not NULL, every later frame of the target
+ * (plain or learned) writes the net's input features after reprojection to
+ * this device buffer, planar [8][res_y*res_x] FP32. */
+svo_status svo_target_set_feature_tap(svo_target* t, float* d_features);
+
+/* The net's parameters: SVO_NET_PARAMS FP32 values, per layer l = 0..3 the
+ * weights [9 taps (dy+1)*3+(dx+1)][c_in][c_out] then the biases [c_out];
+ * channels 8 -> 16 -> 16 -> 16 -> 4. */
+#define SVO_NET_PARAMS 6388
+/* Creates a net on the context, initialised by svo_net_init(net, 1). */
+svo_status svo_net_create(svo_context* ctx, svo_net** out);
+svo_status svo_net_destroy(svo_net* net);
+/* Seeded He-normal weights (last layer scaled by 0.1), zero biases; resets
+ * the optimiser. */
+svo_status svo_net_init(svo_net* net, uint64_t seed);
+/* n must be SVO_NET_PARAMS. set_params resets the optimiser. */
+svo_status svo_net_set_params(svo_net* net, const float* host, size_t n);
+svo_status svo_net_get_params(svo_net* net, float* host, size_t n);
+/* Gradient of the last svo_net_backward. */
+svo_status svo_net_get_grads(svo_net* net, float* host, size_t n);
+/* Forward passes over a planar feature image (device pointers; features
+ * [8][h*w], outputs [4][h*w]: R, G, B, confidence logit). svo_net_forward is
+ * the FP32 CUDA-core path used in training; svo_net_infer is the tensor-core
+ * kernel of learned frames. */
+svo_status svo_net_forward(svo_net* net, const float* d_features, int w, int h, float* d_out);
+svo_status svo_net_infer(svo_net* net, const float* d_features, int w, int h, float* d_out);
+/* Forward + loss + backward over one frame: the target is a BGRX8 image
+ * (device pointer, e.g. the full raycast of the same view). Loss per pixel:
+ * mean squared colour error over R, G, B plus lambda * binary cross-entropy
+ * of the confidence against "every colour channel within tau". loss (host,
+ * may be NULL) receives the two mean terms. Synchronises when loss != NULL. */
+svo_status svo_net_backward(svo_net* net, const float* d_features, const uint32_t* d_target_bgrx, int w, int h,
+                            float tau, float lambda, float* loss);
+/* One Adam step with the last gradient (asynchronous). */
+svo_status svo_net_adam(svo_net* net, float lr, float beta1, float beta2, float eps);
 
 /* ----------------------------------------------- allocation-free call -- */
 /* No counterpart in the reference. A full raycast (as svo_raycast_full, one

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -18,6 +19,7 @@
 
 #include "../../include/svo_gb300.h"
 #include "svo_kernels.cuh"
+#include "svo_net.cuh"
 
 using namespace svo;
 
@@ -44,7 +46,27 @@ struct svo_context {
     bool stage_normal = true;               // stage the normal-node region in shared memory
     uint64_t launches = 0;
     std::vector<svo_target*> targets;  // live targets, destroyed with the context
+    std::vector<svo_net*> nets;        // live nets, likewise
     std::string err;
+};
+
+// A captured frame and what its capture baked in.
+struct FrameGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaGraphNode_t params_node = nullptr;
+    uint64_t launches = 0;  // kernels one replay launches
+    bool profiled = false;
+    const void* net = nullptr;
+    float threshold = 0.0f;
+    float* tap = nullptr;
+    void reset() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        exec = nullptr;
+        graph = nullptr;
+        params_node = nullptr;
+    }
 };
 
 struct svo_target {
@@ -59,18 +81,43 @@ struct svo_target {
     uint64_t frames = 0;      // warp frames issued (parity of the current plane)
     int last_cur = 0;
     bool have_prev = false;
-    // CUDA graph of one warp frame
+    // previous frame's camera (motion feature of learned frames)
+    svo_view prev_view{};
+    bool have_prev_view = false;
+    float* feature_tap = nullptr;  // device [8][N]: features written after reprojection
+    // CUDA graphs of one warp frame: [0] plain, [1] learned
     bool use_graph = false;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t graph_exec = nullptr;
-    cudaGraphNode_t params_node = nullptr;
-    bool graph_profiled = false;
+    FrameGraph graphs[2];
     bool capturing = false;
     // per-stage timing
     bool profiling = false;
     cudaEvent_t ev[8] = {};
     int n_events = 0;
-    int last_mode = 0;  // 1 warp, 2 full
+    int last_mode = 0;  // 1 warp, 2 full, 3 learned warp
+};
+
+// The reconstruction net: FP32 master parameters with Adam moments, their
+// bf16 forms for the kernels, and the training buffers (grown on demand).
+struct svo_net {
+    svo_context* ctx = nullptr;
+    float* params = nullptr;
+    float* m = nullptr;
+    float* v = nullptr;
+    float* grads = nullptr;
+    float* wr = nullptr;         // bf16-rounded weights, FP32 (CUDA-core path)
+    uint16_t* packed = nullptr;  // tensor-core operand image
+    float* bias = nullptr;       // 52 biases
+    int step = 0;
+    size_t cap = 0;           // pixels the training buffers hold
+    float* act = nullptr;     // 3 hidden activations, 16 planes each
+    float* out = nullptr;     // 4 planes
+    float* dout = nullptr;    // 4 planes
+    float* g0 = nullptr;      // 16 planes
+    float* g1 = nullptr;      // 16 planes
+    float* partial = nullptr;  // weight-gradient partial sums
+    size_t partial_cap = 0;    // floats
+    float* loss_partial = nullptr;
+    size_t loss_cap = 0;  // blocks
 };
 
 namespace {
@@ -222,24 +269,30 @@ struct TraceLaunch {
     Octree o;
 };
 
+// Trace kernels: full raycast, warp-frame holes + refresh tile, and the same
+// for learned frames (which also write the traced pixels' BGRX).
+enum TraceKind { kTraceFull = 0, kTraceWarp = 1, kTraceWarpBgrx = 2 };
+
 template <int DEPTH, int BLOCK>
-const void* trace_fn(bool warp) {
-    return warp ? (const void*)k_trace_warp<DEPTH, BLOCK> : (const void*)k_trace_full<DEPTH, BLOCK, true>;
+const void* trace_fn(int kind) {
+    if (kind == kTraceWarp) return (const void*)k_trace_warp<DEPTH, BLOCK, false>;
+    if (kind == kTraceWarpBgrx) return (const void*)k_trace_warp<DEPTH, BLOCK, true>;
+    return (const void*)k_trace_full<DEPTH, BLOCK, true>;
 }
 
 template <int BLOCK>
-const void* trace_fn_depth(int depth, bool warp) {
+const void* trace_fn_depth(int depth, int kind) {
     switch (depth) {
-        case 8: return trace_fn<8, BLOCK>(warp);
-        case 9: return trace_fn<9, BLOCK>(warp);
-        case 10: return trace_fn<10, BLOCK>(warp);
-        case 11: return trace_fn<11, BLOCK>(warp);
-        case 12: return trace_fn<12, BLOCK>(warp);
+        case 8: return trace_fn<8, BLOCK>(kind);
+        case 9: return trace_fn<9, BLOCK>(kind);
+        case 10: return trace_fn<10, BLOCK>(kind);
+        case 11: return trace_fn<11, BLOCK>(kind);
+        case 12: return trace_fn<12, BLOCK>(kind);
     }
     return nullptr;
 }
 
-svo_status plan_trace(svo_context* ctx, bool warp, TraceLaunch& L) {
+svo_status plan_trace(svo_context* ctx, int kind, TraceLaunch& L) {
     L.o = Octree{ctx->d_octree, (uint32_t)ctx->n_words, ctx->root, 0u, 0u};
     uint32_t stage_bytes = 0;
     if (ctx->stage_normal && !(ctx->root & 256u) && (reinterpret_cast<uintptr_t>(ctx->d_octree) & 15u) == 0) {
@@ -251,7 +304,7 @@ svo_status plan_trace(svo_context* ctx, bool warp, TraceLaunch& L) {
         }
     }
     L.block = stage_bytes > kStageSmallBytes ? 1024 : 256;
-    L.fn = L.block == 1024 ? trace_fn_depth<1024>(ctx->depth, warp) : trace_fn_depth<256>(ctx->depth, warp);
+    L.fn = L.block == 1024 ? trace_fn_depth<1024>(ctx->depth, kind) : trace_fn_depth<256>(ctx->depth, kind);
     if (!L.fn) return fail(ctx, SVO_ERR_NOT_SUPPORTED, "octree depth");
     L.smem = (size_t)(ctx->depth + 1) * L.block * 4u + stage_bytes;
     SVO_CUDA(ctx, cudaFuncSetAttribute(L.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
@@ -286,15 +339,15 @@ svo_status launch_trace(svo_context* ctx, const TraceLaunch& L, void** args) {
 
 svo_status launch_trace_full(svo_context* ctx, FullBatch* d_batch) {
     TraceLaunch L;
-    svo_status st = plan_trace(ctx, false, L);
+    svo_status st = plan_trace(ctx, kTraceFull, L);
     if (st != SVO_OK) return st;
     void* args[] = {&L.o, &d_batch, &ctx->d_counter, &ctx->d_fault};
     return launch_trace(ctx, L, args);
 }
 
-svo_status launch_trace_warp(svo_context* ctx, svo_target* t) {
+svo_status launch_trace_warp(svo_context* ctx, svo_target* t, bool bgrx = false) {
     TraceLaunch L;
-    svo_status st = plan_trace(ctx, true, L);
+    svo_status st = plan_trace(ctx, bgrx ? kTraceWarpBgrx : kTraceWarp, L);
     if (st != SVO_OK) return st;
     void* args[] = {&L.o, &t->d_params, &t->B, &ctx->d_fault};
     return launch_trace(ctx, L, args);
@@ -327,6 +380,13 @@ FrameParams make_params(const svo_target* t, const svo_view& v, int frame, int c
     const int gx = (rx / 8 + 15) / 16 * 16, gy = (ry / 4 + 15) / 16 * 16;
     p.x_end = std::min(rx, p.add_x + gx);
     p.y_end = std::min(ry, p.add_y + gy);
+    p.have_prev_view = t->have_prev_view ? 1 : 0;
+    for (int i = 0; i < 3; ++i) {
+        p.prev_pos[i] = t->prev_view.pos[i];
+        p.prev_vx[i] = t->prev_view.m[0 + i];
+        p.prev_vy[i] = t->prev_view.m[4 + i];
+        p.prev_vz[i] = t->prev_view.m[8 + i];
+    }
     return p;
 }
 
@@ -344,6 +404,10 @@ svo_status enqueue_warp_body(svo_context* ctx, svo_target* t) {
     record(t, 1);
     k_resolve_gather<<<dim3((res_x + 15) / 16, (res_y + 15) / 16), 256, 0, s>>>(t->d_params, t->B);
     SVO_LAUNCHED(ctx);
+    if (t->feature_tap) {
+        k_net_features<<<dim3((res_x + 31) / 32, (res_y + 7) / 8), 256, 0, s>>>(t->d_params, t->B, t->feature_tap);
+        SVO_LAUNCHED(ctx);
+    }
     record(t, 2);
     k_hole_scan<<<1, 1024, 0, s>>>(t->B);
     SVO_LAUNCHED(ctx);
@@ -359,6 +423,205 @@ svo_status enqueue_warp_body(svo_context* ctx, svo_target* t) {
     k_fill_colorize<<<dim3((res_x + 31) / 32, (res_y + 7) / 8), 256, 0, s>>>(t->d_params, t->B);
     SVO_LAUNCHED(ctx);
     record(t, 6);
+    return SVO_OK;
+}
+
+// Tensor-core inference launch: one CTA per SM over the 56x24 output tiles.
+svo_status launch_net_infer(svo_context* ctx, const svo_net* net, bool pipeline, NetInferArgs& A) {
+    A.packed = net->packed;
+    A.bias = net->bias;
+    A.tiles_x = (A.w + kNetOutW - 1) / kNetOutW;
+    A.tiles = A.tiles_x * ((A.h + kNetOutH - 1) / kNetOutH);
+    A.fault = ctx->d_fault;
+    const void* fn = pipeline ? (const void*)k_net_infer<true> : (const void*)k_net_infer<false>;
+    SVO_CUDA(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kNetSmemBytes));
+    const int grid = std::max(1, std::min(A.tiles, ctx->sm_count));
+    void* args[] = {&A};
+    SVO_CUDA(ctx, cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kNetThreads), args, kNetSmemBytes, ctx->stream));
+    ++ctx->launches;
+    return SVO_OK;
+}
+
+// The launch sequence of one learned warp frame after k_set_params:
+// reprojection as in the plain frame, then the net (colour for every pixel,
+// a ray request for every pixel below the threshold), then the tracer over
+// the requests and the refresh tile. Nothing is filtered or copied: the
+// current plane keeps reprojected and traced pixels and becomes the cache.
+svo_status enqueue_learned_body(svo_context* ctx, svo_target* t, const svo_net* net, float logit_threshold) {
+    cudaStream_t s = ctx->stream;
+    const int res_x = t->res_x, res_y = t->res_y;
+    record(t, 0);
+    {
+        const int threads = 256;
+        int blocks = (int)std::min<size_t>((t->N + threads - 1) / threads, (size_t)ctx->sm_count * 8);
+        k_project<<<blocks, threads, 0, s>>>(t->d_params, t->B);
+        SVO_LAUNCHED(ctx);
+    }
+    record(t, 1);
+    k_resolve_gather<<<dim3((res_x + 15) / 16, (res_y + 15) / 16), 256, 0, s>>>(t->d_params, t->B);
+    SVO_LAUNCHED(ctx);
+    if (t->feature_tap) {
+        k_net_features<<<dim3((res_x + 31) / 32, (res_y + 7) / 8), 256, 0, s>>>(t->d_params, t->B, t->feature_tap);
+        SVO_LAUNCHED(ctx);
+    }
+    record(t, 2);
+    NetInferArgs A{};
+    A.P = t->d_params;
+    A.B = t->B;
+    A.w = res_x;
+    A.h = res_y;
+    A.logit_threshold = logit_threshold;
+    svo_status st = launch_net_infer(ctx, net, true, A);
+    if (st != SVO_OK) return st;
+    record(t, 3);
+    st = launch_trace_warp(ctx, t, true);
+    if (st != SVO_OK) return st;
+    record(t, 4);
+    return SVO_OK;
+}
+
+// Runs one frame: k_set_params then `body`, directly or as a CUDA graph that
+// is captured once per configuration and replayed with new parameters.
+template <class Body>
+svo_status run_frame(svo_context* ctx, svo_target* t, const FrameParams& p, FrameGraph& g, const void* net,
+                     float threshold, Body body) {
+    cudaStream_t s = ctx->stream;
+    if (!t->use_graph) {
+        k_set_params<<<1, 1, 0, s>>>(p, t->d_params, t->B.counters);
+        SVO_LAUNCHED(ctx);
+        return body();
+    }
+    if (!g.exec || g.profiled != t->profiling || g.net != net || g.threshold != threshold || g.tap != t->feature_tap) {
+        g.reset();
+        const uint64_t l0 = ctx->launches;
+        SVO_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        t->capturing = true;
+        k_set_params<<<1, 1, 0, s>>>(p, t->d_params, t->B.counters);
+        svo_status st = body();
+        t->capturing = false;
+        cudaGraph_t gr = nullptr;
+        cudaError_t ce = cudaStreamEndCapture(s, &gr);
+        g.launches = ctx->launches - l0 + 1;
+        ctx->launches = l0;
+        if (st != SVO_OK) {
+            if (gr) cudaGraphDestroy(gr);
+            return st;
+        }
+        if (ce != cudaSuccess) return fail(ctx, SVO_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(ce));
+        g.graph = gr;
+        SVO_CUDA(ctx, cudaGraphInstantiate(&g.exec, gr, 0));
+        // Find the k_set_params node (the only root of the graph).
+        size_t nroots = 0;
+        SVO_CUDA(ctx, cudaGraphGetRootNodes(gr, nullptr, &nroots));
+        std::vector<cudaGraphNode_t> roots(nroots);
+        SVO_CUDA(ctx, cudaGraphGetRootNodes(gr, roots.data(), &nroots));
+        for (auto nd : roots) {
+            cudaGraphNodeType ty;
+            if (cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) {
+                cudaKernelNodeParams kp;
+                if (cudaGraphKernelNodeGetParams(nd, &kp) == cudaSuccess && kp.func == (void*)k_set_params)
+                    g.params_node = nd;
+            }
+        }
+        if (!g.params_node) return fail(ctx, SVO_ERR_CUDA, "graph: parameter node not found");
+        g.profiled = t->profiling;
+        g.net = net;
+        g.threshold = threshold;
+        g.tap = t->feature_tap;
+    }
+    cudaKernelNodeParams kp;
+    SVO_CUDA(ctx, cudaGraphKernelNodeGetParams(g.params_node, &kp));
+    FrameParams pc = p;
+    FrameParams* dst = t->d_params;
+    uint32_t* cnt = t->B.counters;
+    void* args[] = {&pc, &dst, &cnt};
+    kp.kernelParams = args;
+    kp.extra = nullptr;
+    SVO_CUDA(ctx, cudaGraphExecKernelNodeSetParams(g.exec, g.params_node, &kp));
+    SVO_CUDA(ctx, cudaGraphLaunch(g.exec, s));
+    ctx->launches += g.launches;
+    return SVO_OK;
+}
+
+svo_status net_reserve(svo_net* net, size_t n) {
+    svo_context* ctx = net->ctx;
+    if (n > net->cap) {
+        cudaFree(net->act);
+        cudaFree(net->out);
+        cudaFree(net->dout);
+        cudaFree(net->g0);
+        cudaFree(net->g1);
+        net->act = net->out = net->dout = net->g0 = net->g1 = nullptr;
+        net->cap = 0;
+        SVO_CUDA(ctx, cudaMalloc(&net->act, 48 * n * 4));
+        SVO_CUDA(ctx, cudaMalloc(&net->out, 4 * n * 4));
+        SVO_CUDA(ctx, cudaMalloc(&net->dout, 4 * n * 4));
+        SVO_CUDA(ctx, cudaMalloc(&net->g0, 16 * n * 4));
+        SVO_CUDA(ctx, cudaMalloc(&net->g1, 16 * n * 4));
+        net->cap = n;
+    }
+    const size_t blocks = (n + kNetChunk - 1) / kNetChunk;
+    const size_t need = blocks * (9 * 16 * 16 + 16);
+    if (need > net->partial_cap) {
+        cudaFree(net->partial);
+        net->partial = nullptr;
+        net->partial_cap = 0;
+        SVO_CUDA(ctx, cudaMalloc(&net->partial, need * 4));
+        net->partial_cap = need;
+    }
+    const size_t lb = (n + 255) / 256;
+    if (lb > net->loss_cap) {
+        cudaFree(net->loss_partial);
+        net->loss_partial = nullptr;
+        net->loss_cap = 0;
+        SVO_CUDA(ctx, cudaMalloc(&net->loss_partial, lb * 2 * 4));
+        net->loss_cap = lb;
+    }
+    return SVO_OK;
+}
+
+svo_status net_prepare(svo_net* net) {
+    k_net_prepare<<<(kNetMmaTotal * 256 + 255) / 256, 256, 0, net->ctx->stream>>>(net->params, net->wr, net->packed,
+                                                                                   net->bias);
+    SVO_LAUNCHED(net->ctx);
+    return SVO_OK;
+}
+
+// FP32 forward of the four layers into net->act / out.
+svo_status net_forward_fp32(svo_net* net, const float* feat, int W, int H, float* out) {
+    svo_context* ctx = net->ctx;
+    cudaStream_t s = ctx->stream;
+    const size_t n = (size_t)W * H;
+    const dim3 grid((W + 31) / 32, (H + 7) / 8);
+    float* a0 = net->act;
+    float* a1 = net->act + 16 * n;
+    float* a2 = net->act + 32 * n;
+    k_net_conv_fwd<8, 16, true, false><<<grid, 256, 0, s>>>(feat, net->wr + net_w_off(0), net->params + net_b_off(0),
+                                                            feat, a0, W, H);
+    SVO_LAUNCHED(ctx);
+    k_net_conv_fwd<16, 16, false, false><<<grid, 256, 0, s>>>(a0, net->wr + net_w_off(1), net->params + net_b_off(1),
+                                                              feat, a1, W, H);
+    SVO_LAUNCHED(ctx);
+    k_net_conv_fwd<16, 16, false, false><<<grid, 256, 0, s>>>(a1, net->wr + net_w_off(2), net->params + net_b_off(2),
+                                                              feat, a2, W, H);
+    SVO_LAUNCHED(ctx);
+    k_net_conv_fwd<16, 4, false, true><<<grid, 256, 0, s>>>(a2, net->wr + net_w_off(3), net->params + net_b_off(3),
+                                                            feat, out, W, H);
+    SVO_LAUNCHED(ctx);
+    return SVO_OK;
+}
+
+template <int CIN, int COUT, bool kFirst>
+svo_status net_weight_grad(svo_net* net, const float* a, const float* g, int W, int H, int layer) {
+    svo_context* ctx = net->ctx;
+    const size_t n = (size_t)W * H;
+    const int blocks = (int)((n + kNetChunk - 1) / kNetChunk);
+    constexpr int vals = 9 * CIN * COUT + COUT;
+    k_net_conv_bwd_weight<CIN, COUT, kFirst><<<blocks, 160, 0, ctx->stream>>>(a, g, net->partial, W, H);
+    SVO_LAUNCHED(ctx);
+    k_net_reduce<<<(vals + 255) / 256, 256, 0, ctx->stream>>>(net->partial, blocks, vals,
+                                                               net->grads + net_w_off(layer));
+    SVO_LAUNCHED(ctx);
     return SVO_OK;
 }
 
@@ -404,6 +667,7 @@ svo_status svo_context_create(int device, svo_context** out) {
 svo_status svo_context_destroy(svo_context* ctx) {
     if (!ctx) return SVO_OK;
     while (!ctx->targets.empty()) svo_target_destroy(ctx->targets.back());
+    while (!ctx->nets.empty()) svo_net_destroy(ctx->nets.back());
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->l2_window > 0) l2_window_release(ctx->device);
@@ -579,8 +843,7 @@ svo_status svo_target_destroy(svo_target* t) {
     svo_context* ctx = t->ctx;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
-    if (t->graph_exec) cudaGraphExecDestroy(t->graph_exec);
-    if (t->graph) cudaGraphDestroy(t->graph);
+    for (auto& g : t->graphs) g.reset();
     void* ptrs[] = {t->B.col[0], t->B.col[1], t->B.xyz[0], t->B.xyz[1], t->B.disp, t->B.bgrx, t->B.keys, t->B.ids,
                     t->B.tile_mask, t->B.counters, t->d_params, t->full_col, t->full_xyzw, t->full_vox};
     for (void* p : ptrs)
@@ -596,13 +859,8 @@ svo_status svo_target_destroy(svo_target* t) {
 svo_status svo_target_use_graph(svo_target* t, int enable) {
     if (!t) return SVO_ERR_INVALID_ARGUMENT;
     t->use_graph = enable != 0;
-    if (!t->use_graph && t->graph_exec) {
-        cudaGraphExecDestroy(t->graph_exec);
-        cudaGraphDestroy(t->graph);
-        t->graph_exec = nullptr;
-        t->graph = nullptr;
-        t->params_node = nullptr;
-    }
+    if (!t->use_graph)
+        for (auto& g : t->graphs) g.reset();
     return SVO_OK;
 }
 
@@ -616,8 +874,9 @@ int svo_target_stage_times(svo_target* t, float* ms, int cap) {
     if (!t || !ms || t->n_events < 2) return 0;
     if (cudaEventSynchronize(t->ev[t->n_events - 1]) != cudaSuccess) return 0;
     int k = 0;
-    if (t->last_mode == 1) {
-        for (int i = 0; i < 6 && i < cap; ++i, ++k) {
+    if (t->last_mode == 1 || t->last_mode == 3) {
+        const int stages = t->last_mode == 1 ? 6 : 4;
+        for (int i = 0; i < stages && i < cap; ++i, ++k) {
             float v = 0;
             cudaEventElapsedTime(&v, t->ev[i], t->ev[i + 1]);
             ms[i] = v;
@@ -703,70 +962,287 @@ svo_status svo_warp_frame(svo_context* ctx, svo_target* t, const svo_view* view,
     const int cur = (int)(t->frames & 1);
     const bool have_cache = frame >= 2 && t->have_prev;
     FrameParams p = make_params(t, *view, frame, cur, have_cache);
-    cudaStream_t s = ctx->stream;
-    if (t->use_graph) {
-        if (!t->graph_exec || t->graph_profiled != t->profiling) {
-            if (t->graph_exec) {
-                cudaGraphExecDestroy(t->graph_exec);
-                cudaGraphDestroy(t->graph);
-                t->graph_exec = nullptr;
-                t->graph = nullptr;
-            }
-            SVO_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-            t->capturing = true;
-            k_set_params<<<1, 1, 0, s>>>(p, t->d_params, t->B.counters);
-            st = enqueue_warp_body(ctx, t);
-            t->capturing = false;
-            cudaGraph_t g = nullptr;
-            cudaError_t ce = cudaStreamEndCapture(s, &g);
-            if (st != SVO_OK) {
-                if (g) cudaGraphDestroy(g);
-                return st;
-            }
-            if (ce != cudaSuccess) return fail(ctx, SVO_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(ce));
-            t->graph = g;
-            SVO_CUDA(ctx, cudaGraphInstantiate(&t->graph_exec, g, 0));
-            // Find the k_set_params node (the only root of the graph).
-            size_t nroots = 0;
-            SVO_CUDA(ctx, cudaGraphGetRootNodes(g, nullptr, &nroots));
-            std::vector<cudaGraphNode_t> roots(nroots);
-            SVO_CUDA(ctx, cudaGraphGetRootNodes(g, roots.data(), &nroots));
-            t->params_node = nullptr;
-            for (auto nd : roots) {
-                cudaGraphNodeType ty;
-                if (cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) {
-                    cudaKernelNodeParams kp;
-                    if (cudaGraphKernelNodeGetParams(nd, &kp) == cudaSuccess && kp.func == (void*)k_set_params)
-                        t->params_node = nd;
-                }
-            }
-            if (!t->params_node) return fail(ctx, SVO_ERR_CUDA, "graph: parameter node not found");
-            t->graph_profiled = t->profiling;
-        }
-        cudaKernelNodeParams kp;
-        SVO_CUDA(ctx, cudaGraphKernelNodeGetParams(t->params_node, &kp));
-        FrameParams* dst = t->d_params;
-        uint32_t* cnt = t->B.counters;
-        void* args[] = {&p, &dst, &cnt};
-        kp.kernelParams = args;
-        kp.extra = nullptr;
-        SVO_CUDA(ctx, cudaGraphExecKernelNodeSetParams(t->graph_exec, t->params_node, &kp));
-        SVO_CUDA(ctx, cudaGraphLaunch(t->graph_exec, s));
-        ctx->launches += 7;
-    } else {
-        k_set_params<<<1, 1, 0, s>>>(p, t->d_params, t->B.counters);
-        SVO_LAUNCHED(ctx);
-        st = enqueue_warp_body(ctx, t);
-        if (st != SVO_OK) return st;
-    }
+    st = run_frame(ctx, t, p, t->graphs[0], nullptr, 0.0f, [&] { return enqueue_warp_body(ctx, t); });
+    if (st != SVO_OK) return st;
     if (t->profiling) {
         t->n_events = 7;
         t->last_mode = 1;
     }
     t->last_cur = cur;
     t->have_prev = true;
+    t->prev_view = *view;
+    t->have_prev_view = true;
     ++t->frames;
     return SVO_OK;
+}
+
+svo_status svo_warp_frame_learned(svo_context* ctx, svo_target* t, const svo_view* view, int frame, const svo_net* net,
+                                  float threshold) {
+    if (!ctx || !t || t->ctx != ctx || !net || net->ctx != ctx) return SVO_ERR_INVALID_ARGUMENT;
+    svo_status st = check_view(ctx, t, view);
+    if (st != SVO_OK) return st;
+    if (t->res_x < 16 || t->res_y < 16)
+        return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "warp frames need res >= 16 (the reference's 16x16 hole tiles)");
+    if (view->fovx != 1.0f || view->fovy != 1.0f)
+        return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "warp frames use fov 1 (raycast_proj has no fov term)");
+    if (frame < 0) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "frame");
+    if (!(threshold > 0.0f && threshold < 1.0f)) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "threshold in (0, 1)");
+    const float logit = std::log(threshold / (1.0f - threshold));
+    const int cur = (int)(t->frames & 1);
+    const bool have_cache = frame >= 2 && t->have_prev;
+    FrameParams p = make_params(t, *view, frame, cur, have_cache);
+    st = run_frame(ctx, t, p, t->graphs[1], net, threshold, [&] { return enqueue_learned_body(ctx, t, net, logit); });
+    if (st != SVO_OK) return st;
+    if (t->profiling) {
+        t->n_events = 5;
+        t->last_mode = 3;
+    }
+    t->last_cur = cur;
+    t->have_prev = true;
+    t->prev_view = *view;
+    t->have_prev_view = true;
+    ++t->frames;
+    return SVO_OK;
+}
+
+svo_status svo_target_set_feature_tap(svo_target* t, float* d_features) {
+    if (!t) return SVO_ERR_INVALID_ARGUMENT;
+    t->feature_tap = d_features;
+    return SVO_OK;
+}
+
+svo_status svo_read_requested(svo_target* t, uint32_t* count) {
+    if (!t || !count) return SVO_ERR_INVALID_ARGUMENT;
+    svo_context* ctx = t->ctx;
+    SVO_CUDA(ctx, cudaMemcpyAsync(count, t->B.counters + 1, 4, cudaMemcpyDeviceToHost, ctx->stream));
+    SVO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SVO_OK;
+}
+
+// ------------------------------------------------------------------ net --
+// Runs k_net_probe once per device; the verdict is cached for the process.
+static std::mutex g_probe_mutex;
+static int g_probe_state[64] = {};  // 0 not run, 1 passed, 2 failed
+
+static svo_status net_probe(svo_context* ctx) {
+    std::lock_guard<std::mutex> lock(g_probe_mutex);
+    const int d = ctx->device;
+    if (d >= 0 && d < 64 && g_probe_state[d] == 1) return SVO_OK;
+    if (d >= 0 && d < 64 && g_probe_state[d] == 2)
+        return fail(ctx, SVO_ERR_NOT_SUPPORTED, "tensor-core operand layout check failed earlier on this device");
+    uint32_t* dres = nullptr;
+    SVO_CUDA(ctx, cudaMalloc(&dres, 8));
+    uint32_t res[2] = {0, 0};
+    cudaError_t e = cudaMemsetAsync(dres, 0, 8, ctx->stream);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute((const void*)k_net_probe, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   kNetProbeSmem);
+    if (e == cudaSuccess) {
+        k_net_probe<<<1, 128, kNetProbeSmem, ctx->stream>>>(dres);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(res, dres, 8, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(dres);
+    if (e != cudaSuccess) return fail(ctx, SVO_ERR_CUDA, std::string("net probe: ") + cudaGetErrorString(e));
+    ++ctx->launches;
+    const bool ok = res[0] == 0 && res[1] == 0;
+    if (d >= 0 && d < 64) g_probe_state[d] = ok ? 1 : 2;
+    if (!ok) {
+        char buf[128];
+        std::snprintf(buf, sizeof(buf), "tensor-core operand layout check failed (%u mismatches, timeout %u)", res[0],
+                      res[1]);
+        return fail(ctx, SVO_ERR_NOT_SUPPORTED, buf);
+    }
+    return SVO_OK;
+}
+
+svo_status svo_net_create(svo_context* ctx, svo_net** out) {
+    if (!ctx || !out) return SVO_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    SVO_CUDA(ctx, cudaSetDevice(ctx->device));
+    {
+        const svo_status ps = net_probe(ctx);
+        if (ps != SVO_OK) return ps;
+    }
+    auto* net = new svo_net;
+    net->ctx = ctx;
+    svo_status st = SVO_OK;
+    auto A = [&](void** p, size_t bytes) {
+        if (st == SVO_OK) st = alloc(ctx, p, bytes);
+    };
+    A((void**)&net->params, kNetParams * 4);
+    A((void**)&net->m, kNetParams * 4);
+    A((void**)&net->v, kNetParams * 4);
+    A((void**)&net->grads, kNetParams * 4);
+    A((void**)&net->wr, kNetParams * 4);
+    A((void**)&net->packed, kNetMmaTotal * 512);
+    A((void**)&net->bias, 64 * 4);
+    if (st != SVO_OK) {
+        svo_net_destroy(net);
+        return st;
+    }
+    ctx->nets.push_back(net);
+    *out = net;
+    return svo_net_init(net, 1);
+}
+
+svo_status svo_net_destroy(svo_net* net) {
+    if (!net) return SVO_OK;
+    cudaSetDevice(net->ctx->device);
+    cudaStreamSynchronize(net->ctx->stream);
+    void* ptrs[] = {net->params, net->m, net->v, net->grads, net->wr, net->packed, net->bias, net->act,
+                    net->out, net->dout, net->g0, net->g1, net->partial, net->loss_partial};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    auto& v = net->ctx->nets;
+    auto it = std::find(v.begin(), v.end(), net);
+    if (it != v.end()) v.erase(it);
+    delete net;
+    return SVO_OK;
+}
+
+svo_status svo_net_set_params(svo_net* net, const float* host, size_t n) {
+    if (!net || !host) return SVO_ERR_INVALID_ARGUMENT;
+    svo_context* ctx = net->ctx;
+    if (n != (size_t)kNetParams) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "parameter count");
+    for (size_t i = 0; i < n; ++i)
+        if (!std::isfinite(host[i])) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "non-finite parameter");
+    SVO_CUDA(ctx, cudaMemcpyAsync(net->params, host, n * 4, cudaMemcpyHostToDevice, ctx->stream));
+    SVO_CUDA(ctx, cudaMemsetAsync(net->m, 0, n * 4, ctx->stream));
+    SVO_CUDA(ctx, cudaMemsetAsync(net->v, 0, n * 4, ctx->stream));
+    SVO_CUDA(ctx, cudaMemsetAsync(net->grads, 0, n * 4, ctx->stream));
+    net->step = 0;
+    svo_status st = net_prepare(net);
+    if (st != SVO_OK) return st;
+    SVO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SVO_OK;
+}
+
+// He-normal weights (seeded splitmix64 + Box-Muller), the last layer scaled
+// by 0.1, zero biases.
+svo_status svo_net_init(svo_net* net, uint64_t seed) {
+    if (!net) return SVO_ERR_INVALID_ARGUMENT;
+    std::vector<float> p(kNetParams, 0.0f);
+    uint64_t state = seed * 0x9E3779B97F4A7C15ull + 0x1234567ull;
+    auto next = [&]() {
+        uint64_t z = (state += 0x9E3779B97F4A7C15ull);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        return ((z >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+    };
+    for (int l = 0; l < kNetLayers; ++l) {
+        const double sd = std::sqrt(2.0 / (9.0 * net_cin(l))) * (l == kNetLayers - 1 ? 0.1 : 1.0);
+        for (int i = 0; i < 9 * net_cin(l) * net_cout(l); ++i) {
+            const double u1 = next(), u2 = next();
+            p[net_w_off(l) + i] = (float)(sd * std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2));
+        }
+    }
+    return svo_net_set_params(net, p.data(), p.size());
+}
+
+static svo_status net_copy_out(svo_net* net, const float* dev, float* host, size_t n) {
+    svo_context* ctx = net->ctx;
+    if (!host) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "null host buffer");
+    if (n != (size_t)kNetParams) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "parameter count");
+    SVO_CUDA(ctx, cudaMemcpyAsync(host, dev, n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    SVO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SVO_OK;
+}
+
+svo_status svo_net_get_params(svo_net* net, float* host, size_t n) {
+    return net ? net_copy_out(net, net->params, host, n) : SVO_ERR_INVALID_ARGUMENT;
+}
+
+svo_status svo_net_get_grads(svo_net* net, float* host, size_t n) {
+    return net ? net_copy_out(net, net->grads, host, n) : SVO_ERR_INVALID_ARGUMENT;
+}
+
+svo_status svo_net_forward(svo_net* net, const float* d_features, int w, int h, float* d_out) {
+    if (!net || !d_features || !d_out || w < 1 || h < 1) return SVO_ERR_INVALID_ARGUMENT;
+    svo_status st = net_reserve(net, (size_t)w * h);
+    if (st != SVO_OK) return st;
+    return net_forward_fp32(net, d_features, w, h, d_out);
+}
+
+svo_status svo_net_infer(svo_net* net, const float* d_features, int w, int h, float* d_out) {
+    if (!net || !d_features || !d_out || w < 1 || h < 1) return SVO_ERR_INVALID_ARGUMENT;
+    NetInferArgs A{};
+    A.feat = d_features;
+    A.out = d_out;
+    A.w = w;
+    A.h = h;
+    return launch_net_infer(net->ctx, net, false, A);
+}
+
+svo_status svo_net_backward(svo_net* net, const float* d_features, const uint32_t* d_target_bgrx, int w, int h,
+                            float tau, float lambda, float* loss) {
+    if (!net || !d_features || !d_target_bgrx || w < 1 || h < 1) return SVO_ERR_INVALID_ARGUMENT;
+    svo_context* ctx = net->ctx;
+    cudaStream_t s = ctx->stream;
+    const size_t n = (size_t)w * h;
+    svo_status st = net_reserve(net, n);
+    if (st != SVO_OK) return st;
+    st = net_forward_fp32(net, d_features, w, h, net->out);
+    if (st != SVO_OK) return st;
+    const int lb = (int)((n + 255) / 256);
+    k_net_loss<<<lb, 256, 0, s>>>(net->out, d_target_bgrx, net->dout, net->loss_partial, (int)n, tau, lambda);
+    SVO_LAUNCHED(ctx);
+    float* a0 = net->act;
+    float* a1 = net->act + 16 * n;
+    float* a2 = net->act + 32 * n;
+    const dim3 grid((w + 31) / 32, (h + 7) / 8);
+    const int rg = std::min<size_t>((16 * n + 255) / 256, (size_t)ctx->sm_count * 16);
+    // layer 3
+    st = net_weight_grad<16, 4, false>(net, a2, net->dout, w, h, 3);
+    if (st != SVO_OK) return st;
+    k_net_conv_bwd_data<16, 4><<<grid, 256, 0, s>>>(net->dout, net->wr + net_w_off(3), net->g0, w, h);
+    SVO_LAUNCHED(ctx);
+    k_net_relu_grad<<<rg, 256, 0, s>>>(net->g0, a2, 16 * n);
+    SVO_LAUNCHED(ctx);
+    // layer 2
+    st = net_weight_grad<16, 16, false>(net, a1, net->g0, w, h, 2);
+    if (st != SVO_OK) return st;
+    k_net_conv_bwd_data<16, 16><<<grid, 256, 0, s>>>(net->g0, net->wr + net_w_off(2), net->g1, w, h);
+    SVO_LAUNCHED(ctx);
+    k_net_relu_grad<<<rg, 256, 0, s>>>(net->g1, a1, 16 * n);
+    SVO_LAUNCHED(ctx);
+    // layer 1
+    st = net_weight_grad<16, 16, false>(net, a0, net->g1, w, h, 1);
+    if (st != SVO_OK) return st;
+    k_net_conv_bwd_data<16, 16><<<grid, 256, 0, s>>>(net->g1, net->wr + net_w_off(1), net->g0, w, h);
+    SVO_LAUNCHED(ctx);
+    k_net_relu_grad<<<rg, 256, 0, s>>>(net->g0, a0, 16 * n);
+    SVO_LAUNCHED(ctx);
+    // layer 0
+    st = net_weight_grad<8, 16, true>(net, d_features, net->g0, w, h, 0);
+    if (st != SVO_OK) return st;
+    if (loss) {
+        std::vector<float> part(2 * (size_t)lb);
+        SVO_CUDA(ctx, cudaMemcpyAsync(part.data(), net->loss_partial, part.size() * 4, cudaMemcpyDeviceToHost, s));
+        SVO_CUDA(ctx, cudaStreamSynchronize(s));
+        double a = 0.0, c = 0.0;
+        for (int i = 0; i < lb; ++i) {
+            a += part[2 * i];
+            c += part[2 * i + 1];
+        }
+        loss[0] = (float)(a / (double)n);
+        loss[1] = (float)(c / (double)n);
+    }
+    return SVO_OK;
+}
+
+svo_status svo_net_adam(svo_net* net, float lr, float beta1, float beta2, float eps) {
+    if (!net || !(lr >= 0.0f) || !(beta1 >= 0.0f && beta1 < 1.0f) || !(beta2 >= 0.0f && beta2 < 1.0f) || !(eps > 0.0f))
+        return SVO_ERR_INVALID_ARGUMENT;
+    svo_context* ctx = net->ctx;
+    ++net->step;
+    const float c1 = (float)(1.0 - std::pow((double)beta1, net->step));
+    const float c2 = (float)(1.0 - std::pow((double)beta2, net->step));
+    k_net_adam<<<(kNetParams + 255) / 256, 256, 0, ctx->stream>>>(net->params, net->m, net->v, net->grads, kNetParams,
+                                                                  lr, beta1, beta2, eps, c1, c2);
+    SVO_LAUNCHED(ctx);
+    return net_prepare(net);
 }
 
 static svo_status read_back(svo_target* t, void* host, const void* dev, size_t bytes) {

@@ -36,6 +36,9 @@ struct FrameParams {
     int cur;         // which of the two colour/coordinate planes is current
     int have_cache;  // the other plane holds the previous frame
     int add_x, add_y, x_end, y_end;  // refresh tile rectangle (raycast.h:363-366)
+    // previous frame's camera (the reconstruction net's motion feature)
+    float prev_pos[3], prev_vx[3], prev_vy[3], prev_vz[3];
+    int have_prev_view;
 };
 
 // Buffers of one render target.
@@ -324,7 +327,8 @@ __global__ void __launch_bounds__(BLOCK) k_trace_full(Octree o_in, const FullBat
     if (fault) atomicOr(fault_out, fault);
 }
 
-template <int DEPTH, int BLOCK>
+// kBgrx (learned frames): also writes the traced pixels' colourised output.
+template <int DEPTH, int BLOCK, bool kBgrx>
 __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FrameParams* __restrict__ P,
                                                     TargetBuffers B, uint32_t* fault_out) {
     __shared__ uint64_t mbar;
@@ -372,6 +376,7 @@ __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FramePa
             const size_t ofs = (size_t)y * res_x + x;
             col[ofs] = r.colour;
             xyz[ofs] = make_float4(r.hx, r.hy, r.hz, r.dist);
+            if (kBgrx) B.bgrx[ofs] = colorize(r.colour);
         }
     }
     if (o_in.n_smem > 0 && !staged) stage_drain(&mbar);

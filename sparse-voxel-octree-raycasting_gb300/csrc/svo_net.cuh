@@ -1,0 +1,717 @@
+// svo_net.cuh -- the learned reconstruction stage of the warp pipeline.
+//
+// The reference renderer fills the pixels that reprojection left empty with a
+// fixed 3x3 filter (raycast_fillhole2, kernel.cl:404-470) and traces every
+// 2x2 hole block (raycast_counthole/writeids/holes). The learned stage
+// replaces both decisions: a small convolutional net looks at the warped
+// frame (colour, depth, hole mask, reprojection motion) and outputs a colour
+// plus a confidence per pixel; pixels below the confidence threshold are
+// traced exactly like the reference's holes, the rest show the net's colour.
+//
+// Net: four 3x3 same-size convolutions, zero padding at the frame border,
+// channels 8 -> 16 -> 16 -> 16 -> 4, ReLU after the first three; the output's
+// first three channels are added to the input colour (a residual), the fourth
+// is the confidence logit. Weights, features and hidden activations are
+// bfloat16, sums FP32.
+//
+// Kernels:
+//   k_net_features    features of every pixel of the current plane (the
+//                     training tap)
+//   k_net_infer       the whole net fused per 56x24-pixel tile on the tensor
+//                     cores: tcgen05.mma (kind::f16, bf16 x bf16 -> fp32 in
+//                     tensor memory) as an implicit GEMM, activations staged
+//                     in shared memory between layers
+//   k_net_conv_*      FP32 CUDA-core forward / backward of one layer, the
+//                     loss, a deterministic reduction and Adam (training)
+#pragma once
+#include <cstdint>
+#include <cstring>
+
+#include "svo_kernels.cuh"
+
+namespace svo {
+
+constexpr int kNetLayers = 4;
+constexpr int kNetParams = 6388;
+__host__ __device__ constexpr int net_cin(int l) { return l == 0 ? 8 : 16; }
+__host__ __device__ constexpr int net_cout(int l) { return l == 3 ? 4 : 16; }
+// Flat parameter layout: per layer W [9][cin][cout] then b [cout].
+__host__ __device__ constexpr int net_w_off(int l) {
+    return l == 0 ? 0 : net_w_off(l - 1) + 9 * net_cin(l - 1) * net_cout(l - 1) + net_cout(l - 1);
+}
+__host__ __device__ constexpr int net_b_off(int l) { return net_w_off(l) + 9 * net_cin(l) * net_cout(l); }
+static_assert(net_b_off(3) + 4 == kNetParams, "parameter layout");
+
+// Round to bfloat16, nearest even (finite inputs): the bit pattern and the
+// value it stands for.
+__host__ __device__ __forceinline__ uint32_t bf16_bits(float x) {
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    return (u + 0x7FFFu + ((u >> 16) & 1u)) >> 16;
+}
+__host__ __device__ __forceinline__ float bf16_round(float x) {
+    const uint32_t u = bf16_bits(x) << 16;
+    float r;
+    memcpy(&r, &u, 4);
+    return r;
+}
+
+// --------------------------------------------------------------- features --
+// Per pixel of the current plane after reprojection:
+//   0-2  colour of the warped pixel (colourised, /255), 0 when empty
+//   3    log2(1 + distance from the camera) / 16, 0 when empty
+//   4    1 when the pixel is empty (a hole), else 0
+//   5    reprojection motion: distance in pixels between where the cached
+//        point appears now and where it appeared from the previous camera,
+//        clamped to 8 and divided by 8 (1 when it was behind that camera)
+//   6-7  0
+// (The previous camera travels in FrameParams: prev_pos, prev_vx/vy/vz.)
+__device__ __forceinline__ void net_features(const FrameParams& P, const TargetBuffers& B, int x, int y, float f[8]) {
+    const size_t ofs = (size_t)y * B.res_x + x;
+    const uint32_t c = plane_col(B, P.cur)[ofs];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) f[i] = 0.0f;
+    if (c == kEmptyPixel) {
+        f[4] = 1.0f;
+        return;
+    }
+    const uint32_t bgrx = colorize(c);
+    f[0] = (float)((bgrx >> 16) & 255u) * (1.0f / 255.0f);
+    f[1] = (float)((bgrx >> 8) & 255u) * (1.0f / 255.0f);
+    f[2] = (float)(bgrx & 255u) * (1.0f / 255.0f);
+    const float4 q = plane_xyz(B, P.cur)[ofs];
+    const float ax = q.x - P.ray.px, ay = q.y - P.ray.py, az = q.z - P.ray.pz;
+    const float d = sqrtf(ax * ax + ay * ay + az * az);
+    f[3] = fminf(log2f(1.0f + d) * (1.0f / 16.0f), 1.0f);
+    float m = 8.0f;
+    if (P.have_prev_view) {
+        const float bx = q.x - P.prev_pos[0], by = q.y - P.prev_pos[1], bz = q.z - P.prev_pos[2];
+        const float zp = bx * P.prev_vz[0] + by * P.prev_vz[1] + bz * P.prev_vz[2];
+        const float zc = ax * P.vz[0] + ay * P.vz[1] + az * P.vz[2];
+        if (zp >= 0.05f && zc >= 0.05f) {
+            const float ry = (float)B.res_y;
+            const float sxp = (bx * P.prev_vx[0] + by * P.prev_vx[1] + bz * P.prev_vx[2]) * ry / zp;
+            const float syp = (bx * P.prev_vy[0] + by * P.prev_vy[1] + bz * P.prev_vy[2]) * ry / zp;
+            const float sxc = (ax * P.vx[0] + ay * P.vx[1] + az * P.vx[2]) * ry / zc;
+            const float syc = (ax * P.vy[0] + ay * P.vy[1] + az * P.vy[2]) * ry / zc;
+            m = fminf(sqrtf((sxc - sxp) * (sxc - sxp) + (syc - syp) * (syc - syp)), 8.0f);
+        }
+    } else {
+        m = 0.0f;
+    }
+    f[5] = m * 0.125f;
+}
+
+// Training tap: features of every pixel, planar [8][res_y*res_x], FP32.
+__global__ void __launch_bounds__(256) k_net_features(const FrameParams* __restrict__ P, TargetBuffers B,
+                                                      float* out) {
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= B.res_x || y >= B.res_y) return;
+    float f[8];
+    net_features(*P, B, x, y, f);
+    const size_t n = (size_t)B.res_x * B.res_y, ofs = (size_t)y * B.res_x + x;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) out[i * n + ofs] = f[i];
+}
+
+// ------------------------------------------------- weight preparation --
+// From the FP32 master parameters: a bf16-rounded FP32 copy of the weights
+// (CUDA-core path) and the tensor-core operand image (bf16, one 512-byte
+// block per MMA: [co group 2][ci chunk 2][8 co][8 ci], K-major core matrices).
+// Layer 0 has 8 input channels, so one MMA covers two taps (ci chunk 0 = tap
+// 2m, chunk 1 = tap 2m+1; the fifth MMA pairs tap 8 with zeros); layers 1-3
+// take one tap per MMA; layer 3's 4 output channels are padded to 16.
+__host__ __device__ constexpr int net_mmas(int l) { return l == 0 ? 5 : 9; }
+__host__ __device__ constexpr int net_mma_base(int l) { return l == 0 ? 0 : 5 + 9 * (l - 1); }
+constexpr int kNetMmaTotal = 32;
+constexpr int kNetBias = 16 + 16 + 16 + 4;
+
+__global__ void k_net_prepare(const float* __restrict__ params, float* __restrict__ wr, uint16_t* __restrict__ packed,
+                              float* __restrict__ bias) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < kNetParams) wr[i] = bf16_round(params[i]);
+    if (i < kNetMmaTotal * 256) {
+        const int mma = i >> 8, e = i & 255;
+        const int ng = e >> 7, kc = (e >> 6) & 1, r = (e >> 3) & 7, k = e & 7;
+        int l = 3;
+        while (l > 0 && mma < net_mma_base(l)) --l;
+        const int m = mma - net_mma_base(l);
+        const int co = ng * 8 + r;
+        float v = 0.0f;
+        if (co < net_cout(l)) {
+            int tap, ci;
+            if (l == 0) {
+                tap = 2 * m + kc;
+                ci = k;
+            } else {
+                tap = m;
+                ci = kc * 8 + k;
+            }
+            if (tap < 9) v = params[net_w_off(l) + (tap * net_cin(l) + ci) * net_cout(l) + co];
+        }
+        packed[i] = (uint16_t)bf16_bits(v);
+    }
+    if (i < kNetBias) {
+        const int l = i < 16 ? 0 : (i < 32 ? 1 : (i < 48 ? 2 : 3));
+        bias[i] = params[net_b_off(l) + (i - 16 * l)];
+    }
+}
+
+// ------------------------------------------------ tcgen05 primitives --
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Shared-memory matrix descriptor, no swizzle, K-major canonical layout:
+// 8-row x 16-byte core matrices; lbo = byte distance between the two core
+// matrices of a row group along K, sbo = byte distance between row groups.
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo & 0x3FFFFu) >> 4) << 16) |
+           ((uint64_t)((sbo & 0x3FFFFu) >> 4) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor, kind::f16: D f32, A and B bf16, both K-major,
+// N = 16, M = 128.
+constexpr uint32_t kNetIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((16u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        :
+        : "r"(d_tmem), "l"(a), "l"(b), "r"(kNetIdesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float v[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tc_ld4(uint32_t taddr, float v[4]) {
+    uint32_t r[4];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Bounded wait on an mbarrier phase (~0.5 s), false on timeout.
+__device__ __forceinline__ bool mbar_wait_phase(uint32_t bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (;;) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (global_ns() - t0 > 500000000ull) return false;
+    }
+}
+
+// Operand-layout self-check, run once per device before the first learned
+// frame: one 128x16x16 MMA on small integers laid out exactly as k_net_infer
+// lays out its operands (A: two 8-channel planes 2048 bytes apart, B: the
+// packed weight block), compared with the CUDA-core product. The A region is
+// 64 KB so that every address the descriptors can form stays inside it.
+// result[0] = mismatching elements, result[1] = 1 when the wait timed out.
+constexpr int kNetProbeSmem = 65536 + 512;
+
+__global__ void __launch_bounds__(128, 1) k_net_probe(uint32_t* result) {
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tmem_base_s;
+    uint8_t* smem = reinterpret_cast<uint8_t*>(svo_dsmem);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    uint16_t* a = reinterpret_cast<uint16_t*>(smem);
+    uint16_t* b = reinterpret_cast<uint16_t*>(smem + 65536);
+    for (int i = tid; i < 32768; i += 128) a[i] = 0;
+    __syncthreads();
+    // A[r][k]: chunk k/8 at byte (k/8)*2048 + r*16 + (k%8)*2
+    for (int i = tid; i < 128 * 16; i += 128) {
+        const int r = i >> 4, k = i & 15;
+        a[((k >> 3) * 2048 + r * 16) / 2 + (k & 7)] = (uint16_t)bf16_bits((float)((r * 3 + k * 5) % 7 - 3));
+    }
+    // B[n][k] in the packed block layout [n/8][k/8][n%8][k%8]
+    for (int i = tid; i < 256; i += 128) {
+        const int n = i >> 4, k = i & 15;
+        b[(n >> 3) * 128 + (k >> 3) * 64 + (n & 7) * 8 + (k & 7)] = (uint16_t)bf16_bits((float)((n * 2 + k) % 5 - 2));
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base_s)),
+                     "r"(32)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base_s;
+    if (tid == 0) {
+        tc_mma(tmem, tc_desc(smem_addr(a), 2048u, 128u), tc_desc(smem_addr(b), 128u, 256u), 0u);
+        tc_commit(smem_addr(&mbar));
+    }
+    const bool ok = __syncthreads_and(mbar_wait_phase(smem_addr(&mbar), 0) ? 1 : 0) != 0;
+    tc_fence_after();
+    uint32_t bad = 0;
+    if (ok) {
+        float v[16];
+        tc_ld16(tmem + ((uint32_t)(32 * warp) << 16), v);
+        const int r = 32 * warp + lane;
+        for (int n = 0; n < 16; ++n) {
+            float e = 0.0f;
+            for (int k = 0; k < 16; ++k) e += (float)((r * 3 + k * 5) % 7 - 3) * (float)((n * 2 + k) % 5 - 2);
+            if (v[n] != e) ++bad;
+        }
+    }
+    if (bad) atomicAdd(result, bad);
+    if (!ok && tid == 0) result[1] = 1;
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(32) : "memory");
+    }
+}
+
+// ------------------------------------------------ fused inference --
+// One CTA (256 threads) per SM walks 56x24-pixel output tiles. A tile's input
+// window is 64x32 positions (a 4-pixel halo for the four 3x3 layers), stored
+// as "positions" p = row*64 + col. Activations live in shared memory as
+// planes of 8 bf16 channels (16 bytes per position, positions consecutive),
+// with a zeroed guard of 128 positions before and after each plane.
+//
+// Layer l computes output rows [l+1, 31-l) -- (15-l) blocks of 128
+// consecutive positions -- as D[128 x 16] = sum over MMAs of A[128 x 16] *
+// B[16 x 16]: A for tap (dy,dx) is the input planes read from position
+// p + dy*64 + dx, i.e. the same matrix descriptor shifted by that many
+// 16-byte rows (an implicit GEMM with no im2col copy). Positions whose column
+// wraps into the next row are computed and never used. Each block
+// accumulates into its own 16 columns of tensor memory; one thread issues all
+// MMAs of a layer and commits them to an mbarrier; the 8 warps then read the
+// accumulators back (warp w reads tensor-memory lanes 32*(w%4)..+31, warps
+// w and w+4 split the blocks), add the bias, apply ReLU, zero the positions
+// outside the frame (the border padding) and store bf16 into the other
+// buffer. The last layer writes the outputs.
+constexpr int kNetTW = 64, kNetTH = 32, kNetPos = kNetTW * kNetTH;
+constexpr int kNetGuard = 128;
+constexpr int kNetPlaneBytes = (kNetPos + 2 * kNetGuard) * 16;  // 36864
+constexpr int kNetOutW = kNetTW - 8, kNetOutH = kNetTH - 8;      // 56 x 24
+constexpr int kNetSmemA = 0;                                     // 2 planes
+constexpr int kNetSmemB = 2 * kNetPlaneBytes;                    // 2 planes
+constexpr int kNetSmemW = 4 * kNetPlaneBytes;                    // 32 x 512 B
+constexpr int kNetSmemBias = kNetSmemW + kNetMmaTotal * 512;     // 52 floats
+constexpr int kNetSmemRgb = kNetSmemBias + 256;                  // 3 x 2048 floats
+constexpr int kNetSmemBytes = kNetSmemRgb + 3 * kNetPos * 4;      // 188672
+constexpr int kNetTmemCols = 256;
+constexpr int kNetThreads = 256;
+
+struct NetInferArgs {
+    const uint16_t* packed;  // tensor-core weight image
+    const float* bias;       // 52 biases
+    // input: either the planes of a target (pipeline) or planar features
+    const FrameParams* P;
+    TargetBuffers B;
+    const float* feat;  // [8][h][w] when not from planes
+    float* out;         // [4][h][w] when not from planes
+    int w, h;
+    int tiles_x, tiles;
+    float logit_threshold;  // pipeline: traced when logit < threshold
+    uint32_t* fault;
+};
+
+template <bool kPipeline>
+__global__ void __launch_bounds__(kNetThreads, 1) k_net_infer(NetInferArgs A) {
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t tmem_base_s;
+    uint8_t* smem = reinterpret_cast<uint8_t*>(svo_dsmem);
+    const uint32_t sbase = smem_addr(smem);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int W = A.w, H = A.h;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base_s)),
+                     "r"(kNetTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // weights, biases; zero both activation buffers (guards included)
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(A.packed);
+        uint4* dst = reinterpret_cast<uint4*>(smem + kNetSmemW);
+        for (int i = tid; i < kNetMmaTotal * 32; i += kNetThreads) dst[i] = src[i];
+        float* b = reinterpret_cast<float*>(smem + kNetSmemBias);
+        for (int i = tid; i < kNetBias; i += kNetThreads) b[i] = A.bias[i];
+        uint4* z = reinterpret_cast<uint4*>(smem);
+        for (int i = tid; i < 4 * kNetPlaneBytes / 16; i += kNetThreads) z[i] = make_uint4(0, 0, 0, 0);
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base_s;
+    const uint32_t bar = smem_addr(&mbar);
+    const float* bias = reinterpret_cast<const float*>(smem + kNetSmemBias);
+    float* rgb_in = reinterpret_cast<float*>(smem + kNetSmemRgb);
+    uint32_t phase = 0;
+    uint32_t fault = 0;
+    bool aborted = false;  // block-uniform: an MMA wait timed out
+
+    for (int tile = blockIdx.x; tile < A.tiles; tile += gridDim.x) {
+        const int ox = (tile % A.tiles_x) * kNetOutW, oy = (tile / A.tiles_x) * kNetOutH;
+        const int wx = ox - 4, wy = oy - 4;  // image position of window position 0
+        // ---- input features -> buffer B plane 0 (bf16) and rgb_in (rounded floats)
+        for (int p = tid; p < kNetPos; p += kNetThreads) {
+            const int gx = wx + (p & (kNetTW - 1)), gy = wy + (p >> 6);
+            float f[8];
+            if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+                if (kPipeline) {
+                    net_features(*A.P, A.B, gx, gy, f);
+                } else {
+                    const size_t n = (size_t)W * H, ofs = (size_t)gy * W + gx;
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) f[i] = A.feat[i * n + ofs];
+                }
+            } else {
+#pragma unroll
+                for (int i = 0; i < 8; ++i) f[i] = 0.0f;
+            }
+            uint4 v;
+            v.x = bf16_bits(f[0]) | (bf16_bits(f[1]) << 16);
+            v.y = bf16_bits(f[2]) | (bf16_bits(f[3]) << 16);
+            v.z = bf16_bits(f[4]) | (bf16_bits(f[5]) << 16);
+            v.w = bf16_bits(f[6]) | (bf16_bits(f[7]) << 16);
+            *reinterpret_cast<uint4*>(smem + kNetSmemB + (kNetGuard + p) * 16) = v;
+            rgb_in[p] = bf16_round(f[0]);
+            rgb_in[kNetPos + p] = bf16_round(f[1]);
+            rgb_in[2 * kNetPos + p] = bf16_round(f[2]);
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+
+        for (int l = 0; l < kNetLayers; ++l) {
+            const int nb = 15 - l;
+            const int first = (l + 1) * kNetTW;
+            const uint32_t in_off = (l & 1) ? kNetSmemA : kNetSmemB;
+            const uint32_t out_off = (l & 1) ? kNetSmemB : kNetSmemA;
+            if (tid == 0) {
+                tc_fence_after();
+                const uint32_t wbase = sbase + kNetSmemW + net_mma_base(l) * 512;
+                for (int j = 0; j < nb; ++j) {
+                    const int bs = first + 128 * j;
+                    for (int m = 0; m < net_mmas(l); ++m) {
+                        int shift, lbo;
+                        if (l == 0) {
+                            const int t0 = 2 * m, t1 = 2 * m + 1;
+                            shift = (t0 / 3 - 1) * kNetTW + (t0 % 3 - 1);
+                            lbo = t1 < 9 ? ((t1 / 3 - 1) * kNetTW + (t1 % 3 - 1) - shift) * 16 : 16;
+                        } else {
+                            shift = (m / 3 - 1) * kNetTW + (m % 3 - 1);
+                            lbo = kNetPlaneBytes;
+                        }
+                        const uint32_t a_addr = sbase + in_off + (uint32_t)((kNetGuard + bs + shift) * 16);
+                        const uint64_t ad = tc_desc(a_addr, (uint32_t)lbo, 128u);
+                        const uint64_t bd = tc_desc(wbase + m * 512, 128u, 256u);
+                        tc_mma(tmem + 16u * j, ad, bd, m > 0 ? 1u : 0u);
+                    }
+                }
+                tc_commit(bar);
+            }
+            // every thread waits for the layer's MMAs (bounded); the verdict is
+            // made block-uniform before anyone reads tensor memory
+            aborted = __syncthreads_or(mbar_wait_phase(bar, phase) ? 0 : 1) != 0;
+            phase ^= 1u;
+            tc_fence_after();
+            if (aborted) {
+                fault |= kFaultNet;
+                break;
+            }
+            {
+                const int g = warp & 3;
+                for (int j = warp >> 2; j < nb; j += 2) {
+                    const int p = first + 128 * j + 32 * g + lane;  // this thread's position
+                    const int gx = wx + (p & (kNetTW - 1)), gy = wy + (p >> 6);
+                    const bool inside = gx >= 0 && gx < W && gy >= 0 && gy < H;
+                    const uint32_t taddr = tmem + ((uint32_t)(32 * g) << 16) + 16u * j;
+                    if (l < kNetLayers - 1) {
+                        float v[16];
+                        tc_ld16(taddr, v);
+                        uint32_t h[8];
+#pragma unroll
+                        for (int c = 0; c < 16; c += 2) {
+                            const float a0 = inside ? fmaxf(v[c] + bias[16 * l + c], 0.0f) : 0.0f;
+                            const float a1 = inside ? fmaxf(v[c + 1] + bias[16 * l + c + 1], 0.0f) : 0.0f;
+                            h[c >> 1] = bf16_bits(a0) | (bf16_bits(a1) << 16);
+                        }
+                        *reinterpret_cast<uint4*>(smem + out_off + (kNetGuard + p) * 16) =
+                            make_uint4(h[0], h[1], h[2], h[3]);
+                        *reinterpret_cast<uint4*>(smem + out_off + kNetPlaneBytes + (kNetGuard + p) * 16) =
+                            make_uint4(h[4], h[5], h[6], h[7]);
+                    } else {
+                        float v[4];
+                        tc_ld4(taddr, v);
+                        const int col = p & (kNetTW - 1);
+                        const bool out = inside && col >= 4 && col < 4 + kNetOutW;  // rows are 4..27 here
+                        const float r = v[0] + bias[48] + rgb_in[p];
+                        const float gg = v[1] + bias[49] + rgb_in[kNetPos + p];
+                        const float b = v[2] + bias[50] + rgb_in[2 * kNetPos + p];
+                        const float z = v[3] + bias[51];
+                        if (kPipeline) {
+                            bool req = false;
+                            if (out) {
+                                const size_t ofs = (size_t)gy * W + gx;
+                                const uint32_t ri = (uint32_t)__float2int_rn(fminf(fmaxf(r, 0.0f), 1.0f) * 255.0f);
+                                const uint32_t gi = (uint32_t)__float2int_rn(fminf(fmaxf(gg, 0.0f), 1.0f) * 255.0f);
+                                const uint32_t bi = (uint32_t)__float2int_rn(fminf(fmaxf(b, 0.0f), 1.0f) * 255.0f);
+                                A.B.bgrx[ofs] = bi + (gi << 8) + (ri << 16);
+                                req = !(z >= A.logit_threshold);
+                            }
+                            const uint32_t bal = __ballot_sync(0xffffffffu, req);
+                            if (bal) {
+                                uint32_t base = 0;
+                                if (lane == 0) base = atomicAdd(A.B.counters + 1, (uint32_t)__popc(bal));
+                                base = __shfl_sync(0xffffffffu, base, 0);
+                                if (req) {
+                                    const uint32_t rank = (uint32_t)__popc(bal & ((1u << lane) - 1u));
+                                    A.B.ids[2u * (uint32_t)A.B.tiles_x * (uint32_t)A.B.tiles_y + base + rank] =
+                                        (uint32_t)gx | ((uint32_t)gy << 16);
+                                }
+                            }
+                        } else if (out) {
+                            const size_t n = (size_t)W * H, ofs = (size_t)gy * W + gx;
+                            A.out[ofs] = r;
+                            A.out[n + ofs] = gg;
+                            A.out[2 * n + ofs] = b;
+                            A.out[3 * n + ofs] = z;
+                        }
+                    }
+                }
+            }
+            fence_async_smem();
+            tc_fence_before();
+            __syncthreads();
+            tc_fence_after();
+        }
+        if (aborted) break;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kNetTmemCols) : "memory");
+    }
+    if (fault) atomicOr(A.fault, fault);
+}
+
+// ----------------------------------------------- FP32 training path --
+// One layer forward: one thread per pixel, weights (already bf16-rounded) in
+// shared memory. kFirst rounds the input features to bf16 on load; hidden
+// layers store bf16(ReLU(.)); the last layer stores FP32 plus the residual
+// colour.
+template <int CIN, int COUT, bool kFirst, bool kLast>
+__global__ void __launch_bounds__(256) k_net_conv_fwd(const float* __restrict__ in, const float* __restrict__ wr,
+                                                      const float* __restrict__ b, const float* __restrict__ feat,
+                                                      float* __restrict__ out, int W, int H) {
+    __shared__ float ws[9 * CIN * COUT];
+    __shared__ float bs[COUT];
+    for (int i = threadIdx.x; i < 9 * CIN * COUT; i += blockDim.x) ws[i] = wr[i];
+    if (threadIdx.x < COUT) bs[threadIdx.x] = b[threadIdx.x];
+    __syncthreads();
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= W || y >= H) return;
+    const size_t n = (size_t)W * H;
+    float acc[COUT];
+#pragma unroll
+    for (int c = 0; c < COUT; ++c) acc[c] = 0.0f;
+    for (int t = 0; t < 9; ++t) {
+        const int sx = x + t % 3 - 1, sy = y + t / 3 - 1;
+        if (sx < 0 || sx >= W || sy < 0 || sy >= H) continue;
+        const size_t o = (size_t)sy * W + sx;
+        for (int ci = 0; ci < CIN; ++ci) {
+            float a = __ldg(in + ci * n + o);
+            if (kFirst) a = bf16_round(a);
+            const float* wt = ws + (t * CIN + ci) * COUT;
+#pragma unroll
+            for (int c = 0; c < COUT; ++c) acc[c] = __fmaf_rn(a, wt[c], acc[c]);
+        }
+    }
+    const size_t o = (size_t)y * W + x;
+#pragma unroll
+    for (int c = 0; c < COUT; ++c) {
+        float v = acc[c] + bs[c];
+        if (!kLast) v = bf16_round(fmaxf(v, 0.0f));
+        else if (c < 3) v += bf16_round(__ldg(feat + c * n + o));
+        out[c * n + o] = v;
+    }
+}
+
+// Loss and its gradient w.r.t. the four outputs (see net_oracle.loss_grad):
+// sum_c (rgb_c - t_c)^2 / 3 + lam * BCE(logit, max_c |rgb_c - t_c| < tau),
+// averaged over pixels. Per-block partial sums of the two terms.
+__global__ void __launch_bounds__(256) k_net_loss(const float* __restrict__ out, const uint32_t* __restrict__ target,
+                                                  float* __restrict__ d_out, float* __restrict__ partial, int n,
+                                                  float tau, float lam) {
+    __shared__ float red[2][8];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float lr = 0.0f, lc = 0.0f;
+    if (i < n) {
+        const uint32_t w = __ldg(target + i);
+        const float t0 = (float)((w >> 16) & 255u) / 255.0f, t1 = (float)((w >> 8) & 255u) / 255.0f,
+                    t2 = (float)(w & 255u) / 255.0f;
+        const float d0 = out[i] - t0, d1 = out[n + i] - t1, d2 = out[2 * n + i] - t2;
+        const float z = out[3 * n + i];
+        const float y = fmaxf(fmaxf(fabsf(d0), fabsf(d1)), fabsf(d2)) < tau ? 1.0f : 0.0f;
+        const float inv = 1.0f / (float)n;
+        lr = (d0 * d0 + d1 * d1 + d2 * d2) / 3.0f;
+        lc = fmaxf(z, 0.0f) + log1pf(expf(-fabsf(z))) - y * z;
+        const float s = 1.0f / (1.0f + expf(-z));
+        d_out[i] = 2.0f / 3.0f * d0 * inv;
+        d_out[n + i] = 2.0f / 3.0f * d1 * inv;
+        d_out[2 * n + i] = 2.0f / 3.0f * d2 * inv;
+        d_out[3 * n + i] = lam * (s - y) * inv;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lr += __shfl_down_sync(0xffffffffu, lr, o);
+        lc += __shfl_down_sync(0xffffffffu, lc, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        red[0][threadIdx.x >> 5] = lr;
+        red[1][threadIdx.x >> 5] = lc;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float a = 0.0f, c = 0.0f;
+        for (int k = 0; k < 8; ++k) {
+            a += red[0][k];
+            c += red[1][k];
+        }
+        partial[2 * blockIdx.x] = a;
+        partial[2 * blockIdx.x + 1] = c;
+    }
+}
+
+// g <- g * (a > 0): the gradient w.r.t. a hidden layer's pre-activation.
+__global__ void k_net_relu_grad(float* __restrict__ g, const float* __restrict__ a, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        if (!(a[i] > 0.0f)) g[i] = 0.0f;
+}
+
+// Gradient w.r.t. a layer's input: g_in[ci][q] = sum_t sum_co
+// W[t][ci][co] * g[co][q - off_t] (zero outside the frame).
+template <int CIN, int COUT>
+__global__ void __launch_bounds__(256) k_net_conv_bwd_data(const float* __restrict__ g, const float* __restrict__ wr,
+                                                           float* __restrict__ g_in, int W, int H) {
+    __shared__ float ws[9 * CIN * COUT];
+    for (int i = threadIdx.x; i < 9 * CIN * COUT; i += blockDim.x) ws[i] = wr[i];
+    __syncthreads();
+    const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
+    if (x >= W || y >= H) return;
+    const size_t n = (size_t)W * H;
+    float acc[CIN];
+#pragma unroll
+    for (int c = 0; c < CIN; ++c) acc[c] = 0.0f;
+    for (int t = 0; t < 9; ++t) {
+        const int sx = x - (t % 3 - 1), sy = y - (t / 3 - 1);
+        if (sx < 0 || sx >= W || sy < 0 || sy >= H) continue;
+        const size_t o = (size_t)sy * W + sx;
+        for (int co = 0; co < COUT; ++co) {
+            const float gv = __ldg(g + co * n + o);
+#pragma unroll
+            for (int ci = 0; ci < CIN; ++ci) acc[ci] = __fmaf_rn(ws[(t * CIN + ci) * COUT + co], gv, acc[ci]);
+        }
+    }
+    const size_t o = (size_t)y * W + x;
+#pragma unroll
+    for (int ci = 0; ci < CIN; ++ci) g_in[ci * n + o] = acc[ci];
+}
+
+// Weight and bias gradient partial sums over a chunk of kNetChunk pixels per
+// block: thread (t, ci) accumulates COUT sums a[ci][p + off_t] * g[co][p];
+// threads past 9*CIN sum g for the biases. Partials [block][9*CIN*COUT + COUT].
+constexpr int kNetChunk = 512;
+
+template <int CIN, int COUT, bool kFirst>
+__global__ void __launch_bounds__(160) k_net_conv_bwd_weight(const float* __restrict__ a, const float* __restrict__ g,
+                                                             float* __restrict__ partial, int W, int H) {
+    __shared__ float gs[COUT][kNetChunk];
+    const size_t n = (size_t)W * H;
+    const size_t p0 = (size_t)blockIdx.x * kNetChunk;
+    for (int i = threadIdx.x; i < COUT * kNetChunk; i += blockDim.x) {
+        const int co = i / kNetChunk, k = i % kNetChunk;
+        gs[co][k] = p0 + k < n ? g[co * n + p0 + k] : 0.0f;
+    }
+    __syncthreads();
+    constexpr int kVals = 9 * CIN * COUT + COUT;
+    float* dst = partial + (size_t)blockIdx.x * kVals;
+    const int j = threadIdx.x;
+    if (j < 9 * CIN) {
+        const int t = j / CIN, ci = j % CIN;
+        const int dx = t % 3 - 1, dy = t / 3 - 1;
+        float acc[COUT];
+#pragma unroll
+        for (int c = 0; c < COUT; ++c) acc[c] = 0.0f;
+        for (int k = 0; k < kNetChunk; ++k) {
+            const size_t p = p0 + k;
+            if (p >= n) break;
+            const int x = (int)(p % (size_t)W), y = (int)(p / (size_t)W);
+            const int sx = x + dx, sy = y + dy;
+            if (sx < 0 || sx >= W || sy < 0 || sy >= H) continue;
+            float av = __ldg(a + ci * n + (size_t)sy * W + sx);
+            if (kFirst) av = bf16_round(av);
+#pragma unroll
+            for (int c = 0; c < COUT; ++c) acc[c] = __fmaf_rn(av, gs[c][k], acc[c]);
+        }
+#pragma unroll
+        for (int c = 0; c < COUT; ++c) dst[(t * CIN + ci) * COUT + c] = acc[c];
+    } else if (j < 9 * CIN + COUT) {
+        const int co = j - 9 * CIN;
+        float s = 0.0f;
+        for (int k = 0; k < kNetChunk; ++k) s += gs[co][k];
+        dst[9 * CIN * COUT + co] = s;
+    }
+}
+
+// grads[i] = sum over blocks of partial[block][i], in block order.
+__global__ void k_net_reduce(const float* __restrict__ partial, int blocks, int vals, float* __restrict__ grads) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= vals) return;
+    float s = 0.0f;
+    for (int k = 0; k < blocks; ++k) s += partial[(size_t)k * vals + i];
+    grads[i] = s;
+}
+
+__global__ void k_net_adam(float* __restrict__ p, float* __restrict__ m, float* __restrict__ v,
+                           const float* __restrict__ g, int n, float lr, float b1, float b2, float eps, float c1,
+                           float c2) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * gi;
+    const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+}  // namespace svo

@@ -31,6 +31,7 @@ constexpr uint32_t kFaultFetch = 1u;       // node word index outside the octree
 constexpr uint32_t kFaultSteps = 2u;       // a ray exceeded kStepCap steps
 constexpr uint32_t kFaultHoleEntry = 4u;   // hole list entry outside the frame
 constexpr uint32_t kFaultStage = 8u;       // staging copy of the node prefix did not complete
+constexpr uint32_t kFaultNet = 16u;        // a reconstruction-net tensor-core wait timed out
 
 // Dynamic shared memory of the trace kernels: the per-thread node stack
 // ([level][thread]) followed by a staged copy of the octree's first words

@@ -42,7 +42,12 @@ EXPORTS = [
     "svo_octree_save", "svo_octree_load_header", "svo_octree_load_words", "svo_terrain_build",
     "svo_terrain_voxels", "svo_view_from_euler", "svo_view_look_at", "svo_wrap_position", "svo_camera_path",
     "svo_raycast_full_noalloc", "svo_rle4_voxels", "svo_rle4_build", "svo_write_bmp",
+    "svo_warp_frame_learned", "svo_read_requested", "svo_target_set_feature_tap", "svo_net_create",
+    "svo_net_destroy", "svo_net_init", "svo_net_set_params", "svo_net_get_params", "svo_net_get_grads",
+    "svo_net_forward", "svo_net_infer", "svo_net_backward", "svo_net_adam",
 ]
+
+NET_PARAMS = 6388
 
 
 class SvoError(RuntimeError):
@@ -151,6 +156,19 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "svo_rle4_voxels": (i, [ctypes.c_char_p, i, u32, u32, u32, _P, _P, _P, _P, sz, ctypes.POINTER(sz)]),
         "svo_rle4_build": (i, [_P, ctypes.c_char_p, i, u32, u32, u32]),
         "svo_write_bmp": (i, [ctypes.c_char_p, _P, i, i]),
+        "svo_warp_frame_learned": (i, [_P, _P, ctypes.POINTER(View), i, _P, ctypes.c_float]),
+        "svo_read_requested": (i, [_P, ctypes.POINTER(u32)]),
+        "svo_target_set_feature_tap": (i, [_P, _P]),
+        "svo_net_create": (i, [_P, ctypes.POINTER(_P)]),
+        "svo_net_destroy": (i, [_P]),
+        "svo_net_init": (i, [_P, ctypes.c_uint64]),
+        "svo_net_set_params": (i, [_P, _P, sz]),
+        "svo_net_get_params": (i, [_P, _P, sz]),
+        "svo_net_get_grads": (i, [_P, _P, sz]),
+        "svo_net_forward": (i, [_P, _P, i, i, _P]),
+        "svo_net_infer": (i, [_P, _P, i, i, _P]),
+        "svo_net_backward": (i, [_P, _P, _P, i, i, ctypes.c_float, ctypes.c_float, _P]),
+        "svo_net_adam": (i, [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float]),
     }
     for name, (res, args) in sigs.items():
         fn = getattr(lib, name)
@@ -297,6 +315,7 @@ class Context:
         self._lib = load()
         self._h = _P()
         self._targets: "weakref.WeakSet[Target]" = weakref.WeakSet()
+        self._nets: "weakref.WeakSet[Net]" = weakref.WeakSet()
         _check(self._lib.svo_context_create(device, ctypes.byref(self._h)), None,
                f"svo_context_create(device={device}) failed")
         self.octree: Octree | None = None
@@ -345,11 +364,21 @@ class Context:
     def warp_frame(self, target: "Target", view: View, frame: int) -> None:
         _check(self._lib.svo_warp_frame(self._h, target._h, ctypes.byref(view), frame), self)
 
+    def warp_frame_learned(self, target: "Target", view: View, frame: int, net: "Net",
+                           threshold: float = 0.5) -> None:
+        _check(self._lib.svo_warp_frame_learned(self._h, target._h, ctypes.byref(view), frame, net._h,
+                                                threshold), self)
+
+    def net(self, seed: int = 1) -> "Net":
+        return Net(self, seed)
+
     def close(self) -> None:
-        """Destroy the context; its targets still open are closed first."""
+        """Destroy the context; its targets and nets still open are closed first."""
         if getattr(self, "_h", None):
             for t in list(getattr(self, "_targets", ())):
                 t.close()
+            for n in list(getattr(self, "_nets", ())):
+                n.close()
             self._lib.svo_context_destroy(self._h)
             self._h = None
 
@@ -428,6 +457,17 @@ class Target:
         _check(self._lib.svo_read_voxels(self._h, _ptr(out)), self.ctx)
         return out
 
+    def set_feature_tap(self, d_features: int | None) -> None:
+        """Device buffer (8 x res_y x res_x FP32) receiving the net's input
+        features of every later frame; None stops it."""
+        _check(self._lib.svo_target_set_feature_tap(self._h, _P(d_features) if d_features else None), self.ctx)
+
+    def requested(self) -> int:
+        """Rays the net requested in the last learned frame."""
+        n = ctypes.c_uint32()
+        _check(self._lib.svo_read_requested(self._h, ctypes.byref(n)), self.ctx)
+        return n.value
+
     def device_outputs(self) -> DeviceOutputs:
         d = DeviceOutputs()
         _check(self._lib.svo_target_device_outputs(self._h, ctypes.byref(d)), self.ctx)
@@ -437,6 +477,67 @@ class Target:
         if getattr(self, "_h", None):
             if getattr(self.ctx, "_h", None):  # a closed context already destroyed its targets
                 self._lib.svo_target_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+class Net:
+    """The reconstruction net of learned frames (svo_net_*). Feature, output
+    and target arguments are device pointers (ints)."""
+
+    def __init__(self, ctx: Context, seed: int = 1):
+        self.ctx = ctx
+        self._lib = ctx._lib
+        self._h = _P()
+        _check(self._lib.svo_net_create(ctx._h, ctypes.byref(self._h)), ctx)
+        ctx._nets.add(self)
+        if seed != 1:
+            self.init(seed)
+
+    def init(self, seed: int) -> None:
+        _check(self._lib.svo_net_init(self._h, seed), self.ctx)
+
+    def set_params(self, params: np.ndarray) -> None:
+        p = np.ascontiguousarray(params, np.float32)
+        _check(self._lib.svo_net_set_params(self._h, _ptr(p), p.size), self.ctx)
+
+    def params(self) -> np.ndarray:
+        out = np.empty(NET_PARAMS, np.float32)
+        _check(self._lib.svo_net_get_params(self._h, _ptr(out), out.size), self.ctx)
+        return out
+
+    def grads(self) -> np.ndarray:
+        out = np.empty(NET_PARAMS, np.float32)
+        _check(self._lib.svo_net_get_grads(self._h, _ptr(out), out.size), self.ctx)
+        return out
+
+    def forward(self, d_features: int, w: int, h: int, d_out: int) -> None:
+        _check(self._lib.svo_net_forward(self._h, _P(d_features), w, h, _P(d_out)), self.ctx)
+
+    def infer(self, d_features: int, w: int, h: int, d_out: int) -> None:
+        _check(self._lib.svo_net_infer(self._h, _P(d_features), w, h, _P(d_out)), self.ctx)
+
+    def backward(self, d_features: int, d_target_bgrx: int, w: int, h: int, tau: float, lam: float):
+        loss = np.zeros(2, np.float32)
+        _check(self._lib.svo_net_backward(self._h, _P(d_features), _P(d_target_bgrx), w, h, tau, lam, _ptr(loss)),
+               self.ctx)
+        return float(loss[0]), float(loss[1])
+
+    def adam(self, lr: float, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8) -> None:
+        _check(self._lib.svo_net_adam(self._h, lr, beta1, beta2, eps), self.ctx)
+
+    def save(self, path: str) -> None:
+        np.save(path, self.params())
+
+    def load_file(self, path: str) -> None:
+        self.set_params(np.load(path))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            if getattr(self.ctx, "_h", None):
+                self._lib.svo_net_destroy(self._h)
             self._h = None
 
     def __del__(self):
