@@ -1,17 +1,21 @@
-"""Benchmark: warped sparse-voxel-octree frames/s at 1920x1024 on GB300.
+"""Benchmark: warped + learned sparse-voxel-octree frames/s at 1920x1024 on GB300.
 
-Workload (one step = one warped frame, the body of the reference's
-raycast_draw): 1920x1024, depth-11 (2048^3) seeded fBm terrain octree (visible
-shell), orbit camera at 1.5x extent, 0.5 degrees yaw per frame, height
-sinusoid 0.02x extent over 64 frames. Reported beside it: the plain full
-raycast of the same frames on the same GPU (Mrays/s, frames/s), the warped
-image's PSNR against it, per-stage times and the trace kernel's roofline.
+Workload (one step = one learned warp frame: the reference's raycast_draw
+reprojection, then the reconstruction net, then rays for the pixels the net is
+not confident about plus the 8x4 refresh tile): 1920x1024, depth-11 (2048^3)
+seeded fBm terrain octree (visible shell), orbit camera at 1.5x extent, 0.5
+degrees yaw per frame, height sinusoid 0.02x extent over 64 frames; the net's
+weights are the committed ones (train_net.py). Reported beside it: the plain
+full raycast of the same frames on the same GPU (Mrays/s, frames/s), PSNR and
+maximum error of the learned frames against it, the plain warp pipeline (the
+reference's algorithm, bit-exact) on the same frames, the fast-motion camera
+path, per-stage times and the rooflines of the trace and net kernels.
 
 Timing: each step is bracketed by CUDA events on the library's stream; the L2
 is flushed (256 MiB device write) before every timed step and outside its
 events. `value` = frames of all ranks / max over ranks of the summed step
 times. `e2e` times the C-ABI calls a user makes with host buffers: camera in,
-svo_warp_frame, BGRX8 image out to pinned host memory, per step.
+svo_warp_frame_learned, BGRX8 image out to pinned host memory, per step.
 
 --impl reference times the reference algorithm on the host CPU cores instead
 (oracle/_ref when it was compiled from the reference tree here, else the
@@ -37,7 +41,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "sparse-voxel-octree-raycasting_gb300"))
 
 METRIC = "Mrays/s; 1920x1024 frames/s warped+learned vs full raycast at ≥38 dB PSNR"
-WORKLOAD = "warped pipeline 1920x1024, depth-11 terrain octree, 256-frame orbit (0.5 deg/frame)"
+WORKLOAD = ("warped + learned pipeline 1920x1024, depth-11 terrain octree, 256-frame orbit (0.5 deg/frame), "
+            "confidence threshold 0.5")
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 
 
@@ -54,6 +59,8 @@ def parse_args(argv=None):
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (for profiling runs)")
     ap.add_argument("--graph", type=int, default=1, help="replay each warp frame as a CUDA graph")
     ap.add_argument("--views", type=int, default=8, help="camera streams of the concurrent multi-view measurement")
+    ap.add_argument("--threshold", type=float, default=0.5, help="confidence below which learned frames trace a pixel")
+    ap.add_argument("--weights", default=os.path.join(ROOT, "sparse-voxel-octree-raycasting_gb300", "net_weights.npy"))
     return ap.parse_args(argv)
 
 
@@ -188,7 +195,8 @@ def run_reference(args, rank: int, world: int) -> None:
         "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores,
                          "kind": "reference" if which == "reference" else "port",
                          "sample": f"{args.steps} consecutive warped frames (after {args.warmup} untimed) of the "
-                                   f"benchmark path at {W}x{H}"},
+                                   f"benchmark path at {W}x{H}; the reference's own pipeline (reprojection, "
+                                   f"hole filter, hole rays): it has no learned stage"},
         "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -209,31 +217,56 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     t_build = time.perf_counter() - t_build
     ctx = svo.Context(local_rank)
     ctx.upload(octree, validate=True)
-    tgt = ctx.target(W, H)
-    full = ctx.target(W, H)
+    net = svo.Net(ctx)
+    net.load_file(args.weights)
+    thr = args.threshold
+    tgt, tgt_l, full = ctx.target(W, H), ctx.target(W, H), ctx.target(W, H)
     if args.graph:
         tgt.use_graph(True)
+        tgt_l.use_graph(True)
     ext = torch.cuda.ExternalStream(ctx.stream, device=device)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
     frame_offset = rank * 512  # replicas render different stretches of the orbit
 
-    def view(f):
-        return svo.camera_path(1, depth, frame_offset + f, W, H)
+    def view(f, kind=1):
+        return svo.camera_path(kind, depth, frame_offset + f, W, H)
 
     def flush_l2():
         flush.zero_()
         torch.cuda.synchronize(device)
 
-    # ---- warped frames, device time per step
-    for f in range(args.warmup):
-        ctx.warp_frame(tgt, view(f), f)
-    ctx.synchronize()
+    def plain(t):
+        return lambda f, v: ctx.warp_frame(t, v, f)
+
+    def learned(t, th=thr):
+        return lambda f, v: ctx.warp_frame_learned(t, v, f, net, th)
+
+    def timed(render, kind=1):
+        """Device time (ms) of each of args.steps frames after args.warmup untimed ones."""
+        for f in range(args.warmup):
+            render(f, view(f, kind))
+        ctx.synchronize()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        for i in range(args.steps):
+            f = args.warmup + i
+            v = view(f, kind)
+            flush_l2()
+            starts[i].record(ext)
+            render(f, v)
+            ends[i].record(ext)
+        ctx.synchronize()
+        return [s_.elapsed_time(e_) for s_, e_ in zip(starts, ends)]
+
+    # ---- headline: learned warp frames, device time per step
     barrier(world)
     torch.cuda.synchronize(device)
+    for f in range(args.warmup):
+        ctx.warp_frame_learned(tgt_l, view(f), f, net, thr)
+    ctx.synchronize()
     clocks = ClockSampler(local_rank)
     clocks.start()
     launches0 = ctx.launch_count()
-    step_ms = []
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     for i in range(args.steps):
@@ -241,38 +274,53 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
         v = view(f)
         flush_l2()
         starts[i].record(ext)
-        ctx.warp_frame(tgt, v, f)
+        ctx.warp_frame_learned(tgt_l, v, f, net, thr)
         ends[i].record(ext)
     ctx.synchronize()
     launches = ctx.launch_count() - launches0
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    step_ms = [s_.elapsed_time(e_) for s_, e_ in zip(starts, ends)]
     clock_info = clocks.stop()
     barrier(world)
     torch.cuda.synchronize(device)
-    warped_s = sum(step_ms) / 1000.0
-    value, t_max = aggregate(args.steps, warped_s, world, device if world > 1 else None)
-    ms_per_step = 1000.0 * warped_s / args.steps
+    learned_s = sum(step_ms) / 1000.0
+    value, _ = aggregate(args.steps, learned_s, world, device if world > 1 else None)
+    ms_per_step = 1000.0 * learned_s / args.steps
 
-    # ---- the same frames with per-stage events (roofline and breakdown)
-    tgt2 = ctx.target(W, H)
+    # ---- the plain warp pipeline (bit-exact with the reference) on the same frames
+    tgt_p = ctx.target(W, H)
     if args.graph:
-        tgt2.use_graph(True)
-    tgt2.set_profiling(True)
-    for f in range(args.warmup):
-        ctx.warp_frame(tgt2, view(f), f)
-    ctx.synchronize()
-    stages = []
-    for i in range(args.steps):
-        f = args.warmup + i
-        flush_l2()
-        ctx.warp_frame(tgt2, view(f), f)
-        stages.append(tgt2.stage_times())
-    stage_names = ["project", "resolve_gather", "hole_scan", "hole_write", "trace", "fill_colorize"]
-    stages = np.array([s for s in stages if len(s) == len(stage_names)], np.float64)
-    if stages.size == 0:
-        raise RuntimeError("per-stage CUDA events returned no timings")
-    stage_ms = {n: float(stages[:, k].mean()) for k, n in enumerate(stage_names)}
-    tgt2.close()
+        tgt_p.use_graph(True)
+    plain_ms = timed(plain(tgt_p))
+    plain_fps = 1000.0 / statistics.mean(plain_ms)
+    tgt_p.close()
+
+    # ---- per-stage events of both pipelines
+    def stage_times(render_target, render, names):
+        render_target.set_profiling(True)
+        for f in range(args.warmup):
+            render(f, view(f))
+        ctx.synchronize()
+        rows = []
+        for i in range(args.steps):
+            f = args.warmup + i
+            flush_l2()
+            render(f, view(f))
+            rows.append(render_target.stage_times())
+        rows = np.array([r for r in rows if len(r) == len(names)], np.float64)
+        if rows.size == 0:
+            raise RuntimeError("per-stage CUDA events returned no timings")
+        return {n: float(rows[:, k].mean()) for k, n in enumerate(names)}
+
+    t_sp = ctx.target(W, H)
+    t_sl = ctx.target(W, H)
+    if args.graph:
+        t_sp.use_graph(True)
+        t_sl.use_graph(True)
+    stage_ms = stage_times(t_sp, plain(t_sp), ["project", "resolve_gather", "hole_scan", "hole_write", "trace",
+                                               "fill_colorize"])
+    stage_ms_learned = stage_times(t_sl, learned(t_sl), ["project", "resolve", "net", "trace"])
+    t_sp.close()
+    t_sl.close()
 
     # ---- plain full raycast of the same frames
     full_ms = []
@@ -290,39 +338,61 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     full_fps = 1000.0 / statistics.mean(full_ms)
     mrays_full = W * H * full_fps / 1e6
 
-    # ---- end to end through the C ABI with host buffers
+    # ---- end to end through the C ABI with host buffers (learned frames)
     host_img = torch.empty(W * H, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
     tgt3 = ctx.target(W, H)
     if args.graph:
         tgt3.use_graph(True)
     for f in range(args.warmup):
-        ctx.warp_frame(tgt3, view(f), f)
+        ctx.warp_frame_learned(tgt3, view(f), f, net, thr)
         tgt3.bgrx_into(host_img)
     e2e_s = 0.0
     for i in range(args.steps):
         f = args.warmup + i
         flush_l2()
         t0 = time.perf_counter()
-        ctx.warp_frame(tgt3, view(f), f)  # camera parameters travel host -> device inside the call
-        tgt3.bgrx_into(host_img)           # BGRX8 frame device -> pinned host, synchronising
+        ctx.warp_frame_learned(tgt3, view(f), f, net, thr)  # camera host -> device inside the call
+        tgt3.bgrx_into(host_img)                              # BGRX8 frame device -> pinned host, synchronising
         e2e_s += time.perf_counter() - t0
     e2e_value, _ = aggregate(args.steps, e2e_s, world, device if world > 1 else None)
+    tgt3.close()
 
-    # ---- quality: warped frames vs full raycast of the same cameras
-    psnr, traced_frac = [], []
-    tgt4 = ctx.target(W, H)
-    for f in range(args.warmup + args.steps):
-        v = view(f)
-        ctx.warp_frame(tgt4, v, f)
-        if f >= args.warmup:
-            ctx.raycast_full(full, v)
-            a = tgt4.bgrx()
-            b = full.bgrx()
-            psnr.append(svo.psnr_bgrx(a, b))
-            _, holes = tgt4.holes()
-            traced_frac.append(holes / (W * H))
-    tgt4.close()
-    psnr_mean = float(np.mean([p for p in psnr if np.isfinite(p)])) if psnr else None
+    # ---- quality against the full raycast of the same cameras
+    def quality(render, t, kind, traced_of):
+        mse, traced, worst = [], [], []
+        for f in range(args.warmup + args.steps):
+            v = view(f, kind)
+            render(f, v)
+            if f >= args.warmup:
+                ctx.raycast_full(full, v)
+                a, b = t.bgrx(), full.bgrx()
+                d = (a.view(np.uint8).reshape(-1, 4)[:, :3].astype(np.int32)
+                     - b.view(np.uint8).reshape(-1, 4)[:, :3].astype(np.int32))
+                mse.append(float((d.astype(np.float64) ** 2).mean()))
+                worst.append(int(np.abs(d).max()))
+                traced.append(traced_of(t) / (W * H))
+        m = float(np.mean(mse))
+        return {"psnr_db": 10 * np.log10(255.0 ** 2 / m) if m > 0 else float("inf"),
+                "max_abs_error": int(max(worst)), "traced_fraction": float(np.mean(traced))}
+
+    tq = ctx.target(W, H)
+    q_plain = quality(plain(tq), tq, 1, lambda t: t.holes()[1])
+    tq.close()
+    tq = ctx.target(W, H)
+    q_learned = quality(learned(tq), tq, 1, lambda t: t.requested())
+    tq.close()
+    # fast motion (2 deg/frame + 0.05 extent/frame), the learned configuration
+    tq = ctx.target(W, H)
+    if args.graph:
+        tq.use_graph(True)
+    fast_ms = timed(learned(tq), kind=2)
+    tq.close()
+    tq = ctx.target(W, H)
+    q_fast = quality(learned(tq), tq, 2, lambda t: t.requested())
+    tq.close()
+    tq = ctx.target(W, H)
+    q_fast_plain = quality(plain(tq), tq, 2, lambda t: t.holes()[1])
+    tq.close()
 
     # ---- several camera streams at once: one context (stream) per view, the
     # octree words shared; the warp frames of all views are in flight together
@@ -331,48 +401,58 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     if args.views > 1:
         d_words = torch.from_numpy(octree.words.view(np.int32)).to(device)
         torch.cuda.synchronize(device)
-        ctxs, tgts = [], []
+        ctxs, tgts, nets = [], [], []
         for k in range(args.views):
             c = svo.Context(local_rank)
             c.upload_device(d_words.data_ptr(), octree.words.size, octree.root, octree.depth)
             t = c.target(W, H)
+            n = svo.Net(c)
+            n.load_file(args.weights)
             if args.graph:
                 t.use_graph(True)
             ctxs.append(c)
             tgts.append(t)
+            nets.append(n)
 
         def mv_view(k, f):
             return svo.camera_path(1, depth, frame_offset + 37 * k + f, W, H)
 
-        for f in range(args.warmup):
-            for k in range(args.views):
-                ctxs[k].warp_frame(tgts[k], mv_view(k, f), f)
-        for c in ctxs:
-            c.synchronize()
-        mv_s = 0.0
-        for i in range(args.steps):
-            f = args.warmup + i
-            views = [mv_view(k, f) for k in range(args.views)]
-            flush_l2()
-            t0 = time.perf_counter()
-            for k in range(args.views):
-                ctxs[k].warp_frame(tgts[k], views[k], f)
+        multiview = {"views": args.views,
+                     "note": "host-timed: all views' frames launched, then every stream synchronised"}
+        for mode in ("learned", "plain"):
+            def go(k, f):
+                if mode == "learned":
+                    ctxs[k].warp_frame_learned(tgts[k], mv_view(k, f), f, nets[k], thr)
+                else:
+                    ctxs[k].warp_frame(tgts[k], mv_view(k, f), f)
+            for f in range(args.warmup):
+                for k in range(args.views):
+                    go(k, f)
             for c in ctxs:
                 c.synchronize()
-            mv_s += time.perf_counter() - t0
-        multiview = {"views": args.views, "frames_per_s": args.views * args.steps / mv_s,
-                     "ms_per_step": 1000.0 * mv_s / args.steps,
-                     "note": "host-timed: all views' warp frames launched, then every stream synchronised"}
+            mv_s = 0.0
+            for i in range(args.steps):
+                f = args.warmup + i
+                flush_l2()
+                t0 = time.perf_counter()
+                for k in range(args.views):
+                    go(k, f)
+                for c in ctxs:
+                    c.synchronize()
+                mv_s += time.perf_counter() - t0
+            multiview[mode] = {"frames_per_s": args.views * args.steps / mv_s, "ms_per_step": 1000.0 * mv_s / args.steps}
         for t in tgts:
             t.close()
+        for n in nets:
+            n.close()
         for c in ctxs:
             c.close()
         del d_words
 
-    # ---- CPU oracle on the same frames: parity of the last frame, fetch
+    # ---- CPU oracle on the same frames: parity of the last plain frame, fetch
     # counts for the roofline's algorithmic bytes, and the CPU baseline.
     cpu = None
-    algo_bytes_trace = None
+    bytes_per_ray = None
     parity = None
     if not args.no_cpu and rank == 0:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -382,7 +462,6 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
         threads = oracle.max_threads()
         warp = oracle.Warp(depth, W, H)
         n_cpu = args.steps if args.cpu_frames < 0 else min(args.cpu_frames, args.steps)
-        fetch_bytes = []
         for f in range(args.warmup):
             v = view(f)
             warp.frame(octree.words, octree.root, v.pos_array, v.m_array, f, threads)
@@ -391,38 +470,56 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
             f = args.warmup + i
             v = view(f)
             warp.frame(octree.words, octree.root, v.pos_array, v.m_array, f, threads)
-            st = warp.stats()  # rays, child fetches, colour fetches, boundary rays
-            holes = warp.hole_count()
-            # per traced ray: node words read + colour word + float4 store; per
-            # hole entry: its 4-byte id read
-            fetch_bytes.append(4.0 * (int(st[1]) + int(st[2])) + 20.0 * int(st[0]) + 4.0 * holes)
         cpu_s = time.perf_counter() - t0
         cpu = {"value": n_cpu / cpu_s, "unit": "frames/s", "cores": threads, "kind": "port",
                "sample": f"{n_cpu} consecutive warped frames of the benchmark path at {W}x{H} "
                          f"(after {args.warmup} untimed), oracle port of kernel.cl/raycast.h, OpenMP"}
-        algo_bytes_trace = float(np.mean(fetch_bytes))
         if n_cpu == args.steps:
-            parity = bool(np.array_equal(warp.tex(), tgt.bgrx()))
+            tp = ctx.target(W, H)
+            for f in range(args.warmup + args.steps):
+                ctx.warp_frame(tp, view(f), f)
+            parity = bool(np.array_equal(warp.tex(), tp.bgrx()))
+            tp.close()
+        # algorithmic bytes per traced ray, counted by the oracle on the full
+        # raycast of the last frame: node words + colour word read, float4 +
+        # colour word written (4 * fetches + 20)
+        v = view(args.warmup + args.steps - 1)
+        _, _, _, st = oracle.raycast_full(depth, octree.words, octree.root, v.pos_array, v.m_array, W, H,
+                                          1.0, 1.0, threads)
+        bytes_per_ray = (4.0 * (float(st[1]) + float(st[2])) + 20.0 * float(st[0])) / float(st[0])
 
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs")
+    tflops = peaks.get("bf16_tflops")
     roofline = None
-    if algo_bytes_trace is not None and stage_ms["trace"] > 0:
-        achieved = algo_bytes_trace / (stage_ms["trace"] * 1e-3) / 1e9
+    roofline_net = None
+    rays_learned = (q_learned["traced_fraction"] * W * H
+                    + (W // 8 + 15) // 16 * 16 * ((H // 4 + 15) // 16 * 16))
+    if bytes_per_ray is not None and stage_ms_learned["trace"] > 0:
+        algo = bytes_per_ray * rays_learned
+        achieved = algo / (stage_ms_learned["trace"] * 1e-3) / 1e9
         peak = hbm if hbm else 6800.0
-        roofline = {"bound": "hbm", "kernel": "k_trace_warp", "achieved": achieved, "peak": peak,
-                    "unit": "GB/s", "frac": achieved / peak,
-                    "peak_source": "measured" if hbm else "fallback",
-                    "algorithmic_bytes_per_launch": algo_bytes_trace, "traffic": None}
-    rays_per_frame = None
+        roofline = {"bound": "hbm", "kernel": "k_trace_warp (learned frame: requested pixels + refresh tile)",
+                    "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                    "peak_source": "measured" if hbm else "fallback", "algorithmic_bytes_per_launch": algo,
+                    "bytes_per_ray": bytes_per_ray, "rays_per_launch": rays_learned, "traffic": None}
+    if stage_ms_learned["net"] > 0:
+        flops = 12096.0 * W * H  # 2 * 9 * (8*16 + 16*16 + 16*16 + 16*4) per pixel
+        ach = flops / (stage_ms_learned["net"] * 1e-3) / 1e12
+        peak = tflops if tflops else 1900.0
+        roofline_net = {"bound": "tensor", "kernel": "k_net_infer", "achieved": ach, "peak": peak,
+                        "unit": "TFLOP/s", "frac": ach / peak, "peak_source": "measured" if tflops else "fallback",
+                        "hbm_gbs": 24.0 * W * H / (stage_ms_learned["net"] * 1e-3) / 1e9,
+                        "flops_per_launch": flops}
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32",
+            "vs_baseline": None, "dtype": "f32 traversal, bf16 net",
             "data": "synthetic: seeded value-noise fBm terrain (visible shell), seeded orbit camera",
             "config": {"workload": WORKLOAD, "res": [W, H], "depth": depth, "seed": args.seed,
                        "octree_words": int(octree.words.size), "voxels": int(octree.voxels),
+                       "confidence_threshold": thr, "weights": os.path.relpath(args.weights, ROOT),
                        "l2": "flushed before every timed step (256 MiB device write, outside the step events)",
                        "cuda_graph": bool(args.graph), "replicas": world},
             "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": 4 * 33,
@@ -430,20 +527,27 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
             "gpu_launches": int(launches),
             "clocks": clock_info,
             "roofline": roofline,
+            "roofline_net": roofline_net,
             "cpu_baseline": cpu,
             "full_raycast": {"frames_per_s": full_fps, "mrays_per_s": mrays_full,
                              "ms_per_frame": statistics.mean(full_ms)},
             "speedup_vs_full": value / world / full_fps,
-            "psnr_db_vs_full": psnr_mean,
-            "hole_pixel_fraction": float(np.mean(traced_frac)) if traced_frac else None,
-            "stage_ms": stage_ms,
+            "learned": q_learned,
+            "plain_warped": {"frames_per_s": plain_fps, "ms_per_frame": statistics.mean(plain_ms),
+                             "speedup_vs_full": plain_fps / full_fps, **q_plain},
+            "fast_motion": {"workload": "2 deg/frame yaw + 0.05 extent/frame translation",
+                            "learned_frames_per_s": 1000.0 / statistics.mean(fast_ms), "learned": q_fast,
+                            "plain": q_fast_plain},
+            "stage_ms": stage_ms_learned,
+            "stage_ms_plain": stage_ms,
             "multiview": multiview,
-            "parity_last_frame_vs_oracle": parity,
+            "parity_plain_vs_oracle": parity,
             "octree_build_s": t_build,
         }
         print(json.dumps(line), flush=True)
-    for t in (tgt, full, tgt3):
+    for t in (tgt, tgt_l, full):
         t.close()
+    net.close()
     ctx.close()
 
 

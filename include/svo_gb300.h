@@ -227,8 +227,9 @@ svo_status svo_target_set_feature_tap(svo_target* t, float* d_features);
 /* Creates a net on the context, initialised by svo_net_init(net, 1). */
 svo_status svo_net_create(svo_context* ctx, svo_net** out);
 svo_status svo_net_destroy(svo_net* net);
-/* Seeded He-normal weights (last layer scaled by 0.1), zero biases; resets
- * the optimiser. */
+/* Seeded He-normal weights; the last layer's colour weights zero (the net
+ * starts as the identity on colour) and its confidence weights scaled by
+ * 0.1; zero biases. Resets the optimiser. */
 svo_status svo_net_init(svo_net* net, uint64_t seed);
 /* n must be SVO_NET_PARAMS. set_params resets the optimiser. */
 svo_status svo_net_set_params(svo_net* net, const float* host, size_t n);

@@ -8,7 +8,8 @@ the product imports it.
 
 Net: four 3x3 "same" convolutions with zero padding at the frame border,
 channels 8 -> 16 -> 16 -> 16 -> 4, ReLU after the first three. Inputs
-(8 planes): R, G, B, depth, hole mask, motion magnitude, 0, 0. Outputs
+(8 planes): R, G, B, depth, hole mask, motion magnitude, sub-pixel offset, ray
+elevation. Outputs
 (4 planes): R, G, B (the input colour plus the last layer's first three
 channels) and a confidence logit.
 

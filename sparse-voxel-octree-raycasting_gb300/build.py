@@ -31,7 +31,7 @@ CXX_FLAGS = ["-std=c++17", "-O3", "-ffp-contract=off", "-fno-fast-math", "-fPIC"
 
 SOURCES_CU = ["svo_device.cu"]
 SOURCES_CPP = ["svo_host.cpp"]
-HEADERS = ["svo_trace.cuh", "svo_kernels.cuh"]
+HEADERS = ["svo_trace.cuh", "svo_kernels.cuh", "svo_net.cuh"]
 
 
 def _nvcc() -> str:
@@ -59,6 +59,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     """Compiles (if stale) and returns the path of libsvo_gb300.so."""
     os.makedirs(OBJ, exist_ok=True)
     deps = [os.path.join(CSRC, f) for f in SOURCES_CU + SOURCES_CPP + HEADERS]
+    deps += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h", ".hpp"))]
     deps.append(os.path.join(INCLUDE, "svo_gb300.h"))
     deps.append(os.path.abspath(__file__))
     newest = max(_mtime(d) for d in deps)

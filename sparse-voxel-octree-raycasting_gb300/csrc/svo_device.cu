@@ -1118,8 +1118,9 @@ svo_status svo_net_set_params(svo_net* net, const float* host, size_t n) {
     return SVO_OK;
 }
 
-// He-normal weights (seeded splitmix64 + Box-Muller), the last layer scaled
-// by 0.1, zero biases.
+// He-normal weights (seeded splitmix64 + Box-Muller), the confidence output's
+// weights scaled by 0.1, the colour outputs' weights zero (the net starts as
+// the identity on colour), zero biases.
 svo_status svo_net_init(svo_net* net, uint64_t seed) {
     if (!net) return SVO_ERR_INVALID_ARGUMENT;
     std::vector<float> p(kNetParams, 0.0f);
@@ -1135,7 +1136,10 @@ svo_status svo_net_init(svo_net* net, uint64_t seed) {
         const double sd = std::sqrt(2.0 / (9.0 * net_cin(l))) * (l == kNetLayers - 1 ? 0.1 : 1.0);
         for (int i = 0; i < 9 * net_cin(l) * net_cout(l); ++i) {
             const double u1 = next(), u2 = next();
-            p[net_w_off(l) + i] = (float)(sd * std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2));
+            const double w = sd * std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+            // the colour outputs start as the identity (residual weights 0)
+            const bool colour_out = l == kNetLayers - 1 && i % net_cout(l) < 3;
+            p[net_w_off(l) + i] = colour_out ? 0.0f : (float)w;
         }
     }
     return svo_net_set_params(net, p.data(), p.size());

@@ -64,40 +64,74 @@ __host__ __device__ __forceinline__ float bf16_round(float x) {
 //   5    reprojection motion: distance in pixels between where the cached
 //        point appears now and where it appeared from the previous camera,
 //        clamped to 8 and divided by 8 (1 when it was behind that camera)
-//   6-7  0
+//   6    distance in pixels between the pixel centre (which the pixel's own
+//        ray passes through) and where the cached point projects now,
+//        clamped to 1; 0 when empty
+//   7    elevation of the pixel's ray: (1 + world-y of its unit direction)/2,
+//        for every pixel (rays above the horizon of the periodic terrain
+//        meet nothing)
 // (The previous camera travels in FrameParams: prev_pos, prev_vx/vy/vz.)
-__device__ __forceinline__ void net_features(const FrameParams& P, const TargetBuffers& B, int x, int y, float f[8]) {
+// net_load fetches what net_compute needs, so callers can issue the loads
+// of several pixels before using any of them.
+struct NetPixel {
+    uint32_t c;
+    float4 q;
+};
+
+__device__ __forceinline__ NetPixel net_load(const FrameParams& P, const TargetBuffers& B, int x, int y) {
     const size_t ofs = (size_t)y * B.res_x + x;
-    const uint32_t c = plane_col(B, P.cur)[ofs];
+    NetPixel px;
+    px.c = __ldg(plane_col(B, P.cur) + ofs);
+    px.q = __ldg(plane_xyz(B, P.cur) + ofs);
+    return px;
+}
+
+__device__ __forceinline__ void net_compute(const FrameParams& P, int res_x, int res_y, int x, int y,
+                                            const NetPixel& px, float f[8]) {
 #pragma unroll
     for (int i = 0; i < 8; ++i) f[i] = 0.0f;
-    if (c == kEmptyPixel) {
+    {
+        const float d1x = ((float)(x - (res_x >> 1)) + 0.5f) * P.ray.fovx / (float)res_y;
+        const float d1y = ((float)(y - (res_y >> 1)) + 0.5f) * P.ray.fovy / (float)res_y;
+        const float dx = d1x * P.ray.mxx + d1y * P.ray.mxy + P.ray.mxz;
+        const float dy = d1x * P.ray.myx + d1y * P.ray.myy + P.ray.myz;
+        const float dz = d1x * P.ray.mzx + d1y * P.ray.mzy + P.ray.mzz;
+        f[7] = 0.5f + 0.5f * dy * rsqrtf(dx * dx + dy * dy + dz * dz);
+    }
+    if (px.c == kEmptyPixel) {
         f[4] = 1.0f;
         return;
     }
-    const uint32_t bgrx = colorize(c);
+    const uint32_t bgrx = colorize(px.c);
     f[0] = (float)((bgrx >> 16) & 255u) * (1.0f / 255.0f);
     f[1] = (float)((bgrx >> 8) & 255u) * (1.0f / 255.0f);
     f[2] = (float)(bgrx & 255u) * (1.0f / 255.0f);
-    const float4 q = plane_xyz(B, P.cur)[ofs];
+    const float4 q = px.q;
     const float ax = q.x - P.ray.px, ay = q.y - P.ray.py, az = q.z - P.ray.pz;
     const float d = sqrtf(ax * ax + ay * ay + az * az);
     f[3] = fminf(log2f(1.0f + d) * (1.0f / 16.0f), 1.0f);
-    float m = 8.0f;
+    const float ry = (float)res_y;
+    const float zc = ax * P.vz[0] + ay * P.vz[1] + az * P.vz[2];
+    float sxc = 0.0f, syc = 0.0f;
+    if (zc >= 0.05f) {
+        const float iz = ry / zc;
+        sxc = (ax * P.vx[0] + ay * P.vx[1] + az * P.vx[2]) * iz;
+        syc = (ax * P.vy[0] + ay * P.vy[1] + az * P.vy[2]) * iz;
+        const float ex = sxc + 0.5f * (float)res_x - ((float)x + 0.5f);
+        const float ey = syc + 0.5f * ry - ((float)y + 0.5f);
+        f[6] = fminf(sqrtf(ex * ex + ey * ey), 1.0f);
+    }
+    float m = 0.0f;
     if (P.have_prev_view) {
+        m = 8.0f;
         const float bx = q.x - P.prev_pos[0], by = q.y - P.prev_pos[1], bz = q.z - P.prev_pos[2];
         const float zp = bx * P.prev_vz[0] + by * P.prev_vz[1] + bz * P.prev_vz[2];
-        const float zc = ax * P.vz[0] + ay * P.vz[1] + az * P.vz[2];
         if (zp >= 0.05f && zc >= 0.05f) {
-            const float ry = (float)B.res_y;
-            const float sxp = (bx * P.prev_vx[0] + by * P.prev_vx[1] + bz * P.prev_vx[2]) * ry / zp;
-            const float syp = (bx * P.prev_vy[0] + by * P.prev_vy[1] + bz * P.prev_vy[2]) * ry / zp;
-            const float sxc = (ax * P.vx[0] + ay * P.vx[1] + az * P.vx[2]) * ry / zc;
-            const float syc = (ax * P.vy[0] + ay * P.vy[1] + az * P.vy[2]) * ry / zc;
+            const float iz = ry / zp;
+            const float sxp = (bx * P.prev_vx[0] + by * P.prev_vx[1] + bz * P.prev_vx[2]) * iz;
+            const float syp = (bx * P.prev_vy[0] + by * P.prev_vy[1] + bz * P.prev_vy[2]) * iz;
             m = fminf(sqrtf((sxc - sxp) * (sxc - sxp) + (syc - syp) * (syc - syp)), 8.0f);
         }
-    } else {
-        m = 0.0f;
     }
     f[5] = m * 0.125f;
 }
@@ -107,8 +141,9 @@ __global__ void __launch_bounds__(256) k_net_features(const FrameParams* __restr
                                                       float* out) {
     const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
     if (x >= B.res_x || y >= B.res_y) return;
+    const FrameParams p = *P;
     float f[8];
-    net_features(*P, B, x, y, f);
+    net_compute(p, B.res_x, B.res_y, x, y, net_load(p, B, x, y), f);
     const size_t n = (size_t)B.res_x * B.res_y, ofs = (size_t)y * B.res_x + x;
 #pragma unroll
     for (int i = 0; i < 8; ++i) out[i * n + ofs] = f[i];
@@ -189,14 +224,21 @@ __device__ __forceinline__ void tc_commit(uint32_t mbar) {
                  : "memory");
 }
 
-__device__ __forceinline__ void tc_ld16(uint32_t taddr, float v[16]) {
-    uint32_t r[16];
+// 16 columns of this warp's 32 lanes; the registers are valid only after
+// tc_wait_ld (so several loads can be in flight together).
+__device__ __forceinline__ void tc_ld16_nowait(uint32_t taddr, uint32_t r[16]) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
           "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
         : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float v[16]) {
+    uint32_t r[16];
+    tc_ld16_nowait(taddr, r);
+    tc_wait_ld();
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
@@ -211,12 +253,26 @@ __device__ __forceinline__ void tc_ld4(uint32_t taddr, float v[4]) {
     for (int i = 0; i < 4; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// try_wait that may suspend the thread for up to ~20 us while the phase is
+// incomplete (fewer spinning instructions competing with the MMA issuer).
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, 20000;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
 // Bounded wait on an mbarrier phase (~0.5 s), false on timeout.
 __device__ __forceinline__ bool mbar_wait_phase(uint32_t bar, uint32_t parity) {
-    if (mbar_try_wait(bar, parity)) return true;
+    if (mbar_try_wait_sleep(bar, parity)) return true;
     const uint64_t t0 = global_ns();
     for (;;) {
-        if (mbar_try_wait(bar, parity)) return true;
+        if (mbar_try_wait_sleep(bar, parity)) return true;
         if (global_ns() - t0 > 500000000ull) return false;
     }
 }
@@ -291,7 +347,7 @@ __global__ void __launch_bounds__(128, 1) k_net_probe(uint32_t* result) {
 }
 
 // ------------------------------------------------ fused inference --
-// One CTA (256 threads) per SM walks 56x24-pixel output tiles. A tile's input
+// One CTA (512 threads) per SM walks 56x24-pixel output tiles. A tile's input
 // window is 64x32 positions (a 4-pixel halo for the four 3x3 layers), stored
 // as "positions" p = row*64 + col. Activations live in shared memory as
 // planes of 8 bf16 channels (16 bytes per position, positions consecutive),
@@ -304,11 +360,11 @@ __global__ void __launch_bounds__(128, 1) k_net_probe(uint32_t* result) {
 // 16-byte rows (an implicit GEMM with no im2col copy). Positions whose column
 // wraps into the next row are computed and never used. Each block
 // accumulates into its own 16 columns of tensor memory; one thread issues all
-// MMAs of a layer and commits them to an mbarrier; the 8 warps then read the
-// accumulators back (warp w reads tensor-memory lanes 32*(w%4)..+31, warps
-// w and w+4 split the blocks), add the bias, apply ReLU, zero the positions
-// outside the frame (the border padding) and store bf16 into the other
-// buffer. The last layer writes the outputs.
+// MMAs of a layer and commits them to an mbarrier; the 16 warps then read the
+// accumulators back (warp w reads tensor-memory lanes 32*(w%4)..+31, the four
+// warps of a lane group split the blocks), add the bias, apply ReLU, zero the
+// positions outside the frame (the border padding) and store bf16 into the
+// other buffer. The last layer writes the outputs.
 constexpr int kNetTW = 64, kNetTH = 32, kNetPos = kNetTW * kNetTH;
 constexpr int kNetGuard = 128;
 constexpr int kNetPlaneBytes = (kNetPos + 2 * kNetGuard) * 16;  // 36864
@@ -320,7 +376,8 @@ constexpr int kNetSmemBias = kNetSmemW + kNetMmaTotal * 512;     // 52 floats
 constexpr int kNetSmemRgb = kNetSmemBias + 256;                  // 3 x 2048 floats
 constexpr int kNetSmemBytes = kNetSmemRgb + 3 * kNetPos * 4;      // 188672
 constexpr int kNetTmemCols = 256;
-constexpr int kNetThreads = 256;
+constexpr int kNetThreads = 512;
+constexpr int kNetWarps = kNetThreads / 32;
 
 struct NetInferArgs {
     const uint16_t* packed;  // tensor-core weight image
@@ -336,10 +393,47 @@ struct NetInferArgs {
     uint32_t* fault;
 };
 
+// Two floats to a packed bf16 pair, round to nearest even (lo in the low half).
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+    uint32_t r;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    return r;
+}
+
+// All MMAs of layer L for the blocks of one tile (issued by one thread).
+template <int L>
+__device__ __forceinline__ void net_issue_layer(uint32_t sbase, uint32_t tmem) {
+    constexpr int kMmas = net_mmas(L);
+    constexpr int kBlocks = 15 - L;
+    constexpr int kFirst = (L + 1) * kNetTW;
+    constexpr uint32_t kIn = (L & 1) ? kNetSmemA : kNetSmemB;
+    uint64_t ad[kMmas], bd[kMmas];
+#pragma unroll
+    for (int m = 0; m < kMmas; ++m) {
+        int shift, lbo;
+        if (L == 0) {
+            const int t0 = 2 * m, t1 = 2 * m + 1;
+            shift = (t0 / 3 - 1) * kNetTW + (t0 % 3 - 1);
+            lbo = t1 < 9 ? ((t1 / 3 - 1) * kNetTW + (t1 % 3 - 1) - shift) * 16 : 16;
+        } else {
+            shift = (m / 3 - 1) * kNetTW + (m % 3 - 1);
+            lbo = kNetPlaneBytes;
+        }
+        ad[m] = tc_desc(sbase + kIn + (uint32_t)((kNetGuard + kFirst + shift) * 16), (uint32_t)lbo, 128u);
+        bd[m] = tc_desc(sbase + kNetSmemW + (uint32_t)((net_mma_base(L) + m) * 512), 128u, 256u);
+    }
+    for (int j = 0; j < kBlocks; ++j) {
+        // block j starts 128 positions (2048 bytes, 128 in the address field) later
+#pragma unroll
+        for (int m = 0; m < kMmas; ++m) tc_mma(tmem + 16u * j, ad[m] + 128ull * j, bd[m], m > 0 ? 1u : 0u);
+    }
+}
+
 template <bool kPipeline>
 __global__ void __launch_bounds__(kNetThreads, 1) k_net_infer(NetInferArgs A) {
     __shared__ uint64_t mbar;
     __shared__ uint32_t tmem_base_s;
+    __shared__ FrameParams sP;
     uint8_t* smem = reinterpret_cast<uint8_t*>(svo_dsmem);
     const uint32_t sbase = smem_addr(smem);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -354,6 +448,11 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_infer(NetInferArgs A) {
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (kPipeline) {
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(A.P);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(&sP);
+        for (int i = tid; i < (int)(sizeof(FrameParams) / 4); i += kNetThreads) dst[i] = src[i];
     }
     // weights, biases; zero both activation buffers (guards included)
     {
@@ -380,31 +479,43 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_infer(NetInferArgs A) {
     for (int tile = blockIdx.x; tile < A.tiles; tile += gridDim.x) {
         const int ox = (tile % A.tiles_x) * kNetOutW, oy = (tile / A.tiles_x) * kNetOutH;
         const int wx = ox - 4, wy = oy - 4;  // image position of window position 0
-        // ---- input features -> buffer B plane 0 (bf16) and rgb_in (rounded floats)
-        for (int p = tid; p < kNetPos; p += kNetThreads) {
+        // ---- input features -> buffer B plane 0 (bf16) and rgb_in (rounded floats);
+        // every thread first issues the loads of all its positions
+        constexpr int kPer = kNetPos / kNetThreads;
+        NetPixel px[kPer];
+#pragma unroll
+        for (int k = 0; k < kPer; ++k) {
+            const int p = tid + k * kNetThreads;
+            const int gx = wx + (p & (kNetTW - 1)), gy = wy + (p >> 6);
+            px[k].c = kEmptyPixel;
+            if (kPipeline && gx >= 0 && gx < W && gy >= 0 && gy < H) px[k] = net_load(sP, A.B, gx, gy);
+        }
+#pragma unroll
+        for (int k = 0; k < kPer; ++k) {
+            const int p = tid + k * kNetThreads;
             const int gx = wx + (p & (kNetTW - 1)), gy = wy + (p >> 6);
             float f[8];
             if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
                 if (kPipeline) {
-                    net_features(*A.P, A.B, gx, gy, f);
+                    net_compute(sP, W, H, gx, gy, px[k], f);
                 } else {
                     const size_t n = (size_t)W * H, ofs = (size_t)gy * W + gx;
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) f[i] = A.feat[i * n + ofs];
+                    for (int i = 0; i < 8; ++i) f[i] = __ldg(A.feat + i * n + ofs);
                 }
             } else {
 #pragma unroll
                 for (int i = 0; i < 8; ++i) f[i] = 0.0f;
             }
             uint4 v;
-            v.x = bf16_bits(f[0]) | (bf16_bits(f[1]) << 16);
-            v.y = bf16_bits(f[2]) | (bf16_bits(f[3]) << 16);
-            v.z = bf16_bits(f[4]) | (bf16_bits(f[5]) << 16);
-            v.w = bf16_bits(f[6]) | (bf16_bits(f[7]) << 16);
+            v.x = pack_bf16x2(f[0], f[1]);
+            v.y = pack_bf16x2(f[2], f[3]);
+            v.z = pack_bf16x2(f[4], f[5]);
+            v.w = pack_bf16x2(f[6], f[7]);
             *reinterpret_cast<uint4*>(smem + kNetSmemB + (kNetGuard + p) * 16) = v;
-            rgb_in[p] = bf16_round(f[0]);
-            rgb_in[kNetPos + p] = bf16_round(f[1]);
-            rgb_in[2 * kNetPos + p] = bf16_round(f[2]);
+            rgb_in[p] = __uint_as_float(v.x << 16);
+            rgb_in[kNetPos + p] = __uint_as_float(v.x & 0xFFFF0000u);
+            rgb_in[2 * kNetPos + p] = __uint_as_float(v.y << 16);
         }
         fence_async_smem();
         tc_fence_before();
@@ -414,28 +525,14 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_infer(NetInferArgs A) {
         for (int l = 0; l < kNetLayers; ++l) {
             const int nb = 15 - l;
             const int first = (l + 1) * kNetTW;
-            const uint32_t in_off = (l & 1) ? kNetSmemA : kNetSmemB;
             const uint32_t out_off = (l & 1) ? kNetSmemB : kNetSmemA;
             if (tid == 0) {
                 tc_fence_after();
-                const uint32_t wbase = sbase + kNetSmemW + net_mma_base(l) * 512;
-                for (int j = 0; j < nb; ++j) {
-                    const int bs = first + 128 * j;
-                    for (int m = 0; m < net_mmas(l); ++m) {
-                        int shift, lbo;
-                        if (l == 0) {
-                            const int t0 = 2 * m, t1 = 2 * m + 1;
-                            shift = (t0 / 3 - 1) * kNetTW + (t0 % 3 - 1);
-                            lbo = t1 < 9 ? ((t1 / 3 - 1) * kNetTW + (t1 % 3 - 1) - shift) * 16 : 16;
-                        } else {
-                            shift = (m / 3 - 1) * kNetTW + (m % 3 - 1);
-                            lbo = kNetPlaneBytes;
-                        }
-                        const uint32_t a_addr = sbase + in_off + (uint32_t)((kNetGuard + bs + shift) * 16);
-                        const uint64_t ad = tc_desc(a_addr, (uint32_t)lbo, 128u);
-                        const uint64_t bd = tc_desc(wbase + m * 512, 128u, 256u);
-                        tc_mma(tmem + 16u * j, ad, bd, m > 0 ? 1u : 0u);
-                    }
+                switch (l) {
+                    case 0: net_issue_layer<0>(sbase, tmem); break;
+                    case 1: net_issue_layer<1>(sbase, tmem); break;
+                    case 2: net_issue_layer<2>(sbase, tmem); break;
+                    default: net_issue_layer<3>(sbase, tmem); break;
                 }
                 tc_commit(bar);
             }
@@ -448,28 +545,44 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_infer(NetInferArgs A) {
                 fault |= kFaultNet;
                 break;
             }
-            {
-                const int g = warp & 3;
-                for (int j = warp >> 2; j < nb; j += 2) {
+            const int g = warp & 3;
+            if (l < kNetLayers - 1) {
+                // the (at most 4) blocks of this warp: all loads in flight, one wait
+                constexpr int kSlices = kNetWarps / 4;
+                uint32_t r[4][16];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int j = (warp >> 2) + k * kSlices;
+                    if (j < nb) tc_ld16_nowait(tmem + ((uint32_t)(32 * g) << 16) + 16u * j, r[k]);
+                }
+                tc_wait_ld();
+                const float* bl = bias + 16 * l;
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int j = (warp >> 2) + k * kSlices;
+                    if (j >= nb) continue;
+                    const int p = first + 128 * j + 32 * g + lane;  // this thread's position
+                    const int gx = wx + (p & (kNetTW - 1)), gy = wy + (p >> 6);
+                    const bool inside = gx >= 0 && gx < W && gy >= 0 && gy < H;
+                    uint32_t h[8];
+#pragma unroll
+                    for (int c = 0; c < 16; c += 2) {
+                        const float a0 = inside ? fmaxf(__uint_as_float(r[k][c]) + bl[c], 0.0f) : 0.0f;
+                        const float a1 = inside ? fmaxf(__uint_as_float(r[k][c + 1]) + bl[c + 1], 0.0f) : 0.0f;
+                        h[c >> 1] = pack_bf16x2(a0, a1);
+                    }
+                    *reinterpret_cast<uint4*>(smem + out_off + (kNetGuard + p) * 16) =
+                        make_uint4(h[0], h[1], h[2], h[3]);
+                    *reinterpret_cast<uint4*>(smem + out_off + kNetPlaneBytes + (kNetGuard + p) * 16) =
+                        make_uint4(h[4], h[5], h[6], h[7]);
+                }
+            } else {
+                for (int j = warp >> 2; j < nb; j += kNetWarps / 4) {
                     const int p = first + 128 * j + 32 * g + lane;  // this thread's position
                     const int gx = wx + (p & (kNetTW - 1)), gy = wy + (p >> 6);
                     const bool inside = gx >= 0 && gx < W && gy >= 0 && gy < H;
                     const uint32_t taddr = tmem + ((uint32_t)(32 * g) << 16) + 16u * j;
-                    if (l < kNetLayers - 1) {
-                        float v[16];
-                        tc_ld16(taddr, v);
-                        uint32_t h[8];
-#pragma unroll
-                        for (int c = 0; c < 16; c += 2) {
-                            const float a0 = inside ? fmaxf(v[c] + bias[16 * l + c], 0.0f) : 0.0f;
-                            const float a1 = inside ? fmaxf(v[c + 1] + bias[16 * l + c + 1], 0.0f) : 0.0f;
-                            h[c >> 1] = bf16_bits(a0) | (bf16_bits(a1) << 16);
-                        }
-                        *reinterpret_cast<uint4*>(smem + out_off + (kNetGuard + p) * 16) =
-                            make_uint4(h[0], h[1], h[2], h[3]);
-                        *reinterpret_cast<uint4*>(smem + out_off + kNetPlaneBytes + (kNetGuard + p) * 16) =
-                            make_uint4(h[4], h[5], h[6], h[7]);
-                    } else {
+                    {
                         float v[4];
                         tc_ld4(taddr, v);
                         const int col = p & (kNetTW - 1);

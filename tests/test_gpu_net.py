@@ -22,7 +22,7 @@ def _rand_case(seed, W, H):
     params = no.init_params(seed) + (rng.standard_normal(no.NET_PARAMS) * 0.05).astype(np.float32)
     feat = rng.random((8, H, W)).astype(np.float32)
     feat[4] = (feat[4] > 0.7).astype(np.float32)
-    feat[6:] = 0
+    feat[6:] *= 0.5
     tgt = rng.integers(0, 1 << 24, H * W, dtype=np.uint32)
     return params.astype(np.float32), feat, tgt
 
@@ -153,7 +153,14 @@ def test_feature_tap(svo, scene, gpu_ctx, net):
             assert np.all(hole == 1.0)  # no cache yet: everything is a hole
         else:
             assert hole.mean() < 0.9
-        assert np.all(feat[:4, hole == 1.0] == 0.0) and np.all(feat[6:] == 0.0)
-        assert np.all((feat[5] >= 0) & (feat[5] <= 1))
+        assert np.all(feat[:4, hole == 1.0] == 0.0) and np.all(feat[5:7, hole == 1.0] == 0.0)
+        assert np.all((feat[5:] >= 0) & (feat[5:] <= 1))
+        if f >= 2:
+            # reprojected points land anywhere inside their pixel
+            sub = feat[6][hole == 0.0]
+            assert 0.1 < sub.mean() < 0.7
+        # ray elevation: defined for every pixel, monotonic down the image columns
+        elev = feat[7]
+        assert np.all(np.diff(elev[:, W // 2]) > 0) or np.all(np.diff(elev[:, W // 2]) < 0)
     t.set_feature_tap(None)
     t.close()
