@@ -147,6 +147,15 @@ svo_status svo_raycast_full_batch(svo_context* ctx, svo_target* const* targets, 
  * stays on the device). Asynchronous on the context stream. */
 svo_status svo_warp_frame(svo_context* ctx, svo_target* t, const svo_view* view, int frame);
 
+/* Which cache plane a warp frame copies its result into (src/raycast.h:394-
+ * 405). mode 0 (default): plane 2, as the reference ships it (plane 1 is
+ * never written). mode 1: the alternative the reference leaves commented out
+ * at raycast.h:395, ((frame>>4)%2)+1 -- the two cache planes alternate every
+ * 16 frames, both are reprojected every frame, and rejected source pixels are
+ * cleared in their cache plane (kernel/kernel.cl:549-562). Learned frames
+ * always use one cache plane. */
+svo_status svo_target_set_cache_mode(svo_target* t, int mode);
+
 /* Capture the warp frame of this target as a CUDA graph on first use and
  * replay it on later calls (the per-frame parameters are the arguments of
  * the graph's first kernel node, updated before each replay). Plain and
@@ -168,13 +177,15 @@ int svo_target_stage_times(svo_target* t, float* ms, int cap);
  * res_x*res_y elements (4 floats per pixel for coordinates). */
 
 /* Warp planes. plane 0: displayed colour words after raycast_fillhole2
- * (reference plane 0 at the end of raycast_draw); plane 2: the cache plane
- * (colour words before the filter, the memcpy target of :394-405);
- * plane 1: the reference's never-written second cache (all SVO_EMPTY_PIXEL). */
+ * (reference plane 0 at the end of raycast_draw); planes 1 and 2: the
+ * reference's cache planes (colour words before the filter; the memcpy target
+ * of :394-405 holds this frame's plane 0). With cache mode 0, plane 1 is never
+ * written (all SVO_EMPTY_PIXEL). */
 svo_status svo_read_colour(svo_target* t, int plane, uint32_t* host);
-/* Coordinate (back) buffer of the cache plane: x,y,z world hit position; w is
- * the view-space depth for reprojected pixels and the ray distance for
- * traced pixels. Only pixels whose colour is not SVO_EMPTY_PIXEL are defined. */
+/* Coordinate (back) buffer of a plane (0: the last frame's plane 0 before
+ * the filter, 1 or 2: the cache planes): x,y,z world hit position; w is the
+ * view-space depth for reprojected pixels and the ray distance for traced
+ * pixels. Only pixels whose colour is not SVO_EMPTY_PIXEL are defined. */
 svo_status svo_read_coords(svo_target* t, int plane, float* host);
 /* The hole id buffer of the last warp frame in the reference's layout
  * (kernel/kernel.cl:276-340): [0] total entries, [tiles..2*tiles) exclusive

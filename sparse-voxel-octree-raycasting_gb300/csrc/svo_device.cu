@@ -78,9 +78,15 @@ struct svo_target {
     uint32_t* full_col = nullptr;
     float4* full_xyzw = nullptr;
     uint64_t* full_vox = nullptr;
-    uint64_t frames = 0;      // warp frames issued (parity of the current plane)
-    int last_cur = 0;
+    uint64_t frames = 0;      // warp frames issued
     bool have_prev = false;
+    // Roles of the three physical planes (see plan_planes): the last frame's
+    // plane 0 (reference plane `last_target`), the other cache plane (the
+    // reference's plane 3 - last_target, -1 while it is empty).
+    int cache_mode = 0;  // 0: copy target 2 (raycast.h:395); 1: ((frame>>4)%2)+1
+    int last_cur = 0;
+    int other = -1;
+    int last_target = 2;
     // previous frame's camera (motion feature of learned frames)
     svo_view prev_view{};
     bool have_prev_view = false;
@@ -361,7 +367,46 @@ void record(svo_target* t, int i) {
         cudaEventRecord(t->ev[i], t->ctx->stream);
 }
 
-FrameParams make_params(const svo_target* t, const svo_view& v, int frame, int cur, bool have_cache) {
+// Which physical plane plays which role in one frame. The reference keeps
+// plane 0 (current) and cache planes 1 and 2, projects both caches into
+// plane 0 and copies plane 0 into the target cache at the end. Here plane 0
+// is written into a free physical plane and simply becomes the target cache
+// (no copy); the other cache keeps its physical plane.
+struct PlanePlan {
+    int cur, src[2], target, other_after, fill_past;
+    bool clear;
+};
+
+PlanePlan plan_planes(const svo_target* t, int frame, bool have_cache, int mode) {
+    PlanePlan q{};
+    q.src[0] = q.src[1] = -1;
+    int other = t->other;
+    if (have_cache) {
+        q.src[t->last_target - 1] = t->last_cur;
+        q.src[2 - t->last_target] = other;
+    } else {
+        other = -1;  // frames 0 and 1 clear every plane (raycast.h:150-154)
+    }
+    for (int c = 0; c < 3; ++c)
+        if ((!have_cache || c != t->last_cur) && c != other) {
+            q.cur = c;
+            break;
+        }
+    q.target = mode ? ((frame >> 4) % 2) + 1 : 2;
+    q.other_after = -1;
+    if (mode) q.other_after = (have_cache && q.target != t->last_target) ? t->last_cur : other;
+    q.fill_past = q.target == 1 ? q.cur : q.other_after;
+    q.clear = mode != 0;
+    return q;
+}
+
+void commit_planes(svo_target* t, const PlanePlan& q) {
+    t->last_cur = q.cur;
+    t->other = q.other_after;
+    t->last_target = q.target;
+}
+
+FrameParams make_params(const svo_target* t, const svo_view& v, int frame, const PlanePlan& q, bool have_cache) {
     FrameParams p{};
     p.ray = make_raycam(v);
     for (int i = 0; i < 3; ++i) {
@@ -370,8 +415,12 @@ FrameParams make_params(const svo_target* t, const svo_view& v, int frame, int c
         p.vz[i] = v.m[8 + i];
     }
     p.frame = frame;
-    p.cur = cur;
+    p.cur = q.cur;
     p.have_cache = have_cache ? 1 : 0;
+    p.src_plane[0] = q.src[0];
+    p.src_plane[1] = q.src[1];
+    p.clear_rejected = q.clear ? 1 : 0;
+    p.fill_past = q.fill_past;
     // raycast.h:363-366: tile (frame&7, (frame>>3)&3) of an 8x4 grid; the
     // NDRange of res/8 x res/4 work-items is rounded up to 16 (ocl.h:234-235).
     const int rx = t->res_x, ry = t->res_y;
@@ -804,8 +853,10 @@ svo_status svo_target_create(svo_context* ctx, int res_x, int res_y, svo_target*
     };
     A((void**)&t->B.col[0], N * 4);
     A((void**)&t->B.col[1], N * 4);
+    A((void**)&t->B.col[2], N * 4);
     A((void**)&t->B.xyz[0], N * 16);
     A((void**)&t->B.xyz[1], N * 16);
+    A((void**)&t->B.xyz[2], N * 16);
     A((void**)&t->B.disp, N * 4);
     A((void**)&t->B.bgrx, N * 4);
     A((void**)&t->B.keys, N * 8);
@@ -824,8 +875,10 @@ svo_status svo_target_create(svo_context* ctx, int res_x, int res_y, svo_target*
     SVO_CUDA(ctx, cudaMemsetAsync(t->B.keys, 0xff, N * 8, s));
     SVO_CUDA(ctx, cudaMemsetAsync(t->B.col[0], 0xff, N * 4, s));
     SVO_CUDA(ctx, cudaMemsetAsync(t->B.col[1], 0xff, N * 4, s));
+    SVO_CUDA(ctx, cudaMemsetAsync(t->B.col[2], 0xff, N * 4, s));
     SVO_CUDA(ctx, cudaMemsetAsync(t->B.xyz[0], 0, N * 16, s));
     SVO_CUDA(ctx, cudaMemsetAsync(t->B.xyz[1], 0, N * 16, s));
+    SVO_CUDA(ctx, cudaMemsetAsync(t->B.xyz[2], 0, N * 16, s));
     SVO_CUDA(ctx, cudaMemsetAsync(t->B.ids, 0, (N + 2 * t->tiles + 4) * 4, s));
     SVO_CUDA(ctx, cudaMemsetAsync(t->B.tile_mask, 0, (t->tiles + 1) * 8, s));
     SVO_CUDA(ctx, cudaMemsetAsync(t->B.counters, 0, 64, s));
@@ -844,7 +897,7 @@ svo_status svo_target_destroy(svo_target* t) {
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     for (auto& g : t->graphs) g.reset();
-    void* ptrs[] = {t->B.col[0], t->B.col[1], t->B.xyz[0], t->B.xyz[1], t->B.disp, t->B.bgrx, t->B.keys, t->B.ids,
+    void* ptrs[] = {t->B.col[0], t->B.col[1], t->B.col[2], t->B.xyz[0], t->B.xyz[1], t->B.xyz[2], t->B.disp, t->B.bgrx, t->B.keys, t->B.ids,
                     t->B.tile_mask, t->B.counters, t->d_params, t->full_col, t->full_xyzw, t->full_vox};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -959,16 +1012,16 @@ svo_status svo_warp_frame(svo_context* ctx, svo_target* t, const svo_view* view,
     if (view->fovx != 1.0f || view->fovy != 1.0f)
         return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "warp frames use fov 1 (raycast_proj has no fov term)");
     if (frame < 0) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "frame");
-    const int cur = (int)(t->frames & 1);
     const bool have_cache = frame >= 2 && t->have_prev;
-    FrameParams p = make_params(t, *view, frame, cur, have_cache);
+    const PlanePlan q = plan_planes(t, frame, have_cache, t->cache_mode);
+    FrameParams p = make_params(t, *view, frame, q, have_cache);
     st = run_frame(ctx, t, p, t->graphs[0], nullptr, 0.0f, [&] { return enqueue_warp_body(ctx, t); });
     if (st != SVO_OK) return st;
     if (t->profiling) {
         t->n_events = 7;
         t->last_mode = 1;
     }
-    t->last_cur = cur;
+    commit_planes(t, q);
     t->have_prev = true;
     t->prev_view = *view;
     t->have_prev_view = true;
@@ -988,16 +1041,17 @@ svo_status svo_warp_frame_learned(svo_context* ctx, svo_target* t, const svo_vie
     if (frame < 0) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "frame");
     if (!(threshold > 0.0f && threshold < 1.0f)) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "threshold in (0, 1)");
     const float logit = std::log(threshold / (1.0f - threshold));
-    const int cur = (int)(t->frames & 1);
     const bool have_cache = frame >= 2 && t->have_prev;
-    FrameParams p = make_params(t, *view, frame, cur, have_cache);
+    // learned frames keep one cache plane (the current plane of the last frame)
+    const PlanePlan q = plan_planes(t, frame, have_cache, 0);
+    FrameParams p = make_params(t, *view, frame, q, have_cache);
     st = run_frame(ctx, t, p, t->graphs[1], net, threshold, [&] { return enqueue_learned_body(ctx, t, net, logit); });
     if (st != SVO_OK) return st;
     if (t->profiling) {
         t->n_events = 5;
         t->last_mode = 3;
     }
-    t->last_cur = cur;
+    commit_planes(t, q);
     t->have_prev = true;
     t->prev_view = *view;
     t->have_prev_view = true;
@@ -1260,8 +1314,9 @@ static svo_status read_back(svo_target* t, void* host, const void* dev, size_t b
 svo_status svo_read_colour(svo_target* t, int plane, uint32_t* host) {
     if (!t) return SVO_ERR_INVALID_ARGUMENT;
     if (plane == 0) return read_back(t, host, t->B.disp, t->N * 4);
-    if (plane == 2) return read_back(t, host, t->B.col[t->last_cur], t->N * 4);
-    if (plane == 1) {
+    if (plane == 1 || plane == 2) {
+        const int phys = plane == t->last_target ? t->last_cur : t->other;
+        if (phys >= 0) return read_back(t, host, t->B.col[phys], t->N * 4);
         if (!host) return SVO_ERR_INVALID_ARGUMENT;
         for (size_t i = 0; i < t->N; ++i) host[i] = SVO_EMPTY_PIXEL;
         return SVO_OK;
@@ -1271,8 +1326,21 @@ svo_status svo_read_colour(svo_target* t, int plane, uint32_t* host) {
 
 svo_status svo_read_coords(svo_target* t, int plane, float* host) {
     if (!t) return SVO_ERR_INVALID_ARGUMENT;
-    if (plane == 0 || plane == 2) return read_back(t, host, t->B.xyz[t->last_cur], t->N * 16);
+    if (plane == 0) return read_back(t, host, t->B.xyz[t->last_cur], t->N * 16);
+    if (plane == 1 || plane == 2) {
+        const int phys = plane == t->last_target ? t->last_cur : t->other;
+        if (phys >= 0) return read_back(t, host, t->B.xyz[phys], t->N * 16);
+        if (!host) return SVO_ERR_INVALID_ARGUMENT;
+        for (size_t i = 0; i < 4 * t->N; ++i) host[i] = 0.0f;
+        return SVO_OK;
+    }
     return fail(t->ctx, SVO_ERR_INVALID_ARGUMENT, "plane");
+}
+
+svo_status svo_target_set_cache_mode(svo_target* t, int mode) {
+    if (!t || mode < 0 || mode > 1) return SVO_ERR_INVALID_ARGUMENT;
+    t->cache_mode = mode;
+    return SVO_OK;
 }
 
 svo_status svo_read_holes(svo_target* t, uint32_t* host, size_t cap_words, uint32_t* count) {

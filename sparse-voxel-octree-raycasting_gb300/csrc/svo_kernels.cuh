@@ -33,8 +33,11 @@ struct FrameParams {
     RayCam ray;                 // ray camera (rows of m^T)
     float vx[3], vy[3], vz[3];  // rows of m (raycast_proj's a_mx/a_my/a_mz)
     int frame;
-    int cur;         // which of the two colour/coordinate planes is current
-    int have_cache;  // the other plane holds the previous frame
+    int cur;            // physical plane (0..2) that receives this frame's plane 0
+    int have_cache;     // the source planes hold earlier frames
+    int src_plane[2];   // physical planes of the reference's cache planes 1 and 2, -1 = empty
+    int clear_rejected; // clear rejected source pixels in their cache plane (kernel.cl:549-562)
+    int fill_past;      // physical plane of reference plane 1 after the copy, -1 = empty
     int add_x, add_y, x_end, y_end;  // refresh tile rectangle (raycast.h:363-366)
     // previous frame's camera (the reconstruction net's motion feature)
     float prev_pos[3], prev_vx[3], prev_vy[3], prev_vz[3];
@@ -43,8 +46,8 @@ struct FrameParams {
 
 // Buffers of one render target.
 struct TargetBuffers {
-    uint32_t* col[2];   // current / cache colour planes (swap every frame)
-    float4* xyz[2];     // current / cache coordinate planes
+    uint32_t* col[3];   // colour planes: the current one and up to two caches
+    float4* xyz[3];     // coordinate planes, likewise
     uint32_t* disp;     // displayed colour plane (after the filter)
     uint32_t* bgrx;     // colourised output
     uint64_t* keys;     // per-pixel projection keys, kKeyEmpty between frames
@@ -75,8 +78,12 @@ struct FullBatch {
 
 // Plane selection without dynamic indexing of the by-value parameter struct
 // (which would force a local-memory copy of it).
-__device__ __forceinline__ uint32_t* plane_col(const TargetBuffers& B, int i) { return i ? B.col[1] : B.col[0]; }
-__device__ __forceinline__ float4* plane_xyz(const TargetBuffers& B, int i) { return i ? B.xyz[1] : B.xyz[0]; }
+__device__ __forceinline__ uint32_t* plane_col(const TargetBuffers& B, int i) {
+    return i == 0 ? B.col[0] : (i == 1 ? B.col[1] : B.col[2]);
+}
+__device__ __forceinline__ float4* plane_xyz(const TargetBuffers& B, int i) {
+    return i == 0 ? B.xyz[0] : (i == 1 ? B.xyz[1] : B.xyz[2]);
+}
 
 __global__ void k_set_params(FrameParams p, FrameParams* dst, uint32_t* counters) {
     *dst = p;
@@ -107,15 +114,16 @@ __device__ __forceinline__ float dot3(float ax, float ay, float az, const float*
     return __fadd_rn(__fadd_rn(__fmul_rn(ax, b[0]), __fmul_rn(ay, b[1])), __fmul_rn(az, b[2]));
 }
 
-// Scatter: every non-empty cache pixel proposes itself to the pixel it
-// reprojects to. Key = depth key (int(z*1000)<<8, unsigned) << 32 | source.
+// Scatter: every non-empty pixel of the two cache planes (reference planes 1
+// and 2, raycast.h:176-198) proposes itself to the pixel it reprojects to.
+// Key = (depth key int(z*1000)<<8 | cache plane bit) << 32 | source pixel:
+// the smallest key wins, i.e. the nearest depth key, then plane 1 before
+// plane 2, then the lowest source pixel -- the order in which the reference's
+// work-items run.
 __global__ void __launch_bounds__(256) k_project(const FrameParams* __restrict__ P, TargetBuffers B) {
     if (!P->have_cache) return;
     const int res_x = B.res_x, res_y = B.res_y;
     const uint32_t N = (uint32_t)res_x * (uint32_t)res_y;
-    const int cache = P->cur ^ 1;
-    const uint32_t* __restrict__ col = plane_col(B, cache);
-    const float4* __restrict__ xyz = plane_xyz(B, cache);
     const float px = P->ray.px, py = P->ray.py, pz = P->ray.pz;
     float vx[3], vy[3], vz[3];
     for (int i = 0; i < 3; ++i) {
@@ -125,20 +133,33 @@ __global__ void __launch_bounds__(256) k_project(const FrameParams* __restrict__
     }
     const float hx = (float)res_x / 2.0f, hy = (float)res_y / 2.0f;
     const float fry = (float)res_y;
-    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += gridDim.x * blockDim.x) {
-        const uint32_t c = __ldg(col + s);
-        if (c == kEmptyPixel) continue;
-        const float4 q = __ldg(xyz + s);
-        const float ax = __fsub_rn(q.x, px), ay = __fsub_rn(q.y, py), az = __fsub_rn(q.z, pz);
-        const float zz = dot3(ax, ay, az, vz);
-        if (zz < 0.05f) continue;  // (double)z < 0.05 <=> z < 0.05f for a binary32 z
-        const int sx = proj_coord(__fmul_rn(dot3(ax, ay, az, vx), fry), zz, hx);
-        const int sy = proj_coord(__fmul_rn(dot3(ax, ay, az, vy), fry), zz, hy);
-        if (sx >= res_x - 1 || sx < 0 || sy >= res_y - 1 || sy < 0) continue;
-        const uint32_t sz = (uint32_t)__float2int_rz(__fmul_rn(zz, 1000.0f)) << 8;
-        if (sz >= kEmptyPixel) continue;  // cannot beat the cleared value (kernel.cl:571)
-        const uint32_t t = (uint32_t)sy * (uint32_t)res_x + (uint32_t)sx;
-        atomicMin((unsigned long long*)(B.keys + t), (unsigned long long)(((uint64_t)sz << 32) | s));
+    const bool clear = P->clear_rejected != 0;
+    for (int r = 0; r < 2; ++r) {
+        const int phys = P->src_plane[r];
+        if (phys < 0) continue;
+        uint32_t* __restrict__ col = plane_col(B, phys);
+        const float4* __restrict__ xyz = plane_xyz(B, phys);
+        for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += gridDim.x * blockDim.x) {
+            const uint32_t c = col[s];
+            if (c == kEmptyPixel) continue;
+            const float4 q = __ldg(xyz + s);
+            const float ax = __fsub_rn(q.x, px), ay = __fsub_rn(q.y, py), az = __fsub_rn(q.z, pz);
+            const float zz = dot3(ax, ay, az, vz);
+            if (zz < 0.05f) {  // (double)z < 0.05 <=> z < 0.05f for a binary32 z
+                if (clear) col[s] = kEmptyPixel;
+                continue;
+            }
+            const int sx = proj_coord(__fmul_rn(dot3(ax, ay, az, vx), fry), zz, hx);
+            const int sy = proj_coord(__fmul_rn(dot3(ax, ay, az, vy), fry), zz, hy);
+            if (sx >= res_x - 1 || sx < 0 || sy >= res_y - 1 || sy < 0) {
+                if (clear) col[s] = kEmptyPixel;
+                continue;
+            }
+            const uint32_t sz = (uint32_t)__float2int_rz(__fmul_rn(zz, 1000.0f)) << 8;
+            if (sz >= kEmptyPixel) continue;  // cannot beat the cleared value (kernel.cl:571)
+            const uint32_t t = (uint32_t)sy * (uint32_t)res_x + (uint32_t)sx;
+            atomicMin((unsigned long long*)(B.keys + t), (unsigned long long)(((uint64_t)(sz | (uint32_t)r) << 32) | s));
+        }
     }
 }
 
@@ -163,10 +184,12 @@ __global__ void __launch_bounds__(256) k_resolve_gather(const FrameParams* __res
             if (key != kKeyEmpty) {
                 B.keys[t] = kKeyEmpty;
                 const uint32_t src = (uint32_t)key;
-                const float4 q = plane_xyz(B, cur ^ 1)[src];
+                const uint32_t hi = (uint32_t)(key >> 32);
+                const int phys = (hi & 1u) ? P->src_plane[1] : P->src_plane[0];
+                const float4 q = plane_xyz(B, phys)[src];
                 const float ax = __fsub_rn(q.x, P->ray.px), ay = __fsub_rn(q.y, P->ray.py),
                             az = __fsub_rn(q.z, P->ray.pz);
-                outc = (uint32_t)(key >> 32) + (plane_col(B, cur ^ 1)[src] & 255u);
+                outc = (hi & ~255u) + (plane_col(B, phys)[src] & 255u);
                 plane_xyz(B, cur)[t] = make_float4(q.x, q.y, q.z, dot3(ax, ay, az, P->vz));
             }
         }
@@ -386,10 +409,13 @@ __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FramePa
 // ----------------------------------------------- filter + colourise ----
 // raycast_fillhole2 (kernel.cl:404-470) reading the unfiltered current plane
 // and writing the displayed plane, fused with raycast_colorize.
-__device__ __forceinline__ uint32_t read_lin(const uint32_t* __restrict__ s, long long o, long long n) {
-    // The reference addresses plane 0 linearly; reads past its end land in the
-    // never-written plane 1, i.e. an empty pixel.
-    return (o >= 0 && o < n) ? __ldg(s + o) : kEmptyPixel;
+__device__ __forceinline__ uint32_t read_lin(const uint32_t* __restrict__ s, const uint32_t* __restrict__ next,
+                                             long long o, long long n) {
+    // The reference addresses plane 0 linearly; reads past its end land in
+    // plane 1: empty unless the alternating cache target writes it.
+    if (o >= 0 && o < n) return __ldg(s + o);
+    if (next && o >= n && o < 2 * n) return __ldg(next + (o - n));
+    return kEmptyPixel;
 }
 
 __global__ void __launch_bounds__(256) k_fill_colorize(const FrameParams* __restrict__ P, TargetBuffers B) {
@@ -398,6 +424,7 @@ __global__ void __launch_bounds__(256) k_fill_colorize(const FrameParams* __rest
     const int res_x = B.res_x, res_y = B.res_y;
     if (idx >= res_x || idy >= res_y) return;
     const uint32_t* __restrict__ s = plane_col(B, P->cur);
+    const uint32_t* __restrict__ next = P->fill_past >= 0 ? plane_col(B, P->fill_past) : nullptr;
     const long long n = (long long)res_x * res_y;
     const long long ofs = (long long)idy * res_x + idx;
     uint32_t col = __ldg(s + ofs);
@@ -414,13 +441,13 @@ __global__ void __launch_bounds__(256) k_fill_colorize(const FrameParams* __rest
             col = (uint32_t)((c3 & 3) + ((((c3 & 0xfc) + (c4 & 0xfc)) >> 1) & 0xfc));
         } else {
             for (int i = 0; i < 4; ++i) {
-                col = read_lin(s, ofs + (i & 1) + ((i >> 1) & 1) * res_x, n);
+                col = read_lin(s, next, ofs + (i & 1) + ((i >> 1) & 1) * res_x, n);
                 if (col != kEmptyPixel) break;
             }
             if (col == kEmptyPixel) {
                 for (int i = -2; i < 3 && col == kEmptyPixel; ++i)
                     for (int j = -2; j < 3; ++j) {
-                        col = read_lin(s, ofs + i + (long long)j * res_x, n);
+                        col = read_lin(s, next, ofs + i + (long long)j * res_x, n);
                         if (col != kEmptyPixel) break;
                     }
             }

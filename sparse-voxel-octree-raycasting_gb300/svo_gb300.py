@@ -44,7 +44,7 @@ EXPORTS = [
     "svo_raycast_full_noalloc", "svo_rle4_voxels", "svo_rle4_build", "svo_write_bmp",
     "svo_warp_frame_learned", "svo_read_requested", "svo_target_set_feature_tap", "svo_net_create",
     "svo_net_destroy", "svo_net_init", "svo_net_set_params", "svo_net_get_params", "svo_net_get_grads",
-    "svo_net_forward", "svo_net_infer", "svo_net_backward", "svo_net_adam",
+    "svo_net_forward", "svo_net_infer", "svo_net_backward", "svo_net_adam", "svo_target_set_cache_mode",
 ]
 
 NET_PARAMS = 6388
@@ -159,6 +159,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "svo_warp_frame_learned": (i, [_P, _P, ctypes.POINTER(View), i, _P, ctypes.c_float]),
         "svo_read_requested": (i, [_P, ctypes.POINTER(u32)]),
         "svo_target_set_feature_tap": (i, [_P, _P]),
+        "svo_target_set_cache_mode": (i, [_P, i]),
         "svo_net_create": (i, [_P, ctypes.POINTER(_P)]),
         "svo_net_destroy": (i, [_P]),
         "svo_net_init": (i, [_P, ctypes.c_uint64]),
@@ -456,6 +457,10 @@ class Target:
         out = np.empty(self.n, np.uint64)
         _check(self._lib.svo_read_voxels(self._h, _ptr(out)), self.ctx)
         return out
+
+    def set_cache_mode(self, mode: int) -> None:
+        """0: the reference's copy target 2; 1: the alternating target ((frame>>4)%2)+1."""
+        _check(self._lib.svo_target_set_cache_mode(self._h, mode), self.ctx)
 
     def set_feature_tap(self, d_features: int | None) -> None:
         """Device buffer (8 x res_y x res_x FP32) receiving the net's input

@@ -64,3 +64,29 @@ def test_warp_frames_bit_exact(svo, orc, scene, gpu_ctx, depth, shell, kind, W, 
         want = warp.back()[2][ne]
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), f"frame {f}: coordinate buffer"
     tgt.close()
+
+
+@pytest.mark.parametrize("depth,kind,W,H,frames", [(9, 2, 160, 96, 40), (8, 1, 128, 64, 36)])
+def test_warp_frames_alternating_cache_bit_exact(svo, orc, scene, gpu_ctx, depth, kind, W, H, frames):
+    # raycast.h:395's commented-out copy target ((frame>>4)%2)+1: both cache
+    # planes live, rejected sources cleared in the plane that is kept.
+    octree = scene(depth, 41, True)
+    gpu_ctx.upload(octree)
+    tgt = gpu_ctx.target(W, H)
+    tgt.set_cache_mode(1)
+    warp = orc.Warp(depth, W, H)
+    for f in range(frames):
+        v = svo.camera_path(kind, depth, f, W, H)
+        gpu_ctx.warp_frame(tgt, v, f)
+        warp.frame(octree.words, octree.root, v.pos_array, v.m_array, f, cache_mode=1)
+        gpu_ctx.synchronize()
+        screen, back = warp.screen(), warp.back()
+        assert np.array_equal(tgt.holes()[0], warp.ids()), f"frame {f}: hole id buffer"
+        for plane in (0, 1, 2):
+            assert np.array_equal(tgt.colour(plane), screen[plane]), f"frame {f}: plane {plane}"
+        for plane in (1, 2):
+            ne = screen[plane] != svo.EMPTY_PIXEL
+            assert np.array_equal(tgt.coords(plane)[ne][:, :3].view(np.uint32),
+                                  back[plane][ne][:, :3].view(np.uint32)), f"frame {f}: coordinates {plane}"
+        assert np.array_equal(tgt.bgrx(), warp.tex()), f"frame {f}: BGRX"
+    tgt.close()
