@@ -155,6 +155,12 @@ svo_status svo_warp_frame(svo_context* ctx, svo_target* t, const svo_view* view,
  * cleared in their cache plane (kernel/kernel.cl:549-562). Learned frames
  * always use one cache plane. */
 svo_status svo_target_set_cache_mode(svo_target* t, int mode);
+/* The raycast_fine pass (kernel/kernel.cl:696-843), launched as the block the
+ * reference ships disabled at src/raycast.h:235-261: between reprojection and
+ * the hole gather, one ray per 2x2 block of a screen quadrant that moves every
+ * frame -- the block's first empty pixel, else a frame-dependent one.
+ * Requires res_x and res_y multiples of 4. Plain warp frames only. */
+svo_status svo_target_set_coarse_refresh(svo_target* t, int enable);
 
 /* Capture the warp frame of this target as a CUDA graph on first use and
  * replay it on later calls (the per-frame parameters are the arguments of

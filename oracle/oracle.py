@@ -169,7 +169,10 @@ class Warp:
         if not self._h:
             raise ValueError("warp state: resolution must be at least 16x16")
 
-    def frame(self, words, root, pos, m, frame: int, threads: int = 0, cache_mode: int = 0) -> None:
+    def frame(self, words, root, pos, m, frame: int, threads: int = 0, cache_mode: int = 0,
+              coarse: bool = False) -> None:
+        """cache_mode 1: alternating copy target; coarse: the raycast_fine pass."""
+        cache_mode = (cache_mode & 1) | (2 if coarse else 0)
         words = np.ascontiguousarray(words, np.uint32)
         pos = np.ascontiguousarray(pos, np.float32)
         m = np.ascontiguousarray(m, np.float32)

@@ -668,9 +668,44 @@ void* orc_warp_create(int res_x, int res_y) {
 }
 void orc_warp_free(void* h) { delete static_cast<Warp*>(h); }
 
-// One raycast_draw (raycast.h:147-441) minus the GL display. cache_mode 0:
-// the shipped copy target 2 (raycast.h:395); 1: the commented-out
-// alternating target ((frame>>4)%2)+1.
+// raycast_fine (kernel.cl:696-843) as raycast.h:235-261 launches it (a
+// block the reference ships disabled): work-items over (res/4 rounded up to
+// 16)^2, each owning the 2x2 block at (add + 2*id); it traces the block's
+// first empty pixel (order (0,0),(1,0),(0,1),(1,1)), or when none is empty
+// the pixel ((frame>>2)&1, (frame>>3)&1) of the block. The quadrant origin
+// moves every frame: add = (res/2) * ((frame, frame>>1) & 1). Needs res_x
+// and res_y multiples of 4, so that no block crosses the frame edge.
+void coarse_refresh(Warp& w, const Tracer& tr, const View& v, int frame, uint64_t& rays, uint64_t& child,
+                    uint64_t& col, uint64_t& bnd) {
+    const int res_x = w.res_x, res_y = w.res_y;
+    const int add_x = (res_x / 2) * (frame & 1), add_y = (res_y / 2) * ((frame >> 1) & 1);
+    const int gx = (res_x / 4 + 15) / 16 * 16, gy = (res_y / 4 + 15) / 16 * 16;
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : rays, child, col, bnd)
+    for (int j = 0; j < gy; ++j)
+        for (int i = 0; i < gx; ++i) {
+            const int bx = 2 * i + add_x, by = 2 * j + add_y;
+            if (bx >= res_x || by >= res_y) continue;
+            int x = bx + ((frame >> 2) & 1), y = by + ((frame >> 3) & 1);
+            for (int k = 0; k < 4; ++k) {
+                if (w.screen[(size_t)(by + (k >> 1)) * res_x + bx + (k & 1)] == kEmpty) {
+                    x = bx + (k & 1);
+                    y = by + (k >> 1);
+                    break;
+                }
+            }
+            Ray r = tr.trace(v, x, y, res_x, res_y, 1.0f, 1.0f);
+            store_ray(w, (size_t)y * res_x + x, r);
+            ++rays;
+            child += r.child_fetches;
+            col += r.colour_fetches;
+            bnd += r.boundary;
+        }
+}
+
+// One raycast_draw (raycast.h:147-441) minus the GL display. options bit 0:
+// the commented-out alternating copy target ((frame>>4)%2)+1 instead of the
+// shipped target 2 (raycast.h:395); bit 1: the disabled raycast_fine pass
+// (raycast.h:235-261) between reprojection and the hole gather.
 int orc_warp_frame(void* h, int depth, const uint32_t* words, size_t n_words, uint32_t root, const float* pos4,
                    const float* m16, int frame, int threads, int cache_mode) {
     Warp& w = *static_cast<Warp*>(h);
@@ -684,14 +719,17 @@ int orc_warp_frame(void* h, int depth, const uint32_t* words, size_t n_words, ui
     // raycast.h:150-157
     if (frame < 2) std::fill(w.screen.begin(), w.screen.end(), kEmpty);
     std::fill(w.screen.begin(), w.screen.begin() + N, kEmpty);
+    const bool coarse = (cache_mode & 2) != 0;
+    if (coarse && (res_x % 4 || res_y % 4)) return -2;
     // raycast.h:176-198: planes 1 then 2 into plane 0
     proj_plane(w, v, 1);
     proj_plane(w, v, 2);
     proj_resolve(w, v);
+    uint64_t rays = 0, child = 0, col = 0, bnd = 0;
+    if (coarse) coarse_refresh(w, tr, v, frame, rays, child, col, bnd);
     // raycast.h:263-315
     gather_holes(w);
     // raycast.h:330-387
-    uint64_t rays = 0, child = 0, col = 0, bnd = 0;
     const size_t tiles = w.tiles;
     const int add_x = (res_x / 8) * (frame & 7), add_y = (res_y / 4) * ((frame >> 3) & 3);
     auto round16 = [](int g) { return (g + 15) / 16 * 16; };
@@ -723,7 +761,7 @@ int orc_warp_frame(void* h, int depth, const uint32_t* words, size_t n_words, ui
     w.colour_fetches = col;
     w.boundary_rays = bnd;
     // raycast.h:394-405: copy plane 0 to the cache target plane
-    const int target = cache_mode ? ((frame >> 4) % 2) + 1 : 2;
+    const int target = (cache_mode & 1) ? ((frame >> 4) % 2) + 1 : 2;
     std::memcpy(w.screen.data() + (size_t)target * N, w.screen.data(), N * 4);
     std::memcpy(w.back.data() + (size_t)target * N * 4, w.back.data(), N * 16);
     std::memcpy(w.prefill.data(), w.screen.data(), N * 4);

@@ -60,6 +60,7 @@ struct FrameGraph {
     const void* net = nullptr;
     float threshold = 0.0f;
     float* tap = nullptr;
+    bool coarse = false;
     void reset() {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
@@ -84,6 +85,7 @@ struct svo_target {
     // plane 0 (reference plane `last_target`), the other cache plane (the
     // reference's plane 3 - last_target, -1 while it is empty).
     int cache_mode = 0;  // 0: copy target 2 (raycast.h:395); 1: ((frame>>4)%2)+1
+    bool coarse = false;  // the raycast_fine pass (raycast.h:235-261)
     int last_cur = 0;
     int other = -1;
     int last_target = 2;
@@ -277,12 +279,13 @@ struct TraceLaunch {
 
 // Trace kernels: full raycast, warp-frame holes + refresh tile, and the same
 // for learned frames (which also write the traced pixels' BGRX).
-enum TraceKind { kTraceFull = 0, kTraceWarp = 1, kTraceWarpBgrx = 2 };
+enum TraceKind { kTraceFull = 0, kTraceWarp = 1, kTraceWarpBgrx = 2, kTraceCoarse = 3 };
 
 template <int DEPTH, int BLOCK>
 const void* trace_fn(int kind) {
     if (kind == kTraceWarp) return (const void*)k_trace_warp<DEPTH, BLOCK, false>;
     if (kind == kTraceWarpBgrx) return (const void*)k_trace_warp<DEPTH, BLOCK, true>;
+    if (kind == kTraceCoarse) return (const void*)k_trace_coarse<DEPTH, BLOCK>;
     return (const void*)k_trace_full<DEPTH, BLOCK, true>;
 }
 
@@ -351,9 +354,9 @@ svo_status launch_trace_full(svo_context* ctx, FullBatch* d_batch) {
     return launch_trace(ctx, L, args);
 }
 
-svo_status launch_trace_warp(svo_context* ctx, svo_target* t, bool bgrx = false) {
+svo_status launch_trace_warp(svo_context* ctx, svo_target* t, int kind = kTraceWarp) {
     TraceLaunch L;
-    svo_status st = plan_trace(ctx, bgrx ? kTraceWarpBgrx : kTraceWarp, L);
+    svo_status st = plan_trace(ctx, kind, L);
     if (st != SVO_OK) return st;
     void* args[] = {&L.o, &t->d_params, &t->B, &ctx->d_fault};
     return launch_trace(ctx, L, args);
@@ -429,6 +432,8 @@ FrameParams make_params(const svo_target* t, const svo_view& v, int frame, const
     const int gx = (rx / 8 + 15) / 16 * 16, gy = (ry / 4 + 15) / 16 * 16;
     p.x_end = std::min(rx, p.add_x + gx);
     p.y_end = std::min(ry, p.add_y + gy);
+    p.coarse_x = (rx / 2) * (frame & 1);
+    p.coarse_y = (ry / 2) * ((frame >> 1) & 1);
     p.have_prev_view = t->have_prev_view ? 1 : 0;
     for (int i = 0; i < 3; ++i) {
         p.prev_pos[i] = t->prev_view.pos[i];
@@ -453,6 +458,12 @@ svo_status enqueue_warp_body(svo_context* ctx, svo_target* t) {
     record(t, 1);
     k_resolve_gather<<<dim3((res_x + 15) / 16, (res_y + 15) / 16), 256, 0, s>>>(t->d_params, t->B);
     SVO_LAUNCHED(ctx);
+    if (t->coarse) {
+        svo_status cs = launch_trace_warp(ctx, t, kTraceCoarse);
+        if (cs != SVO_OK) return cs;
+        k_hole_mask<<<dim3((res_x + 15) / 16, (res_y + 15) / 16), 256, 0, s>>>(t->d_params, t->B);
+        SVO_LAUNCHED(ctx);
+    }
     if (t->feature_tap) {
         k_net_features<<<dim3((res_x + 31) / 32, (res_y + 7) / 8), 256, 0, s>>>(t->d_params, t->B, t->feature_tap);
         SVO_LAUNCHED(ctx);
@@ -523,7 +534,7 @@ svo_status enqueue_learned_body(svo_context* ctx, svo_target* t, const svo_net* 
     svo_status st = launch_net_infer(ctx, net, true, A);
     if (st != SVO_OK) return st;
     record(t, 3);
-    st = launch_trace_warp(ctx, t, true);
+    st = launch_trace_warp(ctx, t, kTraceWarpBgrx);
     if (st != SVO_OK) return st;
     record(t, 4);
     return SVO_OK;
@@ -540,7 +551,8 @@ svo_status run_frame(svo_context* ctx, svo_target* t, const FrameParams& p, Fram
         SVO_LAUNCHED(ctx);
         return body();
     }
-    if (!g.exec || g.profiled != t->profiling || g.net != net || g.threshold != threshold || g.tap != t->feature_tap) {
+    if (!g.exec || g.profiled != t->profiling || g.net != net || g.threshold != threshold || g.tap != t->feature_tap ||
+        g.coarse != t->coarse) {
         g.reset();
         const uint64_t l0 = ctx->launches;
         SVO_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
@@ -577,6 +589,7 @@ svo_status run_frame(svo_context* ctx, svo_target* t, const FrameParams& p, Fram
         g.net = net;
         g.threshold = threshold;
         g.tap = t->feature_tap;
+        g.coarse = t->coarse;
     }
     cudaKernelNodeParams kp;
     SVO_CUDA(ctx, cudaGraphKernelNodeGetParams(g.params_node, &kp));
@@ -1340,6 +1353,14 @@ svo_status svo_read_coords(svo_target* t, int plane, float* host) {
 svo_status svo_target_set_cache_mode(svo_target* t, int mode) {
     if (!t || mode < 0 || mode > 1) return SVO_ERR_INVALID_ARGUMENT;
     t->cache_mode = mode;
+    return SVO_OK;
+}
+
+svo_status svo_target_set_coarse_refresh(svo_target* t, int enable) {
+    if (!t) return SVO_ERR_INVALID_ARGUMENT;
+    if (enable && (t->res_x % 4 || t->res_y % 4))
+        return fail(t->ctx, SVO_ERR_NOT_SUPPORTED, "the coarse refresh pass needs res_x and res_y multiples of 4");
+    t->coarse = enable != 0;
     return SVO_OK;
 }
 

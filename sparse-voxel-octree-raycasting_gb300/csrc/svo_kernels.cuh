@@ -39,6 +39,7 @@ struct FrameParams {
     int clear_rejected; // clear rejected source pixels in their cache plane (kernel.cl:549-562)
     int fill_past;      // physical plane of reference plane 1 after the copy, -1 = empty
     int add_x, add_y, x_end, y_end;  // refresh tile rectangle (raycast.h:363-366)
+    int coarse_x, coarse_y;          // quadrant origin of the raycast_fine pass (raycast.h:240-241)
     // previous frame's camera (the reconstruction net's motion feature)
     float prev_pos[3], prev_vx[3], prev_vy[3], prev_vz[3];
     int have_prev_view;
@@ -53,7 +54,7 @@ struct TargetBuffers {
     uint64_t* keys;     // per-pixel projection keys, kKeyEmpty between frames
     uint32_t* ids;      // hole id buffer in the reference layout
     uint64_t* tile_mask;  // per 16x16 tile, bit j*8+i = 2x2 block (i,j) empty
-    uint32_t* counters;   // [0] trace work counter, [1] hole entries
+    uint32_t* counters;   // [0] trace work counter, [1] hole entries, [2] coarse-pass work counter
     int res_x, res_y;
     int tiles_x, tiles_y;  // whole 16x16 tiles (res/16)
 };
@@ -89,6 +90,7 @@ __global__ void k_set_params(FrameParams p, FrameParams* dst, uint32_t* counters
     *dst = p;
     counters[0] = 0;
     counters[1] = 0;
+    counters[2] = 0;
 }
 
 __global__ void k_reset_counter(uint32_t* counter) { *counter = 0; }
@@ -163,6 +165,26 @@ __global__ void __launch_bounds__(256) k_project(const FrameParams* __restrict__
     }
 }
 
+// raycast_counthole's test (HOLE_PIXEL_THRESHOLD = 4, kernel.cl:262-271) for
+// the 16x16 tile of this block: bit j*8+i set when 2x2 block (i,j) is empty.
+// Only whole tiles are counted (kernel.cl:243-244). Every thread calls it.
+__device__ __forceinline__ void tile_mask_store(const TargetBuffers& B, uint8_t (*empty)[17], uint32_t* halves) {
+    __syncthreads();
+    if (blockIdx.x >= (unsigned)B.tiles_x || blockIdx.y >= (unsigned)B.tiles_y) return;  // block-uniform
+    bool hole = false;
+    if (threadIdx.x < 64) {
+        const int i = threadIdx.x & 7, j = threadIdx.x >> 3;
+        hole = empty[2 * j][2 * i] && empty[2 * j][2 * i + 1] && empty[2 * j + 1][2 * i] && empty[2 * j + 1][2 * i + 1];
+    }
+    const uint32_t bal = __ballot_sync(0xffffffffu, hole);
+    if (threadIdx.x == 0 || threadIdx.x == 32) halves[threadIdx.x >> 5] = bal;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const uint32_t tile = blockIdx.y * B.tiles_x + blockIdx.x;
+        B.tile_mask[tile] = (uint64_t)halves[0] | ((uint64_t)halves[1] << 32);
+    }
+}
+
 // Gather + clear + hole count, one 16x16 tile per block: each target pixel
 // takes its winning source (or becomes empty), then the block marks the 2x2
 // blocks whose four pixels are empty (raycast_counthole's test with
@@ -197,20 +219,20 @@ __global__ void __launch_bounds__(256) k_resolve_gather(const FrameParams* __res
         is_empty = outc == kEmptyPixel;
     }
     empty[ty][tx] = is_empty;
-    __syncthreads();
-    if (blockIdx.x >= (unsigned)B.tiles_x || blockIdx.y >= (unsigned)B.tiles_y) return;  // block-uniform
-    bool hole = false;
-    if (threadIdx.x < 64) {
-        const int i = threadIdx.x & 7, j = threadIdx.x >> 3;
-        hole = empty[2 * j][2 * i] && empty[2 * j][2 * i + 1] && empty[2 * j + 1][2 * i] && empty[2 * j + 1][2 * i + 1];
-    }
-    const uint32_t bal = __ballot_sync(0xffffffffu, hole);
-    if (threadIdx.x == 0 || threadIdx.x == 32) halves[threadIdx.x >> 5] = bal;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const uint32_t tile = blockIdx.y * B.tiles_x + blockIdx.x;
-        B.tile_mask[tile] = (uint64_t)halves[0] | ((uint64_t)halves[1] << 32);
-    }
+    tile_mask_store(B, empty, halves);
+}
+
+// The hole count of k_resolve_gather alone, for frames whose plane 0 changed
+// after the gather (the raycast_fine pass).
+__global__ void __launch_bounds__(256) k_hole_mask(const FrameParams* __restrict__ P, TargetBuffers B) {
+    __shared__ uint8_t empty[16][17];
+    __shared__ uint32_t halves[2];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int x = blockIdx.x * 16 + tx, y = blockIdx.y * 16 + ty;
+    bool is_empty = true;
+    if (x < B.res_x && y < B.res_y) is_empty = plane_col(B, P->cur)[(size_t)y * B.res_x + x] == kEmptyPixel;
+    empty[ty][tx] = is_empty;
+    tile_mask_store(B, empty, halves);
 }
 
 // raycast_sumids (kernel.cl:276-296) without the single-thread loop or the
@@ -400,6 +422,56 @@ __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FramePa
             col[ofs] = r.colour;
             xyz[ofs] = make_float4(r.hx, r.hy, r.hz, r.dist);
             if (kBgrx) B.bgrx[ofs] = colorize(r.colour);
+        }
+    }
+    if (o_in.n_smem > 0 && !staged) stage_drain(&mbar);
+    if (fault) atomicOr(fault_out, fault);
+}
+
+// raycast_fine (kernel.cl:696-843) as raycast.h:235-261 would launch it
+// (the reference ships the call disabled): work-items over (res/4 rounded up
+// to 16) in x and y, each owning the 2x2 block at (coarse + 2*id) and
+// tracing its first empty pixel (order (0,0),(1,0),(0,1),(1,1)), else pixel
+// ((frame>>2)&1, (frame>>3)&1) of the block. Runs between the gather and the
+// hole count. Packets: 8x4 work-items. res_x and res_y are multiples of 4
+// (checked by the host), so no block crosses the frame edge.
+template <int DEPTH, int BLOCK>
+__global__ void __launch_bounds__(BLOCK) k_trace_coarse(Octree o_in, const FrameParams* __restrict__ P,
+                                                      TargetBuffers B, uint32_t* fault_out) {
+    __shared__ uint64_t mbar;
+    const int lane = threadIdx.x & 31;
+    uint32_t* stk = svo_dsmem + threadIdx.x;
+    uint32_t fault = 0;
+    bool staged;
+    const Octree o = stage_octree<DEPTH, BLOCK>(o_in, &mbar, fault, staged);
+    const int res_x = B.res_x, res_y = B.res_y;
+    const int gx = (res_x / 4 + 15) / 16 * 16, gy = (res_y / 4 + 15) / 16 * 16;
+    const uint32_t ppx = (uint32_t)gx / 8u, ppy = (uint32_t)gy / 4u;
+    const uint32_t total = ppx * ppy;
+    const int ax = P->coarse_x, ay = P->coarse_y, frame = P->frame;
+    const RayCam cam = P->ray;
+    float4* __restrict__ xyz = plane_xyz(B, P->cur);
+    uint32_t* __restrict__ col = plane_col(B, P->cur);
+    for (;;) {
+        uint32_t p = 0;
+        if (lane == 0) p = atomicAdd(B.counters + 2, 1u);
+        p = __shfl_sync(0xffffffffu, p, 0);
+        if (p >= total) break;
+        const int bx = ax + 2 * ((int)(p % ppx) * 8 + (lane & 7));
+        const int by = ay + 2 * ((int)(p / ppx) * 4 + (lane >> 3));
+        if (bx < res_x && by < res_y) {
+            int x = bx + ((frame >> 2) & 1), y = by + ((frame >> 3) & 1);
+            for (int k = 0; k < 4; ++k) {
+                if (col[(size_t)(by + (k >> 1)) * res_x + bx + (k & 1)] == kEmptyPixel) {
+                    x = bx + (k & 1);
+                    y = by + (k >> 1);
+                    break;
+                }
+            }
+            const RayResult r = trace_ray<DEPTH, false>(o, cam, x, y, res_x, res_y, stk, BLOCK, fault);
+            const size_t ofs = (size_t)y * res_x + x;
+            col[ofs] = r.colour;
+            xyz[ofs] = make_float4(r.hx, r.hy, r.hz, r.dist);
         }
     }
     if (o_in.n_smem > 0 && !staged) stage_drain(&mbar);

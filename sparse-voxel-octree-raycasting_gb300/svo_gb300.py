@@ -45,6 +45,7 @@ EXPORTS = [
     "svo_warp_frame_learned", "svo_read_requested", "svo_target_set_feature_tap", "svo_net_create",
     "svo_net_destroy", "svo_net_init", "svo_net_set_params", "svo_net_get_params", "svo_net_get_grads",
     "svo_net_forward", "svo_net_infer", "svo_net_backward", "svo_net_adam", "svo_target_set_cache_mode",
+    "svo_target_set_coarse_refresh",
 ]
 
 NET_PARAMS = 6388
@@ -160,6 +161,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "svo_read_requested": (i, [_P, ctypes.POINTER(u32)]),
         "svo_target_set_feature_tap": (i, [_P, _P]),
         "svo_target_set_cache_mode": (i, [_P, i]),
+        "svo_target_set_coarse_refresh": (i, [_P, i]),
         "svo_net_create": (i, [_P, ctypes.POINTER(_P)]),
         "svo_net_destroy": (i, [_P]),
         "svo_net_init": (i, [_P, ctypes.c_uint64]),
@@ -461,6 +463,10 @@ class Target:
     def set_cache_mode(self, mode: int) -> None:
         """0: the reference's copy target 2; 1: the alternating target ((frame>>4)%2)+1."""
         _check(self._lib.svo_target_set_cache_mode(self._h, mode), self.ctx)
+
+    def set_coarse_refresh(self, enable: bool = True) -> None:
+        """The raycast_fine pass: one ray per 2x2 block of a moving quadrant, before the hole gather."""
+        _check(self._lib.svo_target_set_coarse_refresh(self._h, 1 if enable else 0), self.ctx)
 
     def set_feature_tap(self, d_features: int | None) -> None:
         """Device buffer (8 x res_y x res_x FP32) receiving the net's input

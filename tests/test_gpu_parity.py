@@ -90,3 +90,34 @@ def test_warp_frames_alternating_cache_bit_exact(svo, orc, scene, gpu_ctx, depth
                                   back[plane][ne][:, :3].view(np.uint32)), f"frame {f}: coordinates {plane}"
         assert np.array_equal(tgt.bgrx(), warp.tex()), f"frame {f}: BGRX"
     tgt.close()
+
+
+@pytest.mark.parametrize("cache_mode,graph", [(0, False), (1, True)])
+def test_warp_frames_coarse_refresh_bit_exact(svo, orc, scene, gpu_ctx, cache_mode, graph):
+    # raycast.h:235-261's disabled raycast_fine pass between reprojection and
+    # the hole gather
+    depth, W, H = 9, 160, 96
+    octree = scene(depth, 43, True)
+    gpu_ctx.upload(octree)
+    tgt = gpu_ctx.target(W, H)
+    tgt.set_cache_mode(cache_mode)
+    tgt.set_coarse_refresh(True)
+    tgt.use_graph(graph)
+    warp = orc.Warp(depth, W, H)
+    for f in range(20):
+        v = svo.camera_path(2, depth, f, W, H)
+        gpu_ctx.warp_frame(tgt, v, f)
+        warp.frame(octree.words, octree.root, v.pos_array, v.m_array, f, cache_mode=cache_mode, coarse=True)
+        gpu_ctx.synchronize()
+        screen, back = warp.screen(), warp.back()
+        assert np.array_equal(tgt.holes()[0], warp.ids()), f"frame {f}: hole id buffer"
+        for plane in (0, 1, 2):
+            assert np.array_equal(tgt.colour(plane), screen[plane]), f"frame {f}: plane {plane}"
+        ne = screen[2] != svo.EMPTY_PIXEL
+        assert np.array_equal(tgt.coords(2)[ne].view(np.uint32), back[2][ne].view(np.uint32)), f"frame {f}"
+        assert np.array_equal(tgt.bgrx(), warp.tex()), f"frame {f}: BGRX"
+    tgt.close()
+    t2 = gpu_ctx.target(30, 20)
+    with pytest.raises(svo.SvoError):
+        t2.set_coarse_refresh(True)
+    t2.close()

@@ -184,3 +184,38 @@ def test_oracle_alternating_cache_target_matches_reference(svo, orc):
         mine.frame(words, root, v.pos_array, v.m_array, f, cache_mode=1)
         assert np.array_equal(ref.screen(), mine.screen()), f"frame {f}"
         assert np.array_equal(ref.ids(), mine.ids()) and np.array_equal(ref.tex(), mine.tex())
+
+
+@needs_ref
+@pytest.mark.parametrize("cache_mode", [0, 1])
+def test_oracle_coarse_refresh_matches_reference(svo, orc, cache_mode):
+    # raycast.h:235-261's disabled raycast_fine pass (one ray per 2x2 block of
+    # a quadrant, before the hole gather), alone and with the alternating target.
+    depth, W, H = 9, 96, 64
+    x, y, z, c = svo.terrain_voxels(43, depth, True)
+    words, root = orc.build_octree(depth, x, y, z, c)
+    ref = orc.Warp(depth, W, H, which="reference")
+    mine = orc.Warp(depth, W, H)
+    for f in range(20):
+        v = svo.camera_path(2, depth, f, W, H)
+        ref.frame(words, root, v.pos_array, v.m_array, f, cache_mode=cache_mode, coarse=True)
+        mine.frame(words, root, v.pos_array, v.m_array, f, cache_mode=cache_mode, coarse=True)
+        rs, ms = ref.screen(), mine.screen()
+        assert np.array_equal(rs, ms), f"frame {f}"
+        assert np.array_equal(ref.ids(), mine.ids()) and np.array_equal(ref.tex(), mine.tex()), f"frame {f}"
+        ne = rs[2] != svo.EMPTY_PIXEL
+        assert np.array_equal(np.ascontiguousarray(ref.back()[2][ne][:, :3]).view(np.uint32),
+                              np.ascontiguousarray(mine.back()[2][ne][:, :3]).view(np.uint32)), f"frame {f}"
+
+
+def test_oracle_coarse_refresh_fills_holes(svo, orc):
+    # the coarse pass leaves fewer whole 2x2 holes for the hole gather
+    depth, W, H = 8, 64, 48
+    x, y, z, c = svo.terrain_voxels(31, depth, True)
+    words, root = orc.build_octree(depth, x, y, z, c)
+    a, b = orc.Warp(depth, W, H), orc.Warp(depth, W, H)
+    for f in range(12):
+        v = svo.camera_path(2, depth, f, W, H)
+        a.frame(words, root, v.pos_array, v.m_array, f)
+        b.frame(words, root, v.pos_array, v.m_array, f, coarse=True)
+    assert b.hole_count() <= a.hole_count()
