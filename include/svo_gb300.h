@@ -95,6 +95,21 @@ svo_status svo_context_set_option(svo_context* ctx, int option, int64_t value);
 
 /* ------------------------------------------------------------ octree -- */
 
+/* The octree builder on the GPU (no reference counterpart on the device; it
+ * produces the words of set_voxel + convert_tree_blocks,
+ * src/octree/octree.h:32-293, and of svo_builder_finish): voxel arrays in
+ * device memory, array order = insertion order (a voxel inserted twice keeps
+ * the last colour, inner nodes the colour of the first voxel through them).
+ * The result becomes the context's octree. initial_words as in
+ * svo_builder_finish (0: SVO_DEFAULT_INITIAL_WORDS); the normal nodes must fit
+ * into it. Synchronises the context stream. */
+svo_status svo_octree_build(svo_context* ctx, const uint32_t* d_x, const uint32_t* d_y, const uint32_t* d_z,
+                            const uint32_t* d_rgba, size_t n, int depth, size_t initial_words);
+/* Size, root word and depth of the context's octree. */
+svo_status svo_octree_info(const svo_context* ctx, size_t* n_words, uint32_t* root_word, int* depth);
+/* Copies the context's octree words (n_words must equal its size) to host. */
+svo_status svo_octree_download(svo_context* ctx, uint32_t* host, size_t n_words);
+
 /* Replaces ocl_malloc(size, &octree_array_compact[0]) of src/raycast.h:68
  * together with the octree_root_normal global (src/octree/octree.h:25).
  * Validates every node word reachable from root_word against n_words

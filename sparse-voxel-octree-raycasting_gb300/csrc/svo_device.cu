@@ -20,6 +20,7 @@
 #include "../../include/svo_gb300.h"
 #include "svo_kernels.cuh"
 #include "svo_net.cuh"
+#include "svo_build.cuh"
 
 using namespace svo;
 
@@ -687,6 +688,70 @@ svo_status net_weight_grad(svo_net* net, const float* a, const float* g, int W, 
     return SVO_OK;
 }
 
+// ------------------------------------------------------- GPU builder --
+// Device allocations freed when the builder returns.
+struct DevScratch {
+    std::vector<void*> ptrs;
+    ~DevScratch() {
+        for (void* p : ptrs) cudaFree(p);
+    }
+    template <class T>
+    cudaError_t get(T** p, size_t count) {
+        void* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+        if (e == cudaSuccess) ptrs.push_back(q);
+        *p = static_cast<T*>(q);
+        return e;
+    }
+};
+
+inline unsigned grid_for(size_t n, int threads, int sm_count) {
+    return (unsigned)std::max<size_t>(1, std::min<size_t>((n + threads - 1) / threads, (size_t)sm_count * 32));
+}
+
+// Exclusive prefix sum of n uint32 values (in and out may alias); *total
+// (host, optional) receives the sum. Synchronises when total is wanted.
+svo_status dev_scan(svo_context* ctx, DevScratch& S, const uint32_t* in, uint32_t* out, size_t n, uint32_t* total) {
+    cudaStream_t s = ctx->stream;
+    if (n == 0) {
+        if (total) *total = 0;
+        return SVO_OK;
+    }
+    uint32_t last_in = 0;  // read before the scan: in and out may alias
+    if (total) SVO_CUDA(ctx, cudaMemcpyAsync(&last_in, in + n - 1, 4, cudaMemcpyDeviceToHost, s));
+    const size_t tiles = (n + kScanTile - 1) / kScanTile;
+    uint32_t* sums = nullptr;
+    if (tiles > 1) SVO_CUDA(ctx, S.get(&sums, tiles));
+    k_scan_tiles<<<(unsigned)tiles, kScanThreads, 0, s>>>(in, out, n, sums);
+    SVO_LAUNCHED(ctx);
+    if (tiles > 1) {
+        svo_status st = dev_scan(ctx, S, sums, sums, tiles, nullptr);
+        if (st != SVO_OK) return st;
+        k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(out, n, sums);
+        SVO_LAUNCHED(ctx);
+    }
+    if (total) {
+        uint32_t a = 0;
+        SVO_CUDA(ctx, cudaMemcpyAsync(&a, out + n - 1, 4, cudaMemcpyDeviceToHost, s));
+        SVO_CUDA(ctx, cudaStreamSynchronize(s));
+        *total = a + last_in;
+    }
+    return SVO_OK;
+}
+
+struct DevLevel {
+    uint64_t* key = nullptr;
+    uint32_t* first = nullptr;
+    uint32_t* begin = nullptr;  // n+1 entries (levels >= 1)
+    uint8_t* mask = nullptr;
+    uint32_t* size = nullptr;   // subtree words (heights 2-6)
+    uint32_t* st = nullptr;     // subtree start (heights 2-5) / block offset (height 6)
+    uint32_t* lr = nullptr;     // block start of the node's block (heights 2-5)
+    uint32_t* cnt = nullptr;    // normal subtree node count (heights >= 7)
+    uint32_t* ps = nullptr;     // post-order start (heights >= 7)
+    size_t n = 0;
+};
+
 svo_status alloc(svo_context* ctx, void** p, size_t bytes) {
     SVO_CUDA(ctx, cudaMalloc(p, bytes));
     return SVO_OK;
@@ -803,6 +868,210 @@ svo_status svo_octree_upload(svo_context* ctx, const uint32_t* words, size_t n_w
     // Keep the node words resident in L2 across frames (persisting window over
     // the whole array, clamped to what the device allows).
     return svo_octree_set_l2_window(ctx, ctx->l2_window_request);
+}
+
+// ------------------------------------------------------- GPU builder --
+svo_status svo_octree_build(svo_context* ctx, const uint32_t* d_x, const uint32_t* d_y, const uint32_t* d_z,
+                            const uint32_t* d_rgba, size_t n, int depth, size_t initial_words) {
+    if (!ctx || (n && (!d_x || !d_y || !d_z || !d_rgba))) return SVO_ERR_INVALID_ARGUMENT;
+    if (depth < SVO_MIN_DEPTH || depth > SVO_MAX_DEPTH) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "depth");
+    if (initial_words == 0) initial_words = SVO_DEFAULT_INITIAL_WORDS;
+    if (initial_words < 10 || initial_words >= (1ull << 31)) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "initial_words");
+    SVO_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    const int sms = ctx->sm_count;
+    DevScratch S;
+    uint32_t* words = nullptr;
+    size_t total_words = initial_words;
+    uint32_t root = 0;
+    if (n == 0) {
+        // empty scene: an all-zero root node with no children
+        SVO_CUDA(ctx, cudaMalloc(&words, initial_words * 4));
+        SVO_CUDA(ctx, cudaMemsetAsync(words, 0, initial_words * 4, s));
+    } else {
+        int ib = 1;
+        while (ib < 40 && ((n - 1) >> ib) != 0) ++ib;
+        const int key_bits = 3 * depth + ib;
+        if (key_bits > 64 || n >= 0xffffffffull)
+            return fail(ctx, SVO_ERR_CAPACITY, "too many voxels for 64-bit sort keys at this depth");
+        uint32_t* bad = nullptr;
+        SVO_CUDA(ctx, S.get(&bad, 4));
+        SVO_CUDA(ctx, cudaMemsetAsync(bad, 0, 16, s));
+        // ---- keys and sort
+        uint64_t *ka = nullptr, *kb = nullptr;
+        SVO_CUDA(ctx, S.get(&ka, n));
+        SVO_CUDA(ctx, S.get(&kb, n));
+        k_bld_keys<<<grid_for(n, 256, sms), 256, 0, s>>>(d_x, d_y, d_z, n, depth, ib, ka, bad);
+        SVO_LAUNCHED(ctx);
+        const uint32_t nblocks = (uint32_t)((n + kSortTile - 1) / kSortTile);
+        uint32_t* counts = nullptr;
+        SVO_CUDA(ctx, S.get(&counts, (size_t)256 * nblocks));
+        for (int shift = 0; shift < key_bits; shift += 8) {
+            k_sort_hist<<<nblocks, kSortThreads, 0, s>>>(ka, n, shift, counts, nblocks);
+            SVO_LAUNCHED(ctx);
+            svo_status st = dev_scan(ctx, S, counts, counts, (size_t)256 * nblocks, nullptr);
+            if (st != SVO_OK) return st;
+            k_sort_scatter<<<nblocks, kSortThreads, 0, s>>>(ka, kb, n, shift, counts, nblocks);
+            SVO_LAUNCHED(ctx);
+            std::swap(ka, kb);
+        }
+        // ---- levels
+        std::vector<DevLevel> L(depth + 1);
+        uint32_t *flags = nullptr, *pos = nullptr;
+        SVO_CUDA(ctx, S.get(&flags, n));
+        SVO_CUDA(ctx, S.get(&pos, n));
+        uint32_t* leaf = nullptr;
+        {
+            k_bld_flags<<<grid_for(n, 256, sms), 256, 0, s>>>(ka, n, ib, flags);
+            SVO_LAUNCHED(ctx);
+            uint32_t n0 = 0;
+            svo_status st = dev_scan(ctx, S, flags, pos, n, &n0);
+            if (st != SVO_OK) return st;
+            DevLevel& l0 = L[0];
+            l0.n = n0;
+            SVO_CUDA(ctx, S.get(&l0.key, n0));
+            SVO_CUDA(ctx, S.get(&l0.first, n0));
+            SVO_CUDA(ctx, S.get(&l0.begin, n0 + 1));
+            SVO_CUDA(ctx, S.get(&leaf, n0));
+            k_bld_level0<<<grid_for(n, 256, sms), 256, 0, s>>>(ka, n, ib, flags, pos, d_rgba, l0.key, l0.first,
+                                                                l0.begin, leaf);
+            SVO_LAUNCHED(ctx);
+        }
+        for (int h = 1; h <= depth; ++h) {
+            const DevLevel& c = L[h - 1];
+            DevLevel& l = L[h];
+            const size_t m = c.n;
+            k_bld_flags<<<grid_for(m, 256, sms), 256, 0, s>>>(c.key, m, 3, flags);
+            SVO_LAUNCHED(ctx);
+            uint32_t np = 0;
+            svo_status st = dev_scan(ctx, S, flags, pos, m, &np);
+            if (st != SVO_OK) return st;
+            l.n = np;
+            SVO_CUDA(ctx, S.get(&l.key, np));
+            SVO_CUDA(ctx, S.get(&l.first, np));
+            SVO_CUDA(ctx, S.get(&l.begin, np + 1));
+            SVO_CUDA(ctx, S.get(&l.mask, np));
+            k_bld_parents<<<grid_for(m, 256, sms), 256, 0, s>>>(c.key, m, flags, pos, l.key, l.begin);
+            SVO_LAUNCHED(ctx);
+            const uint32_t mm = (uint32_t)m;
+            SVO_CUDA(ctx, cudaMemcpyAsync(l.begin + np, &mm, 4, cudaMemcpyHostToDevice, s));
+            k_bld_reduce<<<grid_for(np, 256, sms), 256, 0, s>>>(c.key, c.first, np, l.begin, l.mask, l.first);
+            SVO_LAUNCHED(ctx);
+            SVO_CUDA(ctx, cudaStreamSynchronize(s));  // mm lives on this frame
+        }
+        if (L[depth].n != 1) return fail(ctx, SVO_ERR_CUDA, "builder: root level is not a single node");
+        // ---- block sizes (heights 2..6) and block offsets
+        for (int h = 2; h <= 6; ++h) {
+            DevLevel& l = L[h];
+            SVO_CUDA(ctx, S.get(&l.size, l.n));
+            if (h == 2)
+                k_bld_size2<<<grid_for(l.n, 256, sms), 256, 0, s>>>(l.n, l.begin, L[1].begin, leaf, l.size);
+            else
+                k_bld_size_up<<<grid_for(l.n, 256, sms), 256, 0, s>>>(l.n, l.begin, L[h - 1].size, l.size);
+            SVO_LAUNCHED(ctx);
+        }
+        DevLevel& l6 = L[6];
+        SVO_CUDA(ctx, S.get(&l6.st, l6.n));
+        k_bld_round64<<<grid_for(l6.n, 256, sms), 256, 0, s>>>(l6.n, l6.size, l6.st);
+        SVO_LAUNCHED(ctx);
+        uint32_t blocks_total = 0;
+        svo_status st = dev_scan(ctx, S, l6.st, l6.st, l6.n, &blocks_total);
+        if (st != SVO_OK) return st;
+        uint32_t last_off = 0, last_size = 0;
+        SVO_CUDA(ctx, cudaMemcpyAsync(&last_off, l6.st + l6.n - 1, 4, cudaMemcpyDeviceToHost, s));
+        SVO_CUDA(ctx, cudaMemcpyAsync(&last_size, l6.size + l6.n - 1, 4, cudaMemcpyDeviceToHost, s));
+        SVO_CUDA(ctx, cudaStreamSynchronize(s));
+        const uint64_t base = (initial_words + 63) / 64 * 64;
+        total_words = (size_t)(base + last_off + last_size);
+        uint64_t n_normal = 0;
+        for (int h = 7; h <= depth; ++h) n_normal += L[h].n;
+        if (10 * n_normal > initial_words)
+            return fail(ctx, SVO_ERR_CAPACITY, "normal nodes do not fit into initial_words (10 words each)");
+        if (total_words >= 0xffffffc0ull || (base >> 6) + ((uint64_t)last_off >> 6) >= (1ull << 23))
+            return fail(ctx, SVO_ERR_CAPACITY, "octree exceeds the compact format's 23-bit offsets");
+        SVO_CUDA(ctx, cudaMalloc(&words, total_words * 4));
+        SVO_CUDA(ctx, cudaMemsetAsync(words, 0, total_words * 4, s));
+        // ---- blocks, top-down
+        for (int h = 5; h >= 2; --h) {
+            SVO_CUDA(ctx, S.get(&L[h].st, L[h].n));
+            SVO_CUDA(ctx, S.get(&L[h].lr, L[h].n));
+        }
+        for (int h = 6; h >= 3; --h) {
+            DevLevel& l = L[h];
+            DevLevel& c = L[h - 1];
+            BlockLevel bl{l.begin, l.mask, l.first, l.size}, bc{c.begin, c.mask, c.first, c.size};
+            if (h == 6)
+                k_bld_emit_block<true><<<grid_for(l.n, 128, sms), 128, 0, s>>>(
+                    l.n, bl, bc, false, d_rgba, l.st, nullptr, (uint32_t)base, c.st, c.lr, words, total_words, bad);
+            else
+                k_bld_emit_block<false><<<grid_for(l.n, 128, sms), 128, 0, s>>>(
+                    l.n, bl, bc, h == 3, d_rgba, l.st, l.lr, (uint32_t)base, c.st, c.lr, words, total_words, bad);
+            SVO_LAUNCHED(ctx);
+        }
+        {
+            DevLevel& l2 = L[2];
+            BlockLevel b2{l2.begin, l2.mask, l2.first, l2.size};
+            k_bld_emit_h2<<<grid_for(l2.n, 128, sms), 128, 0, s>>>(l2.n, b2, L[1].begin, L[1].mask, leaf, d_rgba,
+                                                                  l2.st, words, total_words, bad);
+            SVO_LAUNCHED(ctx);
+        }
+        // ---- normal nodes
+        for (int h = 7; h <= depth; ++h) {
+            DevLevel& l = L[h];
+            SVO_CUDA(ctx, S.get(&l.cnt, l.n));
+            SVO_CUDA(ctx, S.get(&l.ps, l.n));
+            k_bld_count_up<<<grid_for(l.n, 256, sms), 256, 0, s>>>(l.n, l.begin, h == 7 ? nullptr : L[h - 1].cnt,
+                                                                  l.cnt);
+            SVO_LAUNCHED(ctx);
+        }
+        SVO_CUDA(ctx, cudaMemsetAsync(L[depth].ps, 0, 4, s));
+        for (int h = depth; h >= 7; --h) {
+            DevLevel& l = L[h];
+            DevLevel& c = L[h - 1];
+            k_bld_emit_normal<<<grid_for(l.n, 128, sms), 128, 0, s>>>(
+                l.n, h, depth, l.begin, l.mask, l.first, l.cnt, l.ps, c.key, c.mask, h - 1 >= 7 ? c.cnt : nullptr,
+                h - 1 >= 7 ? c.ps : nullptr, h - 1 == 6 ? c.st : nullptr, (uint32_t)base, d_rgba, words, total_words,
+                bad);
+            SVO_LAUNCHED(ctx);
+        }
+        uint8_t root_mask = 0;
+        uint32_t flags_host = 0;
+        SVO_CUDA(ctx, cudaMemcpyAsync(&root_mask, L[depth].mask, 1, cudaMemcpyDeviceToHost, s));
+        SVO_CUDA(ctx, cudaMemcpyAsync(&flags_host, bad, 4, cudaMemcpyDeviceToHost, s));
+        SVO_CUDA(ctx, cudaStreamSynchronize(s));
+        if (flags_host) {
+            cudaFree(words);
+            if (flags_host & 1u) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "voxel coordinate outside the volume");
+            if (flags_host & 4u) return fail(ctx, SVO_ERR_CUDA, "builder: store outside the word array");
+            return fail(ctx, SVO_ERR_CAPACITY, "octree exceeds the compact format's 23-bit offsets");
+        }
+        root = ((uint32_t)(10 * (n_normal - 1)) << 9) | root_mask;
+    }
+    SVO_CUDA(ctx, cudaStreamSynchronize(s));
+    if (ctx->owns_octree && ctx->d_octree) cudaFree(ctx->d_octree);
+    ctx->d_octree = words;
+    ctx->owns_octree = true;
+    ctx->n_words = total_words;
+    ctx->root = root;
+    ctx->depth = depth;
+    return svo_octree_set_l2_window(ctx, ctx->l2_window_request);
+}
+
+svo_status svo_octree_info(const svo_context* ctx, size_t* n_words, uint32_t* root_word, int* depth) {
+    if (!ctx || !ctx->d_octree) return SVO_ERR_NO_OCTREE;
+    if (n_words) *n_words = ctx->n_words;
+    if (root_word) *root_word = ctx->root;
+    if (depth) *depth = ctx->depth;
+    return SVO_OK;
+}
+
+svo_status svo_octree_download(svo_context* ctx, uint32_t* host, size_t n_words) {
+    if (!ctx || !host) return SVO_ERR_INVALID_ARGUMENT;
+    if (!ctx->d_octree) return fail(ctx, SVO_ERR_NO_OCTREE, "no octree");
+    if (n_words != ctx->n_words) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "n_words differs from the octree's");
+    SVO_CUDA(ctx, cudaMemcpyAsync(host, ctx->d_octree, n_words * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    SVO_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return SVO_OK;
 }
 
 svo_status svo_octree_upload_device(svo_context* ctx, const uint32_t* d_words, size_t n_words, uint32_t root_word,

@@ -45,7 +45,7 @@ EXPORTS = [
     "svo_warp_frame_learned", "svo_read_requested", "svo_target_set_feature_tap", "svo_net_create",
     "svo_net_destroy", "svo_net_init", "svo_net_set_params", "svo_net_get_params", "svo_net_get_grads",
     "svo_net_forward", "svo_net_infer", "svo_net_backward", "svo_net_adam", "svo_target_set_cache_mode",
-    "svo_target_set_coarse_refresh",
+    "svo_target_set_coarse_refresh", "svo_octree_build", "svo_octree_info", "svo_octree_download",
 ]
 
 NET_PARAMS = 6388
@@ -162,6 +162,9 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "svo_target_set_feature_tap": (i, [_P, _P]),
         "svo_target_set_cache_mode": (i, [_P, i]),
         "svo_target_set_coarse_refresh": (i, [_P, i]),
+        "svo_octree_build": (i, [_P, _P, _P, _P, _P, sz, i, sz]),
+        "svo_octree_info": (i, [_P, ctypes.POINTER(sz), ctypes.POINTER(u32), ctypes.POINTER(i)]),
+        "svo_octree_download": (i, [_P, _P, sz]),
         "svo_net_create": (i, [_P, ctypes.POINTER(_P)]),
         "svo_net_destroy": (i, [_P]),
         "svo_net_init": (i, [_P, ctypes.c_uint64]),
@@ -339,6 +342,24 @@ class Context:
 
     def upload_device(self, d_words: int, n_words: int, root: int, depth: int) -> None:
         _check(self._lib.svo_octree_upload_device(self._h, _P(d_words), n_words, root, depth), self)
+
+    def build_octree(self, d_x: int, d_y: int, d_z: int, d_rgba: int, n: int, depth: int,
+                     initial_words: int = 0) -> None:
+        """Builds the octree on the GPU from device voxel arrays (uint32 each) and installs it."""
+        _check(self._lib.svo_octree_build(self._h, _P(d_x), _P(d_y), _P(d_z), _P(d_rgba), n, depth, initial_words),
+               self)
+
+    def octree_info(self) -> tuple[int, int, int]:
+        """(n_words, root_word, depth) of the installed octree."""
+        nw, root, depth = ctypes.c_size_t(), ctypes.c_uint32(), ctypes.c_int()
+        _check(self._lib.svo_octree_info(self._h, ctypes.byref(nw), ctypes.byref(root), ctypes.byref(depth)), self)
+        return nw.value, root.value, depth.value
+
+    def download_octree(self) -> Octree:
+        nw, root, depth = self.octree_info()
+        words = np.empty(nw, np.uint32)
+        _check(self._lib.svo_octree_download(self._h, _ptr(words), nw), self)
+        return Octree(words, root, depth)
 
     def set_option(self, option: int, value: int) -> None:
         _check(self._lib.svo_context_set_option(self._h, option, value), self)
