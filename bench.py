@@ -60,6 +60,8 @@ def parse_args(argv=None):
     ap.add_argument("--graph", type=int, default=1, help="replay each warp frame as a CUDA graph")
     ap.add_argument("--views", type=int, default=8, help="camera streams of the concurrent multi-view measurement")
     ap.add_argument("--threshold", type=float, default=0.5, help="confidence below which learned frames trace a pixel")
+    ap.add_argument("--extras", type=int, default=1,
+                    help="also measure the GPU octree builder, the 64-view batch and the large depth-12 scene")
     ap.add_argument("--weights", default=os.path.join(ROOT, "sparse-voxel-octree-raycasting_gb300", "net_weights.npy"))
     return ap.parse_args(argv)
 
@@ -200,6 +202,149 @@ def run_reference(args, rank: int, world: int) -> None:
         "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------- extras --
+def measure_builder(svo, torch, octree, depth, seed, device):
+    """GPU octree builder on the benchmark scene's voxels vs the host builder's
+    words (timed on the device; voxel arrays already resident)."""
+    x, y, z, c = svo.terrain_voxels(seed, depth, True)
+    dev = [torch.from_numpy(np.ascontiguousarray(a, np.uint32).view(np.int32)).to(device) for a in (x, y, z, c)]
+    torch.cuda.synchronize(device)
+    ctx = svo.Context(device.index)
+    ext = torch.cuda.ExternalStream(ctx.stream, device=device)
+    ms = []
+    for _ in range(4):
+        s_ev, e_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s_ev.record(ext)
+        ctx.build_octree(*(t.data_ptr() for t in dev), len(x), depth)
+        e_ev.record(ext)
+        e_ev.synchronize()
+        ms.append(s_ev.elapsed_time(e_ev))
+    built = ctx.download_octree()
+    same = bool(built.root == octree.root and np.array_equal(built.words, octree.words))
+    ctx.close()
+    return {"voxels": int(len(x)), "gpu_ms": float(np.median(ms[1:])), "identical_to_host_builder": same,
+            "note": "device events around svo_octree_build (sort, levels, layout, emission; includes its "
+                    "host synchronisations)"}
+
+
+def measure_batch(svo, torch, ctx, depth, device, n_views=64, steps=8):
+    """64 cameras at seeded random poses, resolutions log-uniform 256^2..1920x1080,
+    all traced by one persistent launch (svo_raycast_full_batch)."""
+    rng = np.random.default_rng(64)
+    res = []
+    for _ in range(n_views):
+        w = int(np.exp(rng.uniform(np.log(256), np.log(1920))))
+        h = int(np.clip(w * rng.uniform(0.5, 1.0), 256, 1080))
+        res.append((w, h))
+    targets = [ctx.target(w, h) for w, h in res]
+    views = [svo.camera_path(3, depth, k, w, h, seed=11) for k, (w, h) in enumerate(res)]
+    ext = torch.cuda.ExternalStream(ctx.stream, device=device)
+    for _ in range(2):
+        ctx.raycast_full_batch(targets, views)
+    ctx.synchronize()
+    ms = []
+    for _ in range(steps):
+        s_ev, e_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s_ev.record(ext)
+        ctx.raycast_full_batch(targets, views)
+        e_ev.record(ext)
+        e_ev.synchronize()
+        ms.append(s_ev.elapsed_time(e_ev))
+    rays = sum(w * h for w, h in res)
+    for t in targets:
+        t.close()
+    t_ms = float(np.mean(ms))
+    return {"views": n_views, "rays_per_launch": rays, "ms_per_launch": t_ms, "mrays_per_s": rays / t_ms / 1e3}
+
+
+def measure_large(svo, torch, args, device, frames=16, views=8):
+    """Depth-12 terrain + 2000 solid boxes (built on the GPU), 3840x2160, fast
+    motion, 8 camera streams at once: learned frames/s (all views), plain warp
+    frames/s, full raycast frames/s of one view and the learned frames' PSNR."""
+    W, H, depth = 3840, 2160, 12
+    t0 = time.perf_counter()
+    x, y, z, c = svo.terrain_voxels(args.seed, depth, True, 2000)
+    gen_s = time.perf_counter() - t0
+    dev = [torch.from_numpy(np.ascontiguousarray(a, np.uint32).view(np.int32)).to(device) for a in (x, y, z, c)]
+    n = len(x)
+    del x, y, z, c
+    torch.cuda.synchronize(device)
+    base = svo.Context(device.index)
+    t0 = time.perf_counter()
+    base.build_octree(*(t.data_ptr() for t in dev), n, depth)
+    build_s = time.perf_counter() - t0
+    del dev
+    nw, root, _ = base.octree_info()
+    words = base.download_octree().words
+    d_words = torch.from_numpy(words.view(np.int32)).to(device)
+    torch.cuda.synchronize(device)
+    ctxs, tgts, nets = [], [], []
+    for k in range(views):
+        cx = svo.Context(device.index)
+        cx.upload_device(d_words.data_ptr(), nw, root, depth)
+        t = cx.target(W, H)
+        t.use_graph(True)
+        net = svo.Net(cx)
+        net.load_file(args.weights)
+        ctxs.append(cx)
+        tgts.append(t)
+        nets.append(net)
+
+    def vw(k, f):
+        return svo.camera_path(2, depth, 64 * k + f, W, H)
+
+    out = {"workload": "depth-12 terrain + 2000 boxes, 3840x2160, fast motion, 8 streams",
+           "voxels": int(n), "octree_words": int(nw), "voxel_generation_s": gen_s, "gpu_build_s": build_s}
+    for mode in ("learned", "plain"):
+        for f in range(4):
+            for k in range(views):
+                if mode == "learned":
+                    ctxs[k].warp_frame_learned(tgts[k], vw(k, f), f, nets[k], args.threshold)
+                else:
+                    ctxs[k].warp_frame(tgts[k], vw(k, f), f)
+        for cx in ctxs:
+            cx.synchronize()
+        t0 = time.perf_counter()
+        for f in range(4, 4 + frames):
+            for k in range(views):
+                if mode == "learned":
+                    ctxs[k].warp_frame_learned(tgts[k], vw(k, f), f, nets[k], args.threshold)
+                else:
+                    ctxs[k].warp_frame(tgts[k], vw(k, f), f)
+        for cx in ctxs:
+            cx.synchronize()
+        out[mode + "_frames_per_s"] = views * frames / (time.perf_counter() - t0)
+    full = base.target(W, H)
+    base.raycast_full(full, vw(0, 4))
+    base.synchronize()
+    t0 = time.perf_counter()
+    for f in range(5, 5 + 4):
+        base.raycast_full(full, vw(0, f))
+    base.synchronize()
+    out["full_frames_per_s_one_view"] = 4 / (time.perf_counter() - t0)
+    # learned quality on view 0
+    tq = ctxs[0].target(W, H)
+    mse = []
+    for f in range(0, 12):
+        v = vw(0, f)
+        ctxs[0].warp_frame_learned(tq, v, f, nets[0], args.threshold)
+        if f >= 4:
+            base.raycast_full(full, v)
+            mse.append(10 ** (-svo.psnr_bgrx(tq.bgrx(), full.bgrx()) / 10))
+    out["learned_psnr_db"] = float(-10 * np.log10(np.mean(mse))) if np.mean(mse) > 0 else float("inf")
+    tq.close()
+    full.close()
+    for t in tgts:
+        t.close()
+    for net in nets:
+        net.close()
+    for cx in ctxs:
+        cx.close()
+    base.close()
+    del d_words
+    return out
 
 
 # ------------------------------------------------------------------- ours --
@@ -488,6 +633,12 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                                           1.0, 1.0, threads)
         bytes_per_ray = (4.0 * (float(st[1]) + float(st[2])) + 20.0 * float(st[0])) / float(st[0])
 
+    extras = {}
+    if args.extras and rank == 0:
+        extras["octree_builder"] = measure_builder(svo, torch, octree, depth, args.seed, device)
+        extras["batch_64_views"] = measure_batch(svo, torch, ctx, depth, device)
+        extras["large"] = measure_large(svo, torch, args, device)
+
     peaks = measured_peaks()
     hbm = peaks.get("hbm_gbs")
     tflops = peaks.get("bf16_tflops")
@@ -543,6 +694,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
             "multiview": multiview,
             "parity_plain_vs_oracle": parity,
             "octree_build_s": t_build,
+            **extras,
         }
         print(json.dumps(line), flush=True)
     for t in (tgt, tgt_l, full):

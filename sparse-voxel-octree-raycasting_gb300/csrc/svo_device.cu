@@ -94,6 +94,7 @@ struct svo_target {
     svo_view prev_view{};
     bool have_prev_view = false;
     float* feature_tap = nullptr;  // device [8][N]: features written after reprojection
+    uint32_t* req_offs = nullptr;  // learned frames: request offsets per 8x4 packet
     // CUDA graphs of one warp frame: [0] plain, [1] learned
     bool use_graph = false;
     FrameGraph graphs[2];
@@ -363,6 +364,11 @@ svo_status launch_trace_warp(svo_context* ctx, svo_target* t, int kind = kTraceW
     return launch_trace(ctx, L, args);
 }
 
+// Grid for a grid-stride loop over n items: enough blocks, capped at 32 per SM.
+inline unsigned grid_for(size_t n, int threads, int sm_count) {
+    return (unsigned)std::max<size_t>(1, std::min<size_t>((n + threads - 1) / threads, (size_t)sm_count * 32));
+}
+
 void record(svo_target* t, int i) {
     if (!t->profiling) return;
     if (t->capturing)
@@ -534,6 +540,14 @@ svo_status enqueue_learned_body(svo_context* ctx, svo_target* t, const svo_net* 
     A.logit_threshold = logit_threshold;
     svo_status st = launch_net_infer(ctx, net, true, A);
     if (st != SVO_OK) return st;
+    {
+        const size_t packets = (size_t)t->B.packets_x * t->B.packets_y;
+        const unsigned nb = (unsigned)((packets + kReqBlock - 1) / kReqBlock);
+        k_request_scan<<<nb, kReqBlock, 0, s>>>(t->B, t->req_offs, t->req_offs + packets);
+        SVO_LAUNCHED(ctx);
+        k_request_write<<<nb, kReqBlock, 0, s>>>(t->B, t->req_offs, t->req_offs + packets);
+        SVO_LAUNCHED(ctx);
+    }
     record(t, 3);
     st = launch_trace_warp(ctx, t, kTraceWarpBgrx);
     if (st != SVO_OK) return st;
@@ -704,10 +718,6 @@ struct DevScratch {
         return e;
     }
 };
-
-inline unsigned grid_for(size_t n, int threads, int sm_count) {
-    return (unsigned)std::max<size_t>(1, std::min<size_t>((n + threads - 1) / threads, (size_t)sm_count * 32));
-}
 
 // Exclusive prefix sum of n uint32 values (in and out may alias); *total
 // (host, optional) receives the sum. Synchronises when total is wanted.
@@ -1144,6 +1154,11 @@ svo_status svo_target_create(svo_context* ctx, int res_x, int res_y, svo_target*
     A((void**)&t->B.keys, N * 8);
     A((void**)&t->B.ids, (N + 2 * t->tiles + 4) * 4);
     A((void**)&t->B.tile_mask, (t->tiles + 1) * 8);
+    t->B.packets_x = (res_x + 7) / 8;
+    t->B.packets_y = (res_y + 3) / 4;
+    const size_t packets = (size_t)t->B.packets_x * t->B.packets_y;
+    A((void**)&t->B.req_mask, packets * 4);
+    A((void**)&t->req_offs, (packets + (packets + kReqBlock - 1) / kReqBlock) * 4);  // offsets + block totals
     A((void**)&t->B.counters, 64);
     A((void**)&t->d_params, sizeof(FrameParams));
     A((void**)&t->full_col, N * 4);
@@ -1163,6 +1178,7 @@ svo_status svo_target_create(svo_context* ctx, int res_x, int res_y, svo_target*
     SVO_CUDA(ctx, cudaMemsetAsync(t->B.xyz[2], 0, N * 16, s));
     SVO_CUDA(ctx, cudaMemsetAsync(t->B.ids, 0, (N + 2 * t->tiles + 4) * 4, s));
     SVO_CUDA(ctx, cudaMemsetAsync(t->B.tile_mask, 0, (t->tiles + 1) * 8, s));
+    SVO_CUDA(ctx, cudaMemsetAsync(t->B.req_mask, 0, packets * 4, s));
     SVO_CUDA(ctx, cudaMemsetAsync(t->B.counters, 0, 64, s));
     SVO_CUDA(ctx, cudaMemsetAsync(t->B.bgrx, 0, N * 4, s));
     SVO_CUDA(ctx, cudaMemsetAsync(t->B.disp, 0xff, N * 4, s));
@@ -1180,7 +1196,8 @@ svo_status svo_target_destroy(svo_target* t) {
     cudaStreamSynchronize(ctx->stream);
     for (auto& g : t->graphs) g.reset();
     void* ptrs[] = {t->B.col[0], t->B.col[1], t->B.col[2], t->B.xyz[0], t->B.xyz[1], t->B.xyz[2], t->B.disp, t->B.bgrx, t->B.keys, t->B.ids,
-                    t->B.tile_mask, t->B.counters, t->d_params, t->full_col, t->full_xyzw, t->full_vox};
+                    t->B.tile_mask, t->B.counters, t->d_params, t->full_col, t->full_xyzw, t->full_vox,
+                    t->B.req_mask, t->req_offs};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (auto& e : t->ev)

@@ -54,6 +54,8 @@ struct TargetBuffers {
     uint64_t* keys;     // per-pixel projection keys, kKeyEmpty between frames
     uint32_t* ids;      // hole id buffer in the reference layout
     uint64_t* tile_mask;  // per 16x16 tile, bit j*8+i = 2x2 block (i,j) empty
+    uint32_t* req_mask;   // learned frames: per 8x4 packet, bit (x&7)+8*(y&3) = ray requested
+    int packets_x, packets_y;  // ceil(res/8), ceil(res/4)
     uint32_t* counters;   // [0] trace work counter, [1] hole entries, [2] coarse-pass work counter
     int res_x, res_y;
     int tiles_x, tiles_y;  // whole 16x16 tiles (res/16)

@@ -601,16 +601,16 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_infer(NetInferArgs A) {
                                 A.B.bgrx[ofs] = bi + (gi << 8) + (ri << 16);
                                 req = !(z >= A.logit_threshold);
                             }
+                            // Ray requests: bit (x&7) + 8*(y&3) of the pixel's 8x4 packet. The
+                            // warp's lanes are consecutive pixels of one row, so the first lane
+                            // of each run of one packet ORs the run's bits in one atomic.
                             const uint32_t bal = __ballot_sync(0xffffffffu, req);
-                            if (bal) {
-                                uint32_t base = 0;
-                                if (lane == 0) base = atomicAdd(A.B.counters + 1, (uint32_t)__popc(bal));
-                                base = __shfl_sync(0xffffffffu, base, 0);
-                                if (req) {
-                                    const uint32_t rank = (uint32_t)__popc(bal & ((1u << lane) - 1u));
-                                    A.B.ids[2u * (uint32_t)A.B.tiles_x * (uint32_t)A.B.tiles_y + base + rank] =
-                                        (uint32_t)gx | ((uint32_t)gy << 16);
-                                }
+                            if (bal && (lane == 0 || (gx & 7) == 0)) {
+                                const int len = min(8 - (gx & 7), 32 - lane);
+                                const uint32_t run = (bal >> lane) & ((1u << len) - 1u);
+                                if (run)
+                                    atomicOr(A.B.req_mask + (size_t)(gy >> 2) * A.B.packets_x + (gx >> 3),
+                                             run << ((gx & 7) + 8 * (gy & 3)));
                             }
                         } else if (out) {
                             const size_t n = (size_t)W * H, ofs = (size_t)gy * W + gx;
@@ -635,6 +635,81 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_infer(NetInferArgs A) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kNetTmemCols) : "memory");
     }
     if (fault) atomicOr(A.fault, fault);
+}
+
+// ------------------------------------------------ ray-request list --
+// The requests of a learned frame, compacted in 8x4-packet order (packets in
+// row-major order, pixels in lane order) into the hole list the tracer reads:
+// consecutive entries are spatial neighbours, so the tracer's 32-ray packets
+// stay coherent. k_request_scan: per block of 1024 packets, the exclusive
+// scan of their request counts and the block's total; k_request_write adds
+// the totals of the blocks before it, writes the entries and clears the
+// mask words.
+constexpr int kReqBlock = 1024;
+
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_sums, uint32_t& total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0u;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += t;
+        }
+        warp_sums[lane] = w;
+    }
+    __syncthreads();
+    total = warp_sums[(blockDim.x >> 5) - 1];
+    return incl - v + (warp > 0 ? warp_sums[warp - 1] : 0u);
+}
+
+__global__ void __launch_bounds__(kReqBlock) k_request_scan(TargetBuffers B, uint32_t* __restrict__ offs,
+                                                            uint32_t* __restrict__ block_totals) {
+    __shared__ uint32_t warp_sums[32];
+    const uint32_t n = (uint32_t)B.packets_x * (uint32_t)B.packets_y;
+    const uint32_t t = blockIdx.x * kReqBlock + threadIdx.x;
+    const uint32_t c = t < n ? (uint32_t)__popc(B.req_mask[t]) : 0u;
+    uint32_t total;
+    const uint32_t ex = block_exclusive_scan(c, warp_sums, total);
+    if (t < n) offs[t] = ex;
+    if (threadIdx.x == 0) block_totals[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kReqBlock) k_request_write(TargetBuffers B, const uint32_t* __restrict__ offs,
+                                                             const uint32_t* __restrict__ block_totals) {
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t prefix_s;
+    const uint32_t n = (uint32_t)B.packets_x * (uint32_t)B.packets_y;
+    // totals of the blocks before this one
+    uint32_t part = 0;
+    for (uint32_t k = threadIdx.x; k < blockIdx.x; k += kReqBlock) part += block_totals[k];
+    uint32_t sum;
+    (void)block_exclusive_scan(part, warp_sums, sum);
+    if (threadIdx.x == 0) prefix_s = sum;
+    __syncthreads();
+    const uint32_t prefix = prefix_s;
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
+        B.counters[1] = prefix + block_totals[blockIdx.x];
+        B.counters[0] = 0;
+    }
+    const uint32_t t = blockIdx.x * kReqBlock + threadIdx.x;
+    if (t >= n) return;
+    uint32_t m = B.req_mask[t];
+    if (!m) return;
+    B.req_mask[t] = 0;
+    const uint32_t x0 = (t % (uint32_t)B.packets_x) * 8u, y0 = (t / (uint32_t)B.packets_x) * 4u;
+    uint32_t at = 2u * (uint32_t)B.tiles_x * (uint32_t)B.tiles_y + prefix + offs[t];
+    while (m) {
+        const uint32_t bit = (uint32_t)__ffs(m) - 1u;
+        m &= m - 1u;
+        B.ids[at++] = (x0 + (bit & 7u)) | ((y0 + (bit >> 3)) << 16);
+    }
 }
 
 // ----------------------------------------------- FP32 training path --
