@@ -60,6 +60,7 @@ def parse_args(argv=None):
     ap.add_argument("--graph", type=int, default=1, help="replay each warp frame as a CUDA graph")
     ap.add_argument("--views", type=int, default=8, help="camera streams of the concurrent multi-view measurement")
     ap.add_argument("--threshold", type=float, default=0.5, help="confidence below which learned frames trace a pixel")
+    ap.add_argument("--autotune", type=int, default=1, help="pick the trace configuration by measurement first")
     ap.add_argument("--extras", type=int, default=1,
                     help="also measure the GPU octree builder, the 64-view batch and the large depth-12 scene")
     ap.add_argument("--weights", default=os.path.join(ROOT, "sparse-voxel-octree-raycasting_gb300", "net_weights.npy"))
@@ -375,6 +376,10 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
 
     def view(f, kind=1):
         return svo.camera_path(kind, depth, frame_offset + f, W, H)
+
+    # trace packet shape / block size / node staging: measured on this GPU and scene
+    tune = ctx.autotune(full, view(args.warmup), repeats=3) if args.autotune else []
+    tuned = min(tune, key=lambda r: r["ms"]) if tune else None
 
     def flush_l2():
         flush.zero_()
@@ -692,6 +697,9 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
             "stage_ms": stage_ms_learned,
             "stage_ms_plain": stage_ms,
             "multiview": multiview,
+            "autotune": {"chosen": tuned, "default_8x4_ms": next((r["ms"] for r in tune if r["packet_w"] == 8 and
+                                                                 r["stage_nodes"] == 1 and r["block"] == 256), None),
+                         "candidates": len(tune)} if tune else None,
             "parity_plain_vs_oracle": parity,
             "octree_build_s": t_build,
             **extras,

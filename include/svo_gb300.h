@@ -91,7 +91,25 @@ uint64_t svo_launch_count(const svo_context* ctx);
  * each trace block's shared memory (when it fits, <= 160 KiB); 0 reads every
  * node word from global memory. */
 #define SVO_OPT_STAGE_NODES 1
+/* SVO_OPT_PACKET_WIDTH: ray packets of the trace kernels are W x (32/W)
+ * pixels, W = 4, 8 (default, the reference's 8x4 refresh tiles), 16 or 32. */
+#define SVO_OPT_PACKET_WIDTH 2
+/* SVO_OPT_TRACE_BLOCK: threads per trace block, 256 or 1024; 0 (default)
+ * picks by the size of the staged node region. */
+#define SVO_OPT_TRACE_BLOCK 3
 svo_status svo_context_set_option(svo_context* ctx, int option, int64_t value);
+
+/* Autotuner (no reference counterpart): times `repeats` full raycasts of
+ * `view` into `t` for every packet shape (4x8, 8x4, 16x2, 32x1), block size
+ * (256, 1024) and node staging (on, off), keeps the fastest in the context
+ * and returns every measurement (up to cap) in results. Results are
+ * identical under every setting; only the speed differs. Synchronises. */
+typedef struct svo_tune_result {
+    int packet_w, packet_h, block, stage_nodes;
+    float ms;
+} svo_tune_result;
+svo_status svo_context_autotune(svo_context* ctx, svo_target* t, const svo_view* view, int repeats,
+                                svo_tune_result* results, int cap, int* n_results);
 
 /* ------------------------------------------------------------ octree -- */
 

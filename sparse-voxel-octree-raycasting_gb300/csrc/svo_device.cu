@@ -45,6 +45,9 @@ struct svo_context {
     size_t l2_window = 0;
     size_t l2_window_request = ~(size_t)0;  // default: the whole octree
     bool stage_normal = true;               // stage the normal-node region in shared memory
+    int pw_shift = 3;                       // ray packets (1<<pw_shift) x (32>>pw_shift): 8x4
+    int block_pref = 0;                     // trace block size, 0: chosen by the staging size
+    uint64_t config_gen = 0;                // bumped by every option change (captured graphs re-capture)
     uint64_t launches = 0;
     std::vector<svo_target*> targets;  // live targets, destroyed with the context
     std::vector<svo_net*> nets;        // live nets, likewise
@@ -62,6 +65,7 @@ struct FrameGraph {
     float threshold = 0.0f;
     float* tap = nullptr;
     bool coarse = false;
+    uint64_t config_gen = 0;
     void reset() {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
@@ -315,6 +319,12 @@ svo_status plan_trace(svo_context* ctx, int kind, TraceLaunch& L) {
         }
     }
     L.block = stage_bytes > kStageSmallBytes ? 1024 : 256;
+    if (ctx->block_pref == 1024) L.block = 1024;
+    if (ctx->block_pref == 256 && L.block == 1024) {  // the staged region does not fit a 256-thread block
+        L.block = 256;
+        L.o.n_smem = 0;
+        stage_bytes = 0;
+    }
     L.fn = L.block == 1024 ? trace_fn_depth<1024>(ctx->depth, kind) : trace_fn_depth<256>(ctx->depth, kind);
     if (!L.fn) return fail(ctx, SVO_ERR_NOT_SUPPORTED, "octree depth");
     L.smem = (size_t)(ctx->depth + 1) * L.block * 4u + stage_bytes;
@@ -439,6 +449,7 @@ FrameParams make_params(const svo_target* t, const svo_view& v, int frame, const
     const int gx = (rx / 8 + 15) / 16 * 16, gy = (ry / 4 + 15) / 16 * 16;
     p.x_end = std::min(rx, p.add_x + gx);
     p.y_end = std::min(ry, p.add_y + gy);
+    p.pw_shift = t->ctx->pw_shift;
     p.coarse_x = (rx / 2) * (frame & 1);
     p.coarse_y = (ry / 2) * ((frame >> 1) & 1);
     p.have_prev_view = t->have_prev_view ? 1 : 0;
@@ -567,7 +578,7 @@ svo_status run_frame(svo_context* ctx, svo_target* t, const FrameParams& p, Fram
         return body();
     }
     if (!g.exec || g.profiled != t->profiling || g.net != net || g.threshold != threshold || g.tap != t->feature_tap ||
-        g.coarse != t->coarse) {
+        g.coarse != t->coarse || g.config_gen != ctx->config_gen) {
         g.reset();
         const uint64_t l0 = ctx->launches;
         SVO_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
@@ -605,6 +616,7 @@ svo_status run_frame(svo_context* ctx, svo_target* t, const FrameParams& p, Fram
         g.threshold = threshold;
         g.tap = t->feature_tap;
         g.coarse = t->coarse;
+        g.config_gen = ctx->config_gen;
     }
     cudaKernelNodeParams kp;
     SVO_CUDA(ctx, cudaGraphKernelNodeGetParams(g.params_node, &kp));
@@ -829,9 +841,20 @@ uint64_t svo_launch_count(const svo_context* ctx) { return ctx ? ctx->launches :
 
 svo_status svo_context_set_option(svo_context* ctx, int option, int64_t value) {
     if (!ctx) return SVO_ERR_INVALID_ARGUMENT;
+    ++ctx->config_gen;
     switch (option) {
         case SVO_OPT_STAGE_NODES:
             ctx->stage_normal = value != 0;
+            return SVO_OK;
+        case SVO_OPT_PACKET_WIDTH:
+            if (value != 4 && value != 8 && value != 16 && value != 32)
+                return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "packet width 4, 8, 16 or 32");
+            ctx->pw_shift = value == 4 ? 2 : value == 8 ? 3 : value == 16 ? 4 : 5;
+            return SVO_OK;
+        case SVO_OPT_TRACE_BLOCK:
+            if (value != 0 && value != 256 && value != 1024)
+                return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "trace block 0 (auto), 256 or 1024");
+            ctx->block_pref = (int)value;
             return SVO_OK;
         default:
             return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "unknown option");
@@ -1269,9 +1292,11 @@ svo_status svo_raycast_full_batch(svo_context* ctx, svo_target* const* targets, 
         fv.ray = make_raycam(v);
         fv.res_x = v.res_x;
         fv.res_y = v.res_y;
-        fv.packets_x = (v.res_x + 7) / 8;
+        const int pw = 1 << ctx->pw_shift, ph = 32 >> ctx->pw_shift;
+        fv.pw_shift = ctx->pw_shift;
+        fv.packets_x = (v.res_x + pw - 1) / pw;
         fv.packet_begin = packets;
-        packets += (uint32_t)fv.packets_x * (uint32_t)((v.res_y + 3) / 4);
+        packets += (uint32_t)fv.packets_x * (uint32_t)((v.res_y + ph - 1) / ph);
         fv.col = targets[i]->full_col;
         fv.xyzw = targets[i]->full_xyzw;
         fv.vox = targets[i]->full_vox;
@@ -1300,6 +1325,58 @@ svo_status svo_raycast_full_batch(svo_context* ctx, svo_target* const* targets, 
 svo_status svo_raycast_full(svo_context* ctx, svo_target* t, const svo_view* view) {
     if (!ctx || !t) return SVO_ERR_INVALID_ARGUMENT;
     return svo_raycast_full_batch(ctx, &t, view, 1);
+}
+
+svo_status svo_context_autotune(svo_context* ctx, svo_target* t, const svo_view* view, int repeats,
+                                svo_tune_result* results, int cap, int* n_results) {
+    if (!ctx || !t || !view || repeats < 1) return SVO_ERR_INVALID_ARGUMENT;
+    svo_status st = check_view(ctx, t, view);
+    if (st != SVO_OK) return st;
+    struct Cfg {
+        int pw, block, stage;
+    };
+    std::vector<Cfg> cfgs;
+    for (int pw : {4, 8, 16, 32})
+        for (int stage : {1, 0})
+            for (int block : {256, 1024}) cfgs.push_back({pw, block, stage});
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    SVO_CUDA(ctx, cudaEventCreate(&e0));
+    SVO_CUDA(ctx, cudaEventCreate(&e1));
+    const bool stage0 = ctx->stage_normal;
+    const int pw0 = ctx->pw_shift, block0 = ctx->block_pref;
+    float best = 1e30f;
+    Cfg best_cfg{1 << pw0, block0, stage0 ? 1 : 0};
+    int k = 0;
+    for (const Cfg& c : cfgs) {
+        ctx->pw_shift = c.pw == 4 ? 2 : c.pw == 8 ? 3 : c.pw == 16 ? 4 : 5;
+        ctx->block_pref = c.block;
+        ctx->stage_normal = c.stage != 0;
+        st = svo_raycast_full(ctx, t, view);  // warm-up
+        float ms = 0.0f;
+        if (st == SVO_OK && cudaEventRecord(e0, ctx->stream) == cudaSuccess) {
+            for (int r = 0; r < repeats && st == SVO_OK; ++r) st = svo_raycast_full(ctx, t, view);
+            if (st == SVO_OK && cudaEventRecord(e1, ctx->stream) == cudaSuccess &&
+                cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess)
+                ms /= (float)repeats;
+            else if (st == SVO_OK)
+                st = fail(ctx, SVO_ERR_CUDA, "autotune timing");
+        }
+        if (st != SVO_OK) break;
+        if (results && k < cap) results[k] = svo_tune_result{c.pw, 32 / c.pw, c.block, c.stage, ms};
+        ++k;
+        if (ms < best) {
+            best = ms;
+            best_cfg = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->pw_shift = best_cfg.pw == 4 ? 2 : best_cfg.pw == 8 ? 3 : best_cfg.pw == 16 ? 4 : best_cfg.pw == 32 ? 5 : pw0;
+    ctx->block_pref = best_cfg.block;
+    ctx->stage_normal = best_cfg.stage != 0;
+    ++ctx->config_gen;
+    if (n_results) *n_results = k;
+    return st;
 }
 
 svo_status svo_warp_frame(svo_context* ctx, svo_target* t, const svo_view* view, int frame) {
@@ -1793,6 +1870,7 @@ extern "C" svo_status svo_raycast_full_noalloc(const uint32_t* d_words, size_t n
         fv.ray.fovy = v.fovy;
         fv.res_x = v.res_x;
         fv.res_y = v.res_y;
+        fv.pw_shift = 3;
         fv.packets_x = (v.res_x + 7) / 8;
         fv.packet_begin = packets;
         packets += (uint32_t)fv.packets_x * (uint32_t)((v.res_y + 3) / 4);

@@ -40,6 +40,7 @@ struct FrameParams {
     int fill_past;      // physical plane of reference plane 1 after the copy, -1 = empty
     int add_x, add_y, x_end, y_end;  // refresh tile rectangle (raycast.h:363-366)
     int coarse_x, coarse_y;          // quadrant origin of the raycast_fine pass (raycast.h:240-241)
+    int pw_shift;                    // ray packets are (1<<pw_shift) x (32>>pw_shift) pixels
     // previous frame's camera (the reconstruction net's motion feature)
     float prev_pos[3], prev_vx[3], prev_vy[3], prev_vz[3];
     int have_prev_view;
@@ -65,7 +66,8 @@ struct TargetBuffers {
 struct FullView {
     RayCam ray;
     int res_x, res_y;
-    int packets_x;          // ceil(res_x/8): 8x4-pixel ray packets per row
+    int packets_x;          // ray packets per row: ceil(res_x / packet width)
+    int pw_shift;           // packets are (1<<pw_shift) x (32>>pw_shift) pixels
     uint32_t packet_begin;  // first packet of this view in the batch
     uint32_t* col;
     float4* xyzw;
@@ -358,8 +360,9 @@ __global__ void __launch_bounds__(BLOCK) k_trace_full(Octree o_in, const FullBat
         }
         const FullView& fv = batch->v[v];
         const uint32_t q = p - fv.packet_begin;
-        const int x = (int)(q % (uint32_t)fv.packets_x) * 8 + (lane & 7);
-        const int y = (int)(q / (uint32_t)fv.packets_x) * 4 + (lane >> 3);
+        const int ps = fv.pw_shift;
+        const int x = ((int)(q % (uint32_t)fv.packets_x) << ps) + (lane & ((1 << ps) - 1));
+        const int y = (int)(q / (uint32_t)fv.packets_x) * (32 >> ps) + (lane >> ps);
         if (x < fv.res_x && y < fv.res_y) {
             const RayCam cam = fv.ray;
             const RayResult r = trace_ray<DEPTH, kVoxel>(o, cam, x, y, fv.res_x, fv.res_y, stk, BLOCK, fault);
@@ -389,7 +392,8 @@ __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FramePa
     const uint32_t holes = B.counters[1];
     const uint32_t hole_packets = (holes + 31u) / 32u;
     const int ax = P->add_x, ay = P->add_y, xe = P->x_end, ye = P->y_end;
-    const uint32_t rpx = (uint32_t)max(0, (xe - ax + 7) / 8), rpy = (uint32_t)max(0, (ye - ay + 3) / 4);
+    const int ps = P->pw_shift, pw = 1 << ps, ph = 32 >> ps;
+    const uint32_t rpx = (uint32_t)max(0, (xe - ax + pw - 1) / pw), rpy = (uint32_t)max(0, (ye - ay + ph - 1) / ph);
     const uint32_t total = hole_packets + rpx * rpy;
     const RayCam cam = P->ray;
     float4* __restrict__ xyz = plane_xyz(B, P->cur);
@@ -414,8 +418,8 @@ __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FramePa
             if (x >= ax && x < xe && y >= ay && y < ye) valid = false;  // traced by the refresh tile
         } else {
             const uint32_t q = p - hole_packets;
-            x = ax + (int)(q % rpx) * 8 + (lane & 7);
-            y = ay + (int)(q / rpx) * 4 + (lane >> 3);
+            x = ax + (int)(q % rpx) * pw + (lane & (pw - 1));
+            y = ay + (int)(q / rpx) * ph + (lane >> ps);
             valid = x < xe && y < ye;
         }
         if (valid) {

@@ -22,6 +22,8 @@ LIB_PATH = os.path.join(HERE, "libsvo_gb300.so")
 
 EMPTY_PIXEL = 0xFFFFFF00
 OPT_STAGE_NODES = 1
+OPT_PACKET_WIDTH = 2
+OPT_TRACE_BLOCK = 3
 NOALLOC_MAX_VIEWS = 64
 DEFAULT_INITIAL_WORDS = 2097152
 STATUS = {
@@ -46,6 +48,7 @@ EXPORTS = [
     "svo_net_destroy", "svo_net_init", "svo_net_set_params", "svo_net_get_params", "svo_net_get_grads",
     "svo_net_forward", "svo_net_infer", "svo_net_backward", "svo_net_adam", "svo_target_set_cache_mode",
     "svo_target_set_coarse_refresh", "svo_octree_build", "svo_octree_info", "svo_octree_download",
+    "svo_context_autotune",
 ]
 
 NET_PARAMS = 6388
@@ -80,6 +83,11 @@ class FrameBuffers(ctypes.Structure):
     """svo_frame_buffers: device output buffers of one view of svo_raycast_full_noalloc."""
     _fields_ = [("colour", ctypes.c_void_p), ("xyzw", ctypes.c_void_p), ("voxel", ctypes.c_void_p),
                 ("bgrx", ctypes.c_void_p)]
+
+
+class TuneResult(ctypes.Structure):
+    _fields_ = [("packet_w", ctypes.c_int), ("packet_h", ctypes.c_int), ("block", ctypes.c_int),
+                ("stage_nodes", ctypes.c_int), ("ms", ctypes.c_float)]
 
 
 class DeviceOutputs(ctypes.Structure):
@@ -165,6 +173,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "svo_octree_build": (i, [_P, _P, _P, _P, _P, sz, i, sz]),
         "svo_octree_info": (i, [_P, ctypes.POINTER(sz), ctypes.POINTER(u32), ctypes.POINTER(i)]),
         "svo_octree_download": (i, [_P, _P, sz]),
+        "svo_context_autotune": (i, [_P, _P, ctypes.POINTER(View), i, _P, i, ctypes.POINTER(i)]),
         "svo_net_create": (i, [_P, ctypes.POINTER(_P)]),
         "svo_net_destroy": (i, [_P]),
         "svo_net_init": (i, [_P, ctypes.c_uint64]),
@@ -360,6 +369,16 @@ class Context:
         words = np.empty(nw, np.uint32)
         _check(self._lib.svo_octree_download(self._h, _ptr(words), nw), self)
         return Octree(words, root, depth)
+
+    def autotune(self, target: "Target", view: View, repeats: int = 3) -> list[dict]:
+        """Times every trace configuration on full raycasts of `view`, keeps the fastest;
+        returns the measurements (packet_w, packet_h, block, stage_nodes, ms)."""
+        res = (TuneResult * 32)()
+        n = ctypes.c_int()
+        _check(self._lib.svo_context_autotune(self._h, target._h, ctypes.byref(view), repeats, ctypes.cast(res, _P),
+                                              32, ctypes.byref(n)), self)
+        return [{"packet_w": r.packet_w, "packet_h": r.packet_h, "block": r.block, "stage_nodes": r.stage_nodes,
+                 "ms": r.ms} for r in res[:n.value]]
 
     def set_option(self, option: int, value: int) -> None:
         _check(self._lib.svo_context_set_option(self._h, option, value), self)

@@ -240,3 +240,50 @@ def test_context_close_destroys_live_targets(svo, scene):
     assert lib.svo_target_create(h, 32, 16, ctypes.byref(th)) == 0
     assert lib.svo_context_destroy(h) == 0
 
+
+
+def test_trace_configurations_give_identical_frames(svo, scene, gpu_ctx):
+    # packet shape, block size and node staging change the schedule only
+    octree = scene(9, 77, True)
+    gpu_ctx.upload(octree)
+    W, H = 200, 120
+    full, warp = gpu_ctx.target(W, H), gpu_ctx.target(W, H)
+    v = svo.camera_path(1, 9, 3, W, H)
+    gpu_ctx.raycast_full(full, v)
+    want_col, want_xyz = full.full()
+    frames = [svo.camera_path(1, 9, f, W, H) for f in range(6)]
+    for f, fv in enumerate(frames):
+        gpu_ctx.warp_frame(warp, fv, f)
+    want_warp = warp.bgrx()
+    for pw in (4, 8, 16, 32):
+        for block in (0, 256, 1024):
+            for stage in (0, 1):
+                gpu_ctx.set_option(svo.OPT_PACKET_WIDTH, pw)
+                gpu_ctx.set_option(svo.OPT_TRACE_BLOCK, block)
+                gpu_ctx.set_option(svo.OPT_STAGE_NODES, stage)
+                gpu_ctx.raycast_full(full, v)
+                col, xyz = full.full()
+                assert np.array_equal(col, want_col) and np.array_equal(xyz.view(np.uint32),
+                                                                         want_xyz.view(np.uint32)), (pw, block, stage)
+                t = gpu_ctx.target(W, H)
+                for f, fv in enumerate(frames):
+                    gpu_ctx.warp_frame(t, fv, f)
+                assert np.array_equal(t.bgrx(), want_warp), (pw, block, stage)
+                t.close()
+    with pytest.raises(svo.SvoError):
+        gpu_ctx.set_option(svo.OPT_PACKET_WIDTH, 6)
+    full.close()
+    warp.close()
+
+
+def test_autotune_picks_a_measured_configuration(svo, scene, gpu_ctx):
+    octree = scene(9, 77, True)
+    gpu_ctx.upload(octree)
+    t = gpu_ctx.target(256, 160)
+    v = svo.camera_path(1, 9, 3, 256, 160)
+    res = gpu_ctx.autotune(t, v, repeats=2)
+    assert len(res) == 16 and all(r["ms"] > 0 for r in res)
+    assert {(r["packet_w"], r["packet_h"]) for r in res} == {(4, 8), (8, 4), (16, 2), (32, 1)}
+    gpu_ctx.raycast_full(t, v)  # runs with the chosen configuration
+    gpu_ctx.synchronize()
+    t.close()
