@@ -52,6 +52,7 @@ def parse_args(argv=None):
                          "training caches range from mostly reprojected to mostly traced")
     ap.add_argument("--init-seed", type=int, default=1)
     ap.add_argument("--segment", type=int, default=128, help="frames per camera-path stretch")
+    ap.add_argument("--epochs", type=int, default=1, help="passes over the --frames camera poses")
     ap.add_argument("--out", default=os.path.join(HERE, "net_weights.npy"))
     return ap.parse_args(argv)
 
@@ -116,7 +117,9 @@ def main(argv=None):
     lo, hi = (float(x) for x in args.threshold_range.split(","))
     rng = np.random.default_rng(args.init_seed)
     t0 = time.perf_counter()
-    for f in range(args.frames):
+    steps = args.frames * args.epochs
+    for step in range(steps):
+        f = step % args.frames
         seg = f // args.segment
         kind = ORBIT if seg % 2 == 0 else FAST_MOTION
         # each stretch continues its path where the previous stretch of that
@@ -125,13 +128,13 @@ def main(argv=None):
         v = svo.camera_path(kind, args.depth, pf, W, H)
         ctx.warp_frame_learned(tgt, v, f % args.segment, net, float(rng.uniform(lo, hi)))
         ctx.raycast_full(full, v)
-        lr = args.lr_end + 0.5 * (args.lr - args.lr_end) * (1 + np.cos(np.pi * f / max(1, args.frames - 1)))
+        lr = args.lr_end + 0.5 * (args.lr - args.lr_end) * (1 + np.cos(np.pi * step / max(1, steps - 1)))
         l_rgb, l_conf = net.backward(feat.data_ptr(), target_bgrx, W, H, args.tau, args.lam)
         net.adam(float(lr))
-        if f % 64 == 0 or f == args.frames - 1:
+        if step % 64 == 0 or step == steps - 1:
             req = tgt.requested() / (W * H)
-            curve.append({"frame": f, "loss_rgb": l_rgb, "loss_conf": l_conf, "requested": req})
-            print(f"frame {f:5d}  loss rgb {l_rgb:.3e}  conf {l_conf:.4f}  requested {100 * req:5.1f}%  "
+            curve.append({"step": step, "loss_rgb": l_rgb, "loss_conf": l_conf, "requested": req})
+            print(f"step {step:5d}  loss rgb {l_rgb:.3e}  conf {l_conf:.4f}  requested {100 * req:5.1f}%  "
                   f"lr {lr:.2e}  ({time.perf_counter() - t0:.1f} s)", flush=True)
     ctx.synchronize()
     train_s = time.perf_counter() - t0
