@@ -164,3 +164,48 @@ def test_feature_tap(svo, scene, gpu_ctx, net):
         assert np.all(np.diff(elev[:, W // 2]) > 0) or np.all(np.diff(elev[:, W // 2]) < 0)
     t.set_feature_tap(None)
     t.close()
+
+
+def _learned_quality(svo, ctx, net, octree, W, H, thr, frames=24, kind=2):
+    t, full = ctx.target(W, H), ctx.target(W, H)
+    mse, traced = [], []
+    for f in range(frames):
+        v = svo.camera_path(kind, octree.depth, f, W, H)
+        if net is None:
+            ctx.warp_frame(t, v, f)
+        else:
+            ctx.warp_frame_learned(t, v, f, net, thr)
+        if f >= 8:
+            ctx.raycast_full(full, v)
+            a = t.bgrx().view(np.uint8).reshape(-1, 4)[:, :3].astype(np.float64)
+            b = full.bgrx().view(np.uint8).reshape(-1, 4)[:, :3].astype(np.float64)
+            mse.append(((a - b) ** 2).mean())
+            traced.append((t.holes()[1] if net is None else t.requested()) / (W * H))
+    t.close()
+    full.close()
+    return 10 * np.log10(255.0 ** 2 / max(np.mean(mse), 1e-9)), float(np.mean(traced))
+
+
+def test_trained_net_gains_over_the_method_without_it(svo, gpu_ctx):
+    # The committed weights against the method without them: (a) the plain
+    # warp pipeline (hole filter + hole rays) on the same held-out frames --
+    # the net buys several dB; (b) an untrained net at the same threshold --
+    # its confidence is uninformative (it traces nearly everything or
+    # nothing), the trained one traces a fraction and keeps the quality.
+    import os
+    octree = svo.build_terrain(10, 2024, shell=True)
+    gpu_ctx.upload(octree)
+    W, H = 640, 384
+    trained = gpu_ctx.net()
+    trained.load_file(os.path.join(os.path.dirname(svo.__file__), "net_weights.npy"))
+    p_tr, f_tr = _learned_quality(svo, gpu_ctx, trained, octree, W, H, 0.5)
+    p_plain, f_plain = _learned_quality(svo, gpu_ctx, None, octree, W, H, 0.5)
+    print(f"trained: {p_tr:.2f} dB, {100 * f_tr:.1f}% traced; plain: {p_plain:.2f} dB, {100 * f_plain:.1f}% traced")
+    assert p_tr > p_plain + 4.0, (p_tr, p_plain)
+    assert p_tr > 34.0 and f_tr < 0.85, (p_tr, f_tr)
+    untrained = gpu_ctx.net(seed=3)
+    p_un, f_un = _learned_quality(svo, gpu_ctx, untrained, octree, W, H, 0.5)
+    print(f"untrained: {p_un:.2f} dB, {100 * f_un:.1f}% traced")
+    assert f_un > 0.95 or p_un < p_tr - 4.0, (p_un, f_un)
+    trained.close()
+    untrained.close()
