@@ -209,3 +209,22 @@ def test_trained_net_gains_over_the_method_without_it(svo, gpu_ctx):
     assert f_un > 0.95 or p_un < p_tr - 4.0, (p_un, f_un)
     trained.close()
     untrained.close()
+
+
+@pytest.mark.parametrize("W,H", [(37, 29), (100, 50), (130, 17), (57, 25)])
+def test_learned_frames_ragged_resolutions(svo, scene, gpu_ctx, net, W, H):
+    # ragged net tiles (56x24), ragged 8x4 request packets and ragged 16x16
+    # hole tiles: every pixel requested -> the full raycast, bit for bit
+    octree = scene(8, 31, True)
+    gpu_ctx.upload(octree)
+    t, full = gpu_ctx.target(W, H), gpu_ctx.target(W, H)
+    t.use_graph(True)
+    for f in range(5):
+        v = svo.camera_path(2, 8, f, W, H)
+        gpu_ctx.warp_frame_learned(t, v, f, net, 0.999999)
+        gpu_ctx.raycast_full(full, v)
+        gpu_ctx.synchronize()
+        assert np.array_equal(t.bgrx(), full.bgrx()), f
+        assert t.requested() == W * H
+    t.close()
+    full.close()
