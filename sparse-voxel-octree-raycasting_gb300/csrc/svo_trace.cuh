@@ -183,6 +183,15 @@ template <bool kFast>
 __device__ __forceinline__ float int_to_float(int v) {
     return kFast ? u23_to_float(v) : (float)v;
 }
+// The next cell boundary above coordinate r at level rek, as a float:
+// ((r >> rek) + 1) << rek = (r | (2^rek - 1)) + 1, whose float bits on the
+// fast path are (r | mask) + bits(2^23) + 1 (no carry past bit 23 for
+// r < 2^23; a sum of exactly 2^23 gives bits(2^24), also exact).
+template <bool kFast>
+__device__ __forceinline__ float next_boundary(int r, int rek) {
+    if (kFast) return __fsub_rn(__int_as_float((r | ((1 << rek) - 1)) + 0x4B000001), 8388608.0f);
+    return (float)(((r >> rek) + 1) << rek);
+}
 template <bool kFast>
 __device__ __forceinline__ int float_to_int(float x) {
     return kFast ? trunc_u23(x) : __float2int_rz(x);
@@ -282,10 +291,9 @@ __device__ __forceinline__ void walk(const Octree& o, Walk& w, uint32_t sxyz, fl
             fault |= kFaultSteps;
             break;
         }
-        const int p0x = rix >> rek, p0y = riy >> rek, p0z = riz >> rek;
-        const float m0x = __fsub_rn(int_to_float<kFast>((p0x + 1) << rek), rpx);
-        const float m0y = __fsub_rn(int_to_float<kFast>((p0y + 1) << rek), rpy);
-        const float m0z = __fsub_rn(int_to_float<kFast>((p0z + 1) << rek), rpz);
+        const float m0x = __fsub_rn(next_boundary<kFast>(rix, rek), rpx);
+        const float m0y = __fsub_rn(next_boundary<kFast>(riy, rek), rpy);
+        const float m0z = __fsub_rn(next_boundary<kFast>(riz, rek), rpz);
         float best = __fmul_rn(m0x, lx);
         const float idy_ = __fmul_rn(m0y, ly), idz_ = __fmul_rn(m0z, lz);
         float mm = m0x, gx = 1.0f, gy = g0y, gz = g0z;
