@@ -86,17 +86,23 @@ __device__ __forceinline__ NetPixel net_load(const FrameParams& P, const TargetB
     return px;
 }
 
+// Fast approximate arithmetic is enough here: the features are rounded to
+// bf16 before use, and inference and training compute them with this one
+// function.
+__device__ __forceinline__ float fast_len(float sq) { return sq * rsqrtf(fmaxf(sq, 1e-30f)); }
+
 __device__ __forceinline__ void net_compute(const FrameParams& P, int res_x, int res_y, int x, int y,
                                             const NetPixel& px, float f[8]) {
 #pragma unroll
     for (int i = 0; i < 8; ++i) f[i] = 0.0f;
+    const float ry = (float)res_y, inv_ry = __fdividef(1.0f, ry);
     {
-        const float d1x = ((float)(x - (res_x >> 1)) + 0.5f) * P.ray.fovx / (float)res_y;
-        const float d1y = ((float)(y - (res_y >> 1)) + 0.5f) * P.ray.fovy / (float)res_y;
-        const float dx = d1x * P.ray.mxx + d1y * P.ray.mxy + P.ray.mxz;
-        const float dy = d1x * P.ray.myx + d1y * P.ray.myy + P.ray.myz;
-        const float dz = d1x * P.ray.mzx + d1y * P.ray.mzy + P.ray.mzz;
-        f[7] = 0.5f + 0.5f * dy * rsqrtf(dx * dx + dy * dy + dz * dz);
+        const float d1x = __fmaf_rn((float)(x - (res_x >> 1)) + 0.5f, P.ray.fovx * inv_ry, 0.0f);
+        const float d1y = __fmaf_rn((float)(y - (res_y >> 1)) + 0.5f, P.ray.fovy * inv_ry, 0.0f);
+        const float dx = __fmaf_rn(d1x, P.ray.mxx, __fmaf_rn(d1y, P.ray.mxy, P.ray.mxz));
+        const float dy = __fmaf_rn(d1x, P.ray.myx, __fmaf_rn(d1y, P.ray.myy, P.ray.myz));
+        const float dz = __fmaf_rn(d1x, P.ray.mzx, __fmaf_rn(d1y, P.ray.mzy, P.ray.mzz));
+        f[7] = __fmaf_rn(0.5f * dy, rsqrtf(__fmaf_rn(dx, dx, __fmaf_rn(dy, dy, dz * dz))), 0.5f);
     }
     if (px.c == kEmptyPixel) {
         f[4] = 1.0f;
@@ -108,29 +114,29 @@ __device__ __forceinline__ void net_compute(const FrameParams& P, int res_x, int
     f[2] = (float)(bgrx & 255u) * (1.0f / 255.0f);
     const float4 q = px.q;
     const float ax = q.x - P.ray.px, ay = q.y - P.ray.py, az = q.z - P.ray.pz;
-    const float d = sqrtf(ax * ax + ay * ay + az * az);
-    f[3] = fminf(log2f(1.0f + d) * (1.0f / 16.0f), 1.0f);
-    const float ry = (float)res_y;
-    const float zc = ax * P.vz[0] + ay * P.vz[1] + az * P.vz[2];
+    const float d = fast_len(__fmaf_rn(ax, ax, __fmaf_rn(ay, ay, az * az)));
+    f[3] = fminf(__log2f(1.0f + d) * (1.0f / 16.0f), 1.0f);
+    const float zc = __fmaf_rn(ax, P.vz[0], __fmaf_rn(ay, P.vz[1], az * P.vz[2]));
     float sxc = 0.0f, syc = 0.0f;
     if (zc >= 0.05f) {
-        const float iz = ry / zc;
-        sxc = (ax * P.vx[0] + ay * P.vx[1] + az * P.vx[2]) * iz;
-        syc = (ax * P.vy[0] + ay * P.vy[1] + az * P.vy[2]) * iz;
+        const float iz = __fdividef(ry, zc);
+        sxc = __fmaf_rn(ax, P.vx[0], __fmaf_rn(ay, P.vx[1], az * P.vx[2])) * iz;
+        syc = __fmaf_rn(ax, P.vy[0], __fmaf_rn(ay, P.vy[1], az * P.vy[2])) * iz;
         const float ex = sxc + 0.5f * (float)res_x - ((float)x + 0.5f);
         const float ey = syc + 0.5f * ry - ((float)y + 0.5f);
-        f[6] = fminf(sqrtf(ex * ex + ey * ey), 1.0f);
+        f[6] = fminf(fast_len(__fmaf_rn(ex, ex, ey * ey)), 1.0f);
     }
     float m = 0.0f;
     if (P.have_prev_view) {
         m = 8.0f;
         const float bx = q.x - P.prev_pos[0], by = q.y - P.prev_pos[1], bz = q.z - P.prev_pos[2];
-        const float zp = bx * P.prev_vz[0] + by * P.prev_vz[1] + bz * P.prev_vz[2];
+        const float zp = __fmaf_rn(bx, P.prev_vz[0], __fmaf_rn(by, P.prev_vz[1], bz * P.prev_vz[2]));
         if (zp >= 0.05f && zc >= 0.05f) {
-            const float iz = ry / zp;
-            const float sxp = (bx * P.prev_vx[0] + by * P.prev_vx[1] + bz * P.prev_vx[2]) * iz;
-            const float syp = (bx * P.prev_vy[0] + by * P.prev_vy[1] + bz * P.prev_vy[2]) * iz;
-            m = fminf(sqrtf((sxc - sxp) * (sxc - sxp) + (syc - syp) * (syc - syp)), 8.0f);
+            const float iz = __fdividef(ry, zp);
+            const float sxp = __fmaf_rn(bx, P.prev_vx[0], __fmaf_rn(by, P.prev_vx[1], bz * P.prev_vx[2])) * iz;
+            const float syp = __fmaf_rn(bx, P.prev_vy[0], __fmaf_rn(by, P.prev_vy[1], bz * P.prev_vy[2])) * iz;
+            const float ddx = sxc - sxp, ddy = syc - syp;
+            m = fminf(fast_len(__fmaf_rn(ddx, ddx, ddy * ddy)), 8.0f);
         }
     }
     f[5] = m * 0.125f;
@@ -351,7 +357,7 @@ __global__ void __launch_bounds__(128, 1) k_net_probe(uint32_t* result) {
 // window is 64x32 positions (a 4-pixel halo for the four 3x3 layers), stored
 // as "positions" p = row*64 + col. Activations live in shared memory as
 // planes of 8 bf16 channels (16 bytes per position, positions consecutive),
-// with a zeroed guard of 128 positions before and after each plane.
+// with a zeroed guard of 16 positions before and after each plane.
 //
 // Layer l computes output rows [l+1, 31-l) -- (15-l) blocks of 128
 // consecutive positions -- as D[128 x 16] = sum over MMAs of A[128 x 16] *
@@ -359,25 +365,34 @@ __global__ void __launch_bounds__(128, 1) k_net_probe(uint32_t* result) {
 // p + dy*64 + dx, i.e. the same matrix descriptor shifted by that many
 // 16-byte rows (an implicit GEMM with no im2col copy). Positions whose column
 // wraps into the next row are computed and never used. Each block
-// accumulates into its own 16 columns of tensor memory; one thread issues all
-// MMAs of a layer and commits them to an mbarrier; the 16 warps then read the
-// accumulators back (warp w reads tensor-memory lanes 32*(w%4)..+31, the four
-// warps of a lane group split the blocks), add the bias, apply ReLU, zero the
-// positions outside the frame (the border padding) and store bf16 into the
-// other buffer. The last layer writes the outputs.
+// accumulates into its own 16 columns of tensor memory; four threads issue a
+// layer's MMAs (blocks round-robin), each committing to its own mbarrier.
+// Each group of four warps waits for its issuer's blocks only, reads their
+// accumulators back (warp w reads tensor-memory lanes 32*(w%4)..+31), adds
+// the bias, applies ReLU, zeroes the positions outside the frame (the border
+// padding) and stores bf16 into the other buffer. The last layer writes the
+// outputs.
+//
+// The 8-channel input planes are double-buffered: while the tensor core runs
+// a layer's MMAs, every thread computes a quarter of the next tile's input
+// features into the other input plane, so the feature loads and arithmetic
+// overlap the MMAs.
 constexpr int kNetTW = 64, kNetTH = 32, kNetPos = kNetTW * kNetTH;
-constexpr int kNetGuard = 128;
-constexpr int kNetPlaneBytes = (kNetPos + 2 * kNetGuard) * 16;  // 36864
+constexpr int kNetGuard = 16;
+constexpr int kNetPlaneBytes = (kNetPos + 2 * kNetGuard) * 16;  // 33280
 constexpr int kNetOutW = kNetTW - 8, kNetOutH = kNetTH - 8;      // 56 x 24
-constexpr int kNetSmemA = 0;                                     // 2 planes
+constexpr int kNetSmemA = 0;                                     // 2 planes (16 channels)
 constexpr int kNetSmemB = 2 * kNetPlaneBytes;                    // 2 planes
-constexpr int kNetSmemW = 4 * kNetPlaneBytes;                    // 32 x 512 B
+constexpr int kNetSmemX = 4 * kNetPlaneBytes;                    // 2 input planes (8 channels each)
+constexpr int kNetSmemW = 6 * kNetPlaneBytes;                    // 32 x 512 B
 constexpr int kNetSmemBias = kNetSmemW + kNetMmaTotal * 512;     // 52 floats
-constexpr int kNetSmemRgb = kNetSmemBias + 256;                  // 3 x 2048 floats
-constexpr int kNetSmemBytes = kNetSmemRgb + 3 * kNetPos * 4;      // 188672
+constexpr int kNetSmemBytes = kNetSmemBias + 256;                // 216320
 constexpr int kNetTmemCols = 256;
 constexpr int kNetThreads = 512;
 constexpr int kNetWarps = kNetThreads / 32;
+constexpr int kNetPer = kNetPos / kNetThreads;  // input positions per thread and tile (one per layer)
+constexpr int kNetIssuers = 4;                   // threads (lane 0 of warps 0-3) issuing each layer's MMAs
+static_assert(kNetPer == kNetLayers, "one slice of the next tile's input per layer");
 
 struct NetInferArgs {
     const uint16_t* packed;  // tensor-core weight image
@@ -401,12 +416,14 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
 }
 
 // All MMAs of layer L for the blocks of one tile (issued by one thread).
+// MMAs of blocks j0, j0 + jstep, ... (several threads issue a layer's blocks:
+// one issuing thread cannot feed the tensor core fast enough with N = 16).
 template <int L>
-__device__ __forceinline__ void net_issue_layer(uint32_t sbase, uint32_t tmem) {
+__device__ __forceinline__ void net_issue_layer(uint32_t sbase, uint32_t tmem, uint32_t x_off, int j0, int jstep) {
     constexpr int kMmas = net_mmas(L);
     constexpr int kBlocks = 15 - L;
     constexpr int kFirst = (L + 1) * kNetTW;
-    constexpr uint32_t kIn = (L & 1) ? kNetSmemA : kNetSmemB;
+    const uint32_t kIn = L == 0 ? x_off : ((L & 1) ? kNetSmemA : kNetSmemB);
     uint64_t ad[kMmas], bd[kMmas];
 #pragma unroll
     for (int m = 0; m < kMmas; ++m) {
@@ -422,16 +439,43 @@ __device__ __forceinline__ void net_issue_layer(uint32_t sbase, uint32_t tmem) {
         ad[m] = tc_desc(sbase + kIn + (uint32_t)((kNetGuard + kFirst + shift) * 16), (uint32_t)lbo, 128u);
         bd[m] = tc_desc(sbase + kNetSmemW + (uint32_t)((net_mma_base(L) + m) * 512), 128u, 256u);
     }
-    for (int j = 0; j < kBlocks; ++j) {
+    for (int j = j0; j < kBlocks; j += jstep) {
         // block j starts 128 positions (2048 bytes, 128 in the address field) later
 #pragma unroll
         for (int m = 0; m < kMmas; ++m) tc_mma(tmem + 16u * j, ad[m] + 128ull * j, bd[m], m > 0 ? 1u : 0u);
     }
 }
 
+// Input features of one slice of a tile: position p = tid + k * kNetThreads
+// of the window at image origin (wx, wy), written bf16 into input plane xoff.
+template <bool kPipeline>
+__device__ __forceinline__ void net_stage_input(const NetInferArgs& A, const FrameParams& P, uint8_t* smem,
+                                                uint32_t xoff, int wx, int wy, int k) {
+    const int p = threadIdx.x + k * kNetThreads;
+    const int gx = wx + (p & (kNetTW - 1)), gy = wy + (p >> 6);
+    float f[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) f[i] = 0.0f;
+    if (gx >= 0 && gx < A.w && gy >= 0 && gy < A.h) {
+        if (kPipeline) {
+            net_compute(P, A.w, A.h, gx, gy, net_load(P, A.B, gx, gy), f);
+        } else {
+            const size_t n = (size_t)A.w * A.h, ofs = (size_t)gy * A.w + gx;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) f[i] = __ldg(A.feat + i * n + ofs);
+        }
+    }
+    uint4 v;
+    v.x = pack_bf16x2(f[0], f[1]);
+    v.y = pack_bf16x2(f[2], f[3]);
+    v.z = pack_bf16x2(f[4], f[5]);
+    v.w = pack_bf16x2(f[6], f[7]);
+    *reinterpret_cast<uint4*>(smem + xoff + (kNetGuard + p) * 16) = v;
+}
+
 template <bool kPipeline>
 __global__ void __launch_bounds__(kNetThreads, 1) k_net_infer(NetInferArgs A) {
-    __shared__ uint64_t mbar;
+    __shared__ uint64_t mbar[kNetIssuers];  // issuer i's MMAs of a layer: blocks j = i (mod kNetIssuers)
     __shared__ uint32_t tmem_base_s;
     __shared__ FrameParams sP;
     uint8_t* smem = reinterpret_cast<uint8_t*>(svo_dsmem);
@@ -445,8 +489,8 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_infer(NetInferArgs A) {
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar)) : "memory");
+    if (tid < kNetIssuers) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[tid])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (kPipeline) {
@@ -454,7 +498,7 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_infer(NetInferArgs A) {
         uint32_t* dst = reinterpret_cast<uint32_t*>(&sP);
         for (int i = tid; i < (int)(sizeof(FrameParams) / 4); i += kNetThreads) dst[i] = src[i];
     }
-    // weights, biases; zero both activation buffers (guards included)
+    // weights, biases; zero every activation and input plane (guards included)
     {
         const uint4* src = reinterpret_cast<const uint4*>(A.packed);
         uint4* dst = reinterpret_cast<uint4*>(smem + kNetSmemW);
@@ -462,91 +506,63 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_infer(NetInferArgs A) {
         float* b = reinterpret_cast<float*>(smem + kNetSmemBias);
         for (int i = tid; i < kNetBias; i += kNetThreads) b[i] = A.bias[i];
         uint4* z = reinterpret_cast<uint4*>(smem);
-        for (int i = tid; i < 4 * kNetPlaneBytes / 16; i += kNetThreads) z[i] = make_uint4(0, 0, 0, 0);
+        for (int i = tid; i < 6 * kNetPlaneBytes / 16; i += kNetThreads) z[i] = make_uint4(0, 0, 0, 0);
+    }
+    __syncthreads();
+    // the first tile's input
+    int tile = blockIdx.x;
+    if (tile < A.tiles) {
+        const int wx = (tile % A.tiles_x) * kNetOutW - 4, wy = (tile / A.tiles_x) * kNetOutH - 4;
+#pragma unroll
+        for (int k = 0; k < kNetPer; ++k) net_stage_input<kPipeline>(A, sP, smem, kNetSmemX, wx, wy, k);
     }
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = tmem_base_s;
-    const uint32_t bar = smem_addr(&mbar);
+    // the warps of slice s (warp >> 2) read back blocks j = s (mod 4), which
+    // issuer s issued and committed to its own barrier
+    const uint32_t bar = smem_addr(&mbar[(warp >> 2) % kNetIssuers]);
     const float* bias = reinterpret_cast<const float*>(smem + kNetSmemBias);
-    float* rgb_in = reinterpret_cast<float*>(smem + kNetSmemRgb);
     uint32_t phase = 0;
     uint32_t fault = 0;
     bool aborted = false;  // block-uniform: an MMA wait timed out
+    int xb = 0;            // which input plane holds this tile's input
 
-    for (int tile = blockIdx.x; tile < A.tiles; tile += gridDim.x) {
+    for (; tile < A.tiles; tile += gridDim.x, xb ^= 1) {
         const int ox = (tile % A.tiles_x) * kNetOutW, oy = (tile / A.tiles_x) * kNetOutH;
         const int wx = ox - 4, wy = oy - 4;  // image position of window position 0
-        // ---- input features -> buffer B plane 0 (bf16) and rgb_in (rounded floats);
-        // every thread first issues the loads of all its positions
-        constexpr int kPer = kNetPos / kNetThreads;
-        NetPixel px[kPer];
-#pragma unroll
-        for (int k = 0; k < kPer; ++k) {
-            const int p = tid + k * kNetThreads;
-            const int gx = wx + (p & (kNetTW - 1)), gy = wy + (p >> 6);
-            px[k].c = kEmptyPixel;
-            if (kPipeline && gx >= 0 && gx < W && gy >= 0 && gy < H) px[k] = net_load(sP, A.B, gx, gy);
-        }
-#pragma unroll
-        for (int k = 0; k < kPer; ++k) {
-            const int p = tid + k * kNetThreads;
-            const int gx = wx + (p & (kNetTW - 1)), gy = wy + (p >> 6);
-            float f[8];
-            if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
-                if (kPipeline) {
-                    net_compute(sP, W, H, gx, gy, px[k], f);
-                } else {
-                    const size_t n = (size_t)W * H, ofs = (size_t)gy * W + gx;
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) f[i] = __ldg(A.feat + i * n + ofs);
-                }
-            } else {
-#pragma unroll
-                for (int i = 0; i < 8; ++i) f[i] = 0.0f;
-            }
-            uint4 v;
-            v.x = pack_bf16x2(f[0], f[1]);
-            v.y = pack_bf16x2(f[2], f[3]);
-            v.z = pack_bf16x2(f[4], f[5]);
-            v.w = pack_bf16x2(f[6], f[7]);
-            *reinterpret_cast<uint4*>(smem + kNetSmemB + (kNetGuard + p) * 16) = v;
-            rgb_in[p] = __uint_as_float(v.x << 16);
-            rgb_in[kNetPos + p] = __uint_as_float(v.x & 0xFFFF0000u);
-            rgb_in[2 * kNetPos + p] = __uint_as_float(v.y << 16);
-        }
-        fence_async_smem();
-        tc_fence_before();
-        __syncthreads();
-        tc_fence_after();
+        const uint32_t x_cur = kNetSmemX + (uint32_t)xb * kNetPlaneBytes;
+        const uint32_t x_next = kNetSmemX + (uint32_t)(xb ^ 1) * kNetPlaneBytes;
+        const int next = tile + (int)gridDim.x;
+        const int nwx = (next % A.tiles_x) * kNetOutW - 4, nwy = (next / A.tiles_x) * kNetOutH - 4;
 
         for (int l = 0; l < kNetLayers; ++l) {
             const int nb = 15 - l;
             const int first = (l + 1) * kNetTW;
             const uint32_t out_off = (l & 1) ? kNetSmemB : kNetSmemA;
-            if (tid == 0) {
+            if (lane == 0 && warp < kNetIssuers) {
                 tc_fence_after();
                 switch (l) {
-                    case 0: net_issue_layer<0>(sbase, tmem); break;
-                    case 1: net_issue_layer<1>(sbase, tmem); break;
-                    case 2: net_issue_layer<2>(sbase, tmem); break;
-                    default: net_issue_layer<3>(sbase, tmem); break;
+                    case 0: net_issue_layer<0>(sbase, tmem, x_cur, warp, kNetIssuers); break;
+                    case 1: net_issue_layer<1>(sbase, tmem, x_cur, warp, kNetIssuers); break;
+                    case 2: net_issue_layer<2>(sbase, tmem, x_cur, warp, kNetIssuers); break;
+                    default: net_issue_layer<3>(sbase, tmem, x_cur, warp, kNetIssuers); break;
                 }
-                tc_commit(bar);
+                tc_commit(smem_addr(&mbar[warp]));
             }
-            // every thread waits for the layer's MMAs (bounded); the verdict is
-            // made block-uniform before anyone reads tensor memory
-            aborted = __syncthreads_or(mbar_wait_phase(bar, phase) ? 0 : 1) != 0;
+            // while the MMAs run: one slice of the next tile's input
+            if (next < A.tiles) net_stage_input<kPipeline>(A, sP, smem, x_next, nwx, nwy, l);
+            // each warp waits (bounded) for the MMAs of its own blocks only, so the
+            // read-back of early blocks overlaps the MMAs of later ones
+            const bool ready = mbar_wait_phase(bar, phase);
             phase ^= 1u;
             tc_fence_after();
-            if (aborted) {
-                fault |= kFaultNet;
-                break;
-            }
             const int g = warp & 3;
-            if (l < kNetLayers - 1) {
+            if (!ready) {
+                // skip this warp's read-back; the block leaves after the barrier below
+            } else if (l < kNetLayers - 1) {
                 // the (at most 4) blocks of this warp: all loads in flight, one wait
                 constexpr int kSlices = kNetWarps / 4;
                 uint32_t r[4][16];
@@ -581,51 +597,54 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_infer(NetInferArgs A) {
                     const int p = first + 128 * j + 32 * g + lane;  // this thread's position
                     const int gx = wx + (p & (kNetTW - 1)), gy = wy + (p >> 6);
                     const bool inside = gx >= 0 && gx < W && gy >= 0 && gy < H;
-                    const uint32_t taddr = tmem + ((uint32_t)(32 * g) << 16) + 16u * j;
-                    {
-                        float v[4];
-                        tc_ld4(taddr, v);
-                        const int col = p & (kNetTW - 1);
-                        const bool out = inside && col >= 4 && col < 4 + kNetOutW;  // rows are 4..27 here
-                        const float r = v[0] + bias[48] + rgb_in[p];
-                        const float gg = v[1] + bias[49] + rgb_in[kNetPos + p];
-                        const float b = v[2] + bias[50] + rgb_in[2 * kNetPos + p];
-                        const float z = v[3] + bias[51];
-                        if (kPipeline) {
-                            bool req = false;
-                            if (out) {
-                                const size_t ofs = (size_t)gy * W + gx;
-                                const uint32_t ri = (uint32_t)__float2int_rn(fminf(fmaxf(r, 0.0f), 1.0f) * 255.0f);
-                                const uint32_t gi = (uint32_t)__float2int_rn(fminf(fmaxf(gg, 0.0f), 1.0f) * 255.0f);
-                                const uint32_t bi = (uint32_t)__float2int_rn(fminf(fmaxf(b, 0.0f), 1.0f) * 255.0f);
-                                A.B.bgrx[ofs] = bi + (gi << 8) + (ri << 16);
-                                req = !(z >= A.logit_threshold);
-                            }
-                            // Ray requests: bit (x&7) + 8*(y&3) of the pixel's 8x4 packet. The
-                            // warp's lanes are consecutive pixels of one row, so the first lane
-                            // of each run of one packet ORs the run's bits in one atomic.
-                            const uint32_t bal = __ballot_sync(0xffffffffu, req);
-                            if (bal && (lane == 0 || (gx & 7) == 0)) {
-                                const int len = min(8 - (gx & 7), 32 - lane);
-                                const uint32_t run = (bal >> lane) & ((1u << len) - 1u);
-                                if (run)
-                                    atomicOr(A.B.req_mask + (size_t)(gy >> 2) * A.B.packets_x + (gx >> 3),
-                                             run << ((gx & 7) + 8 * (gy & 3)));
-                            }
-                        } else if (out) {
-                            const size_t n = (size_t)W * H, ofs = (size_t)gy * W + gx;
-                            A.out[ofs] = r;
-                            A.out[n + ofs] = gg;
-                            A.out[2 * n + ofs] = b;
-                            A.out[3 * n + ofs] = z;
+                    float v[4];
+                    tc_ld4(tmem + ((uint32_t)(32 * g) << 16) + 16u * j, v);
+                    const int col = p & (kNetTW - 1);
+                    const bool out = inside && col >= 4 && col < 4 + kNetOutW;  // rows are 4..27 here
+                    // the residual colour: the bf16 input channels 0-2 of this position
+                    const uint2 in = *reinterpret_cast<const uint2*>(smem + x_cur + (kNetGuard + p) * 16);
+                    const float r = v[0] + bias[48] + __uint_as_float(in.x << 16);
+                    const float gg = v[1] + bias[49] + __uint_as_float(in.x & 0xFFFF0000u);
+                    const float b = v[2] + bias[50] + __uint_as_float(in.y << 16);
+                    const float z = v[3] + bias[51];
+                    if (kPipeline) {
+                        bool req = false;
+                        if (out) {
+                            const size_t ofs = (size_t)gy * W + gx;
+                            const uint32_t ri = (uint32_t)__float2int_rn(fminf(fmaxf(r, 0.0f), 1.0f) * 255.0f);
+                            const uint32_t gi = (uint32_t)__float2int_rn(fminf(fmaxf(gg, 0.0f), 1.0f) * 255.0f);
+                            const uint32_t bi = (uint32_t)__float2int_rn(fminf(fmaxf(b, 0.0f), 1.0f) * 255.0f);
+                            A.B.bgrx[ofs] = bi + (gi << 8) + (ri << 16);
+                            req = !(z >= A.logit_threshold);
                         }
+                        // Ray requests: bit (x&7) + 8*(y&3) of the pixel's 8x4 packet. The
+                        // warp's lanes are consecutive pixels of one row, so the first lane
+                        // of each run of one packet ORs the run's bits in one atomic.
+                        const uint32_t bal = __ballot_sync(0xffffffffu, req);
+                        if (bal && (lane == 0 || (gx & 7) == 0)) {
+                            const int len = min(8 - (gx & 7), 32 - lane);
+                            const uint32_t run = (bal >> lane) & ((1u << len) - 1u);
+                            if (run)
+                                atomicOr(A.B.req_mask + (size_t)(gy >> 2) * A.B.packets_x + (gx >> 3),
+                                         run << ((gx & 7) + 8 * (gy & 3)));
+                        }
+                    } else if (out) {
+                        const size_t n = (size_t)W * H, ofs = (size_t)gy * W + gx;
+                        A.out[ofs] = r;
+                        A.out[n + ofs] = gg;
+                        A.out[2 * n + ofs] = b;
+                        A.out[3 * n + ofs] = z;
                     }
                 }
             }
             fence_async_smem();
             tc_fence_before();
-            __syncthreads();
+            aborted = __syncthreads_or(ready ? 0 : 1) != 0;  // block-uniform verdict
             tc_fence_after();
+            if (aborted) {
+                fault |= kFaultNet;
+                break;
+            }
         }
         if (aborted) break;
     }
