@@ -11,10 +11,13 @@ fast-motion path (2 deg/frame yaw plus 0.05 x extent/frame translation).
     python sparse-voxel-octree-raycasting_gb300/train_net.py --frames 2048 \\
         --out sparse-voxel-octree-raycasting_gb300/net_weights.npy
 
-Writes the parameters (.npy) and a JSON report next to them: the training
-curve and, on the held-out path (another terrain seed), PSNR against the full
-raycast and the fraction of pixels traced, for the learned frames at several
-confidence thresholds and for the plain warp pipeline.
+After training, the confidence is calibrated on a third terrain seed: the
+confidence output's bias is shifted (bisection) so that threshold 0.5 reaches
+--calib-db on both camera paths. Writes the parameters (.npy) and a JSON
+report next to them: the training curve, the calibration shift and, on the
+held-out scene (another terrain seed), PSNR against the full raycast and the
+fraction of pixels traced, for the learned frames at several confidence
+thresholds and for the plain warp pipeline.
 """
 from __future__ import annotations
 
@@ -54,6 +57,9 @@ def parse_args(argv=None):
     ap.add_argument("--segment", type=int, default=128, help="frames per camera-path stretch")
     ap.add_argument("--epochs", type=int, default=1, help="passes over the --frames camera poses")
     ap.add_argument("--out", default=os.path.join(HERE, "net_weights.npy"))
+    ap.add_argument("--calib-seed", type=int, default=1234, help="terrain seed of the calibration scene")
+    ap.add_argument("--calib-db", type=float, default=38.5,
+                    help="calibrate the confidence so that threshold 0.5 reaches this PSNR on the calibration scene")
     return ap.parse_args(argv)
 
 
@@ -92,6 +98,55 @@ def evaluate(ctx, net, octree, W, H, frames, thresholds, kind=FAST_MOTION, log=p
         tgt.close()
     full.close()
     return res
+
+
+def path_psnr(ctx, net, depth, W, H, kind, frames, threshold=0.5):
+    """PSNR of learned frames against the full raycast over one camera path."""
+    tgt, full = ctx.target(W, H), ctx.target(W, H)
+    tgt.use_graph(True)
+    mse = []
+    for f in range(frames):
+        v = svo.camera_path(kind, depth, f, W, H)
+        ctx.warp_frame_learned(tgt, v, f, net, threshold)
+        if f >= 8:
+            ctx.raycast_full(full, v)
+            p = svo.psnr_bgrx(tgt.bgrx(), full.bgrx())
+            mse.append(255.0 ** 2 / 10 ** (p / 10) if np.isfinite(p) else 0.0)
+    tgt.close()
+    full.close()
+    m = float(np.mean(mse))
+    return 10 * np.log10(255.0 ** 2 / m) if m > 0 else float("inf")
+
+
+def calibrate(ctx, net, depth, W, H, target_db, frames=48, log=print):
+    """Shifts the confidence output's bias so that threshold 0.5 reaches
+    target_db on both camera paths of the (already uploaded) calibration
+    scene with as few rays as the search finds (bisection on the shift)."""
+    params = net.params()
+    base = float(params[-1])  # the last value is the confidence bias
+    lo, hi = -4.0, 2.0        # shift: lower -> lower confidence -> more rays
+
+    def ok(shift):
+        p = params.copy()
+        p[-1] = base + shift
+        net.set_params(p)
+        db = min(path_psnr(ctx, net, depth, W, H, ORBIT, frames), path_psnr(ctx, net, depth, W, H, FAST_MOTION, frames))
+        log(f"  confidence shift {shift:+.3f}: {db:.2f} dB")
+        return db >= target_db
+
+    if ok(hi):
+        lo = hi
+    else:
+        for _ in range(7):
+            mid = 0.5 * (lo + hi)
+            if ok(mid):
+                lo = mid
+            else:
+                hi = mid
+    p = params.copy()
+    p[-1] = base + lo
+    net.set_params(p)
+    return lo
 
 
 def main(argv=None):
@@ -141,6 +196,12 @@ def main(argv=None):
     tgt.set_feature_tap(None)
     tgt.close()
     full.close()
+    shift = None
+    if args.calib_db > 0:
+        print(f"calibration scene: seed {args.calib_seed}", flush=True)
+        octree_cal = svo.build_terrain(args.depth, args.calib_seed, shell=True)
+        ctx.upload(octree_cal)
+        shift = calibrate(ctx, net, args.depth, W, H, args.calib_db)
     params = net.params()
     np.save(args.out, params)
 
@@ -151,7 +212,7 @@ def main(argv=None):
     for name, kind in (("orbit", ORBIT), ("fast_motion", FAST_MOTION)):
         print(f" {name}:", flush=True)
         evals[name] = evaluate(ctx, net, octree_eval, W, H, args.eval_frames, [0.3, 0.4, 0.5, 0.6, 0.7], kind)
-    report = {"args": vars(args), "train_seconds": train_s, "curve": curve, "eval": evals}
+    report = {"args": vars(args), "train_seconds": train_s, "confidence_shift": shift, "curve": curve, "eval": evals}
     with open(os.path.splitext(args.out)[0] + ".json", "w") as fh:
         json.dump(report, fh, indent=1)
     net.close()
