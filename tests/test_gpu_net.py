@@ -202,7 +202,7 @@ def test_trained_net_gains_over_the_method_without_it(svo, gpu_ctx):
     p_plain, f_plain = _learned_quality(svo, gpu_ctx, None, octree, W, H, 0.5)
     print(f"trained: {p_tr:.2f} dB, {100 * f_tr:.1f}% traced; plain: {p_plain:.2f} dB, {100 * f_plain:.1f}% traced")
     assert p_tr > p_plain + 4.0, (p_tr, p_plain)
-    assert p_tr > 34.0 and f_tr < 0.85, (p_tr, f_tr)
+    assert p_tr > 34.0 and f_tr < 0.9, (p_tr, f_tr)
     untrained = gpu_ctx.net(seed=3)
     p_un, f_un = _learned_quality(svo, gpu_ctx, untrained, octree, W, H, 0.5)
     print(f"untrained: {p_un:.2f} dB, {100 * f_un:.1f}% traced")
