@@ -721,6 +721,9 @@ struct DevScratch {
     ~DevScratch() {
         for (void* p : ptrs) cudaFree(p);
     }
+    void release(const void* p) {
+        ptrs.erase(std::remove(ptrs.begin(), ptrs.end(), p), ptrs.end());
+    }
     template <class T>
     cudaError_t get(T** p, size_t count) {
         void* q = nullptr;
@@ -919,7 +922,7 @@ svo_status svo_octree_build(svo_context* ctx, const uint32_t* d_x, const uint32_
     uint32_t root = 0;
     if (n == 0) {
         // empty scene: an all-zero root node with no children
-        SVO_CUDA(ctx, cudaMalloc(&words, initial_words * 4));
+        SVO_CUDA(ctx, S.get(&words, initial_words));
         SVO_CUDA(ctx, cudaMemsetAsync(words, 0, initial_words * 4, s));
     } else {
         int ib = 1;
@@ -1022,7 +1025,7 @@ svo_status svo_octree_build(svo_context* ctx, const uint32_t* d_x, const uint32_
             return fail(ctx, SVO_ERR_CAPACITY, "normal nodes do not fit into initial_words (10 words each)");
         if (total_words >= 0xffffffc0ull || (base >> 6) + ((uint64_t)last_off >> 6) >= (1ull << 23))
             return fail(ctx, SVO_ERR_CAPACITY, "octree exceeds the compact format's 23-bit offsets");
-        SVO_CUDA(ctx, cudaMalloc(&words, total_words * 4));
+        SVO_CUDA(ctx, S.get(&words, total_words));
         SVO_CUDA(ctx, cudaMemsetAsync(words, 0, total_words * 4, s));
         // ---- blocks, top-down
         for (int h = 5; h >= 2; --h) {
@@ -1073,7 +1076,6 @@ svo_status svo_octree_build(svo_context* ctx, const uint32_t* d_x, const uint32_
         SVO_CUDA(ctx, cudaMemcpyAsync(&flags_host, bad, 4, cudaMemcpyDeviceToHost, s));
         SVO_CUDA(ctx, cudaStreamSynchronize(s));
         if (flags_host) {
-            cudaFree(words);
             if (flags_host & 1u) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "voxel coordinate outside the volume");
             if (flags_host & 4u) return fail(ctx, SVO_ERR_CUDA, "builder: store outside the word array");
             return fail(ctx, SVO_ERR_CAPACITY, "octree exceeds the compact format's 23-bit offsets");
@@ -1081,6 +1083,7 @@ svo_status svo_octree_build(svo_context* ctx, const uint32_t* d_x, const uint32_
         root = ((uint32_t)(10 * (n_normal - 1)) << 9) | root_mask;
     }
     SVO_CUDA(ctx, cudaStreamSynchronize(s));
+    S.release(words);  // the words outlive the scratch: they become the context's octree
     if (ctx->owns_octree && ctx->d_octree) cudaFree(ctx->d_octree);
     ctx->d_octree = words;
     ctx->owns_octree = true;
