@@ -19,6 +19,8 @@ def _full_oracle(orc, octree, view):
     (9, True, 1, 256, 128, 1.0),
     (8, False, 3, 200, 152, 1.0),
     (9, False, 0, 512, 512, 1.1547),   # the plain full raycast configuration: 512^2, depth 9, solid terrain
+    (10, True, 2, 160, 96, 1.0),
+    (12, True, 1, 128, 80, 1.0),       # the deepest supported octree (4096^3)
 ])
 def test_full_raycast_bit_exact(svo, orc, scene, gpu_ctx, depth, shell, kind, W, H, fov):
     octree = scene(depth, 1234, shell)
@@ -41,6 +43,7 @@ def test_full_raycast_bit_exact(svo, orc, scene, gpu_ctx, depth, shell, kind, W,
     (8, True, 1, 128, 96, 40),    # covers a whole 8x4 refresh cycle
     (9, True, 2, 200, 120, 12),   # ragged: 200x120 is not a multiple of 16
     (8, False, 1, 96, 64, 6),
+    (12, True, 2, 96, 64, 6),     # depth 12
 ])
 def test_warp_frames_bit_exact(svo, orc, scene, gpu_ctx, depth, shell, kind, W, H, frames):
     octree = scene(depth, 99, shell)
