@@ -61,6 +61,8 @@ def parse_args(argv=None):
     ap.add_argument("--views", type=int, default=8, help="camera streams of the concurrent multi-view measurement")
     ap.add_argument("--threshold", type=float, default=0.5, help="confidence below which learned frames trace a pixel")
     ap.add_argument("--autotune", type=int, default=1, help="pick the trace configuration by measurement first")
+    ap.add_argument("--guided", type=int, default=1,
+                    help="learned frames walk pixels with a cached surface nearby from just in front of it")
     ap.add_argument("--extras", type=int, default=1,
                     help="also measure the GPU octree builder, the 64-view batch and the large depth-12 scene")
     ap.add_argument("--weights", default=os.path.join(ROOT, "sparse-voxel-octree-raycasting_gb300", "net_weights.npy"))
@@ -287,6 +289,7 @@ def measure_large(svo, torch, args, device, frames=16, views=8):
         cx.upload_device(d_words.data_ptr(), nw, root, depth)
         t = cx.target(W, H)
         t.use_graph(True)
+        t.set_guided(bool(args.guided))
         net = svo.Net(cx)
         net.load_file(args.weights)
         ctxs.append(cx)
@@ -327,6 +330,7 @@ def measure_large(svo, torch, args, device, frames=16, views=8):
     out["full_frames_per_s_one_view"] = 4 / (time.perf_counter() - t0)
     # learned quality on view 0
     tq = ctxs[0].target(W, H)
+    tq.set_guided(bool(args.guided))
     mse = []
     for f in range(0, 12):
         v = vw(0, f)
@@ -367,6 +371,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     net.load_file(args.weights)
     thr = args.threshold
     tgt, tgt_l, full = ctx.target(W, H), ctx.target(W, H), ctx.target(W, H)
+    tgt_l.set_guided(bool(args.guided))
     if args.graph:
         tgt.use_graph(True)
         tgt_l.use_graph(True)
@@ -389,6 +394,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
         return lambda f, v: ctx.warp_frame(t, v, f)
 
     def learned(t, th=thr):
+        t.set_guided(bool(args.guided))
         return lambda f, v: ctx.warp_frame_learned(t, v, f, net, th)
 
     def timed(render, kind=1):
@@ -491,6 +497,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     # ---- end to end through the C ABI with host buffers (learned frames)
     host_img = torch.empty(W * H, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
     tgt3 = ctx.target(W, H)
+    tgt3.set_guided(bool(args.guided))
     if args.graph:
         tgt3.use_graph(True)
     for f in range(args.warmup):
@@ -508,8 +515,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     tgt3.close()
 
     # ---- quality against the full raycast of the same cameras
-    def quality(render, t, kind, traced_of):
-        mse, traced, worst = [], [], []
+    def quality(render, t, kind, traced_of, walked=False):
+        mse, traced, worst, walk = [], [], [], []
         for f in range(args.warmup + args.steps):
             v = view(f, kind)
             render(f, v)
@@ -521,15 +528,20 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                 mse.append(float((d.astype(np.float64) ** 2).mean()))
                 worst.append(int(np.abs(d).max()))
                 traced.append(traced_of(t) / (W * H))
+                if walked:
+                    walk.append(float((t.guide() >= 0).mean()))
         m = float(np.mean(mse))
-        return {"psnr_db": 10 * np.log10(255.0 ** 2 / m) if m > 0 else float("inf"),
-                "max_abs_error": int(max(worst)), "traced_fraction": float(np.mean(traced))}
+        out = {"psnr_db": 10 * np.log10(255.0 ** 2 / m) if m > 0 else float("inf"),
+               "max_abs_error": int(max(worst)), "traced_fraction": float(np.mean(traced))}
+        if walked:
+            out["walked_fraction"] = float(np.mean(walk))
+        return out
 
     tq = ctx.target(W, H)
     q_plain = quality(plain(tq), tq, 1, lambda t: t.holes()[1])
     tq.close()
     tq = ctx.target(W, H)
-    q_learned = quality(learned(tq), tq, 1, lambda t: t.requested())
+    q_learned = quality(learned(tq), tq, 1, lambda t: t.requested(), bool(args.guided))
     tq.close()
     # fast motion (2 deg/frame + 0.05 extent/frame), the learned configuration
     tq = ctx.target(W, H)
@@ -538,7 +550,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     fast_ms = timed(learned(tq), kind=2)
     tq.close()
     tq = ctx.target(W, H)
-    q_fast = quality(learned(tq), tq, 2, lambda t: t.requested())
+    q_fast = quality(learned(tq), tq, 2, lambda t: t.requested(), bool(args.guided))
     tq.close()
     tq = ctx.target(W, H)
     q_fast_plain = quality(plain(tq), tq, 2, lambda t: t.holes()[1])
@@ -571,6 +583,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
             c = svo.Context(local_rank)
             c.upload_device(d_words.data_ptr(), octree.words.size, octree.root, octree.depth)
             t = c.target(W, H)
+            t.set_guided(bool(args.guided))
             n = svo.Net(c)
             n.load_file(args.weights)
             if args.graph:
@@ -691,6 +704,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
             "config": {"workload": WORKLOAD, "res": [W, H], "depth": depth, "seed": args.seed,
                        "octree_words": int(octree.words.size), "voxels": int(octree.voxels),
                        "confidence_threshold": thr, "weights": os.path.relpath(args.weights, ROOT),
+                       "guided_walks": bool(args.guided),
                        "l2": "flushed before every timed step (256 MiB device write, outside the step events)",
                        "cuda_graph": bool(args.graph), "replicas": world},
             "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": 4 * 33,

@@ -265,6 +265,20 @@ svo_status svo_warp_frame_learned(svo_context* ctx, svo_target* t, const svo_vie
                                   const svo_net* net, float threshold);
 /* Rays the net requested in the target's last learned frame (synchronises). */
 svo_status svo_read_requested(svo_target* t, uint32_t* count);
+/* Guided learned frames (enable = 1): after reprojection, every pixel with a
+ * cached surface point in its 3x3 neighbourhood is walked from just in front
+ * of the nearest such point (4 cells of the level of detail at that
+ * distance) instead of from the camera -- the same walk, started late, so it
+ * finds the same voxel unless a surface the cache never saw lies in front of
+ * the start. Only the remaining (unguided) pixels go to the net, which runs
+ * on the 56x24 tiles that hold one; those below `threshold` are traced from
+ * the camera, as is the refresh tile. Learned frames also re-base cached
+ * points across wraps of the camera into the periodic volume
+ * (src/raycast.h:136-145). enable = 0: every pixel goes to the net. */
+svo_status svo_target_set_guided(svo_target* t, int enable);
+/* The start distances of the last guided frame, res_x*res_y floats in raypos
+ * units (16 per world unit; 0 = from the camera, -1 = unguided). */
+svo_status svo_read_guide(svo_target* t, float* host);
 /* Training tap: when d_features is not NULL, every later frame of the target
  * (plain or learned) writes the net's input features after reprojection to
  * this device buffer, planar [8][res_y*res_x] FP32. */

@@ -54,6 +54,7 @@ def oracle() -> ctypes.CDLL:
         lib.orc_octree_free.argtypes = [_P]
         lib.orc_raycast_full.argtypes = [i, _P, sz, u32, _P, _P, i, i, ctypes.c_float, ctypes.c_float, _P, _P, _P,
                                          _P, i]
+        lib.orc_raycast_guided.argtypes = [i, _P, sz, u32, _P, _P, i, i, _P, _P, _P, i]
         lib.orc_warp_create.restype = _P
         lib.orc_warp_create.argtypes = [i, i]
         lib.orc_warp_free.argtypes = [_P]
@@ -149,6 +150,25 @@ def raycast_full(depth, words, root, pos, m, res_x, res_y, fovx=1.0, fovy=1.0, t
     if rc != 0:
         raise RuntimeError(f"ref_raycast_full failed: {rc}")
     return col, xyzw.reshape(n, 4), None, None
+
+
+def raycast_guided(depth, words, root, pos, m, res_x, res_y, s0, threads=0):
+    """Guided walks (the product's learned frames): pixel o's ray starts at
+    s0[o] raypos units (0: from the camera; < 0: not traced, colour left at
+    the empty word and xyzw at 0). Returns colour words and float4 per pixel."""
+    words = np.ascontiguousarray(words, np.uint32)
+    pos = np.ascontiguousarray(pos, np.float32)
+    m = np.ascontiguousarray(m, np.float32)
+    s0 = np.ascontiguousarray(s0, np.float32)
+    n = res_x * res_y
+    assert s0.size == n
+    col = np.full(n, 0xFFFFFF00, np.uint32)
+    xyzw = np.zeros(n * 4, np.float32)
+    rc = oracle().orc_raycast_guided(depth, _ptr(words), words.size, root, _ptr(pos), _ptr(m), res_x, res_y, _ptr(s0),
+                                     _ptr(col), _ptr(xyzw), threads)
+    if rc != 0:
+        raise RuntimeError(f"orc_raycast_guided failed: {rc}")
+    return col, xyzw.reshape(n, 4)
 
 
 class Warp:

@@ -270,7 +270,12 @@ struct Tracer {
 
     // Ray setup of raycast_fine_2 / raycast_holes (kernel.cl:883-899, 639-655)
     // followed by CAST_RAY (kernel.cl:114-214) and the colour fetch (:911-921).
-    Ray trace(const View& v, int idx, int idy, int res_x, int res_y, float fovx, float fovy) const {
+    // s0 > 0 (the product's guided walks, not in the reference): the walk
+    // starts s0 raypos units along the ray -- at most up to 16 units before
+    // the ray leaves the volume's height -- at camera + s0 * d/|d| in the
+    // mirrored frame, with the distance at s0 and the level of detail
+    // advanced over the lodswitch doublings below s0 (at most to the depth).
+    Ray trace(const View& v, int idx, int idy, int res_x, int res_y, float fovx, float fovy, float s0 = 0.0f) const {
         Ray r{};
         const int scale_max = 1 << (depth + 1);
         const int depth_and = (1 << depth) - 1;
@@ -300,10 +305,25 @@ struct Tracer {
         float len[3];
         for (int a = 0; a < 3; ++a) len[a] = std::sqrt(dot3(g[a], g[a]));
 
-        int rpi[3] = {(int)rp[0], (int)rp[1], (int)rp[2]};
-        int rek = depth, lod = 1;
+        int lod = 1;
         float lodswitch = (float)(res_x * 1 * 2);  // LOD_ADJUST=1, kernel.cl:908
         float distance = 0.0f;
+        if (s0 > 0.0f) {  // not past the ray's exit through the volume's top (16 raypos units margin)
+            const float nd = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            const float t_top = (((float)scale_max - rp[1]) / d[1]) * nd;
+            s0 = std::fmin(s0, t_top - 16.0f);
+        }
+        if (s0 > 0.0f) {
+            const float nd = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            for (int a = 0; a < 3; ++a) rp[a] = rp[a] + (d[a] / nd) * s0;
+            distance = s0;
+            while (distance > lodswitch && lod < depth) {
+                lodswitch *= 2.0f;
+                ++lod;
+            }
+        }
+        int rpi[3] = {(int)rp[0], (int)rp[1], (int)rp[2]};
+        int rek = depth;
         uint32_t nodeid = root, nodeid_before = root, local_root = 0, node_test = 0;
         uint32_t sign_xyz = (uint32_t)(sgn[0] | (sgn[1] << 1) | (sgn[2] << 2));
         int x0ry = 0;
@@ -648,6 +668,33 @@ int orc_raycast_full(int depth, const uint32_t* words, size_t n_words, uint32_t 
         stats[4] = steps;
         stats[5] = max_steps;
     }
+    return 0;
+}
+
+// Guided walks over the whole frame: pixel o starts at s0[o] raypos units
+// (0: from the camera); pixels with s0[o] < 0 are not traced (outputs left
+// as they are).
+int orc_raycast_guided(int depth, const uint32_t* words, size_t n_words, uint32_t root, const float* pos4,
+                       const float* m16, int res_x, int res_y, const float* s0, uint32_t* colour, float* xyzw,
+                       int threads) {
+    if (res_x <= 0 || res_y <= 0 || res_x > 65535 || res_y > 65535 || !s0) return -1;
+    Tracer tr{words, n_words, root, depth};
+    View v = make_view(pos4, m16);
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int y = 0; y < res_y; ++y)
+        for (int x = 0; x < res_x; ++x) {
+            size_t o = (size_t)y * res_x + x;
+            if (s0[o] < 0.0f) continue;
+            Ray r = tr.trace(v, x, y, res_x, res_y, 1.0f, 1.0f, s0[o]);
+            if (colour) colour[o] = r.colour;
+            if (xyzw) {
+                xyzw[o * 4 + 0] = r.hit[0];
+                xyzw[o * 4 + 1] = r.hit[1];
+                xyzw[o * 4 + 2] = r.hit[2];
+                xyzw[o * 4 + 3] = r.dist;
+            }
+        }
     return 0;
 }
 

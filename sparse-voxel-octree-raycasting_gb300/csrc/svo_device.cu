@@ -65,6 +65,7 @@ struct FrameGraph {
     float threshold = 0.0f;
     float* tap = nullptr;
     bool coarse = false;
+    bool guided = false;
     uint64_t config_gen = 0;
     void reset() {
         if (exec) cudaGraphExecDestroy(exec);
@@ -99,6 +100,12 @@ struct svo_target {
     bool have_prev_view = false;
     float* feature_tap = nullptr;  // device [8][N]: features written after reprojection
     uint32_t* req_offs = nullptr;  // learned frames: request offsets per 8x4 packet
+    // guided learned frames (walks from the cached depth); buffers in B
+    bool guided = false;
+    float* d_guide = nullptr;
+    // camera position each physical plane's points were written under (the
+    // rebase of learned frames across wraps of the periodic volume)
+    float plane_pos[3][3] = {};
     // CUDA graphs of one warp frame: [0] plain, [1] learned
     bool use_graph = false;
     FrameGraph graphs[2];
@@ -420,13 +427,22 @@ PlanePlan plan_planes(const svo_target* t, int frame, bool have_cache, int mode)
     return q;
 }
 
-void commit_planes(svo_target* t, const PlanePlan& q) {
+void commit_planes(svo_target* t, const PlanePlan& q, const svo_view& v) {
+    for (int i = 0; i < 3; ++i) t->plane_pos[q.cur][i] = v.pos[i];
     t->last_cur = q.cur;
     t->other = q.other_after;
     t->last_target = q.target;
 }
 
-FrameParams make_params(const svo_target* t, const svo_view& v, int frame, const PlanePlan& q, bool have_cache) {
+// Whole periods (of length e) between two wrapped camera positions: a point
+// written under camera a lies at point + shift under camera b, assuming the
+// camera moved less than half a period between the two.
+void period_shift(const float* a, const float* b, float e, float out[3]) {
+    for (int i = 0; i < 3; ++i) out[i] = (float)std::nearbyint(((double)b[i] - (double)a[i]) / e) * e;
+}
+
+FrameParams make_params(const svo_target* t, const svo_view& v, int frame, const PlanePlan& q, bool have_cache,
+                        bool learned = false) {
     FrameParams p{};
     p.ray = make_raycam(v);
     for (int i = 0; i < 3; ++i) {
@@ -458,6 +474,18 @@ FrameParams make_params(const svo_target* t, const svo_view& v, int frame, const
         p.prev_vx[i] = t->prev_view.m[0 + i];
         p.prev_vy[i] = t->prev_view.m[4 + i];
         p.prev_vz[i] = t->prev_view.m[8 + i];
+    }
+    p.serial = (uint32_t)(t->frames + 1);
+    if (learned) {
+        const float period = (float)(1u << (t->ctx->depth + 1)) / 16.0f;  // world units
+        p.rebase = 1;
+        for (int r = 0; r < 2; ++r)
+            if (q.src[r] >= 0) period_shift(t->plane_pos[q.src[r]], v.pos, period, p.src_shift[r]);
+        if (t->have_prev_view) {
+            float sh[3];
+            period_shift(t->prev_view.pos, v.pos, period, sh);
+            for (int i = 0; i < 3; ++i) p.prev_pos[i] = t->prev_view.pos[i] + sh[i];
+        }
     }
     return p;
 }
@@ -542,6 +570,11 @@ svo_status enqueue_learned_body(svo_context* ctx, svo_target* t, const svo_net* 
         k_net_features<<<dim3((res_x + 31) / 32, (res_y + 7) / 8), 256, 0, s>>>(t->d_params, t->B, t->feature_tap);
         SVO_LAUNCHED(ctx);
     }
+    if (t->B.guide) {
+        k_guide<<<dim3((res_x + kGuideBW - 1) / kGuideBW, (res_y + kGuideBH - 1) / kGuideBH), kGuideBW * kGuideBH, 0,
+                  s>>>(t->d_params, t->B);
+        SVO_LAUNCHED(ctx);
+    }
     record(t, 2);
     NetInferArgs A{};
     A.P = t->d_params;
@@ -578,7 +611,7 @@ svo_status run_frame(svo_context* ctx, svo_target* t, const FrameParams& p, Fram
         return body();
     }
     if (!g.exec || g.profiled != t->profiling || g.net != net || g.threshold != threshold || g.tap != t->feature_tap ||
-        g.coarse != t->coarse || g.config_gen != ctx->config_gen) {
+        g.coarse != t->coarse || g.guided != t->guided || g.config_gen != ctx->config_gen) {
         g.reset();
         const uint64_t l0 = ctx->launches;
         SVO_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
@@ -616,6 +649,7 @@ svo_status run_frame(svo_context* ctx, svo_target* t, const FrameParams& p, Fram
         g.threshold = threshold;
         g.tap = t->feature_tap;
         g.coarse = t->coarse;
+        g.guided = t->guided;
         g.config_gen = ctx->config_gen;
     }
     cudaKernelNodeParams kp;
@@ -1185,6 +1219,10 @@ svo_status svo_target_create(svo_context* ctx, int res_x, int res_y, svo_target*
     const size_t packets = (size_t)t->B.packets_x * t->B.packets_y;
     A((void**)&t->B.req_mask, packets * 4);
     A((void**)&t->req_offs, (packets + (packets + kReqBlock - 1) / kReqBlock) * 4);  // offsets + block totals
+    const size_t net_tiles = (size_t)((res_x + kNetOutW - 1) / kNetOutW) * ((res_y + kNetOutH - 1) / kNetOutH);
+    A((void**)&t->d_guide, N * 4);
+    A((void**)&t->B.net_flags, net_tiles * 4);
+    A((void**)&t->B.net_list, net_tiles * 4);
     A((void**)&t->B.counters, 64);
     A((void**)&t->d_params, sizeof(FrameParams));
     A((void**)&t->full_col, N * 4);
@@ -1205,6 +1243,7 @@ svo_status svo_target_create(svo_context* ctx, int res_x, int res_y, svo_target*
     SVO_CUDA(ctx, cudaMemsetAsync(t->B.ids, 0, (N + 2 * t->tiles + 4) * 4, s));
     SVO_CUDA(ctx, cudaMemsetAsync(t->B.tile_mask, 0, (t->tiles + 1) * 8, s));
     SVO_CUDA(ctx, cudaMemsetAsync(t->B.req_mask, 0, packets * 4, s));
+    SVO_CUDA(ctx, cudaMemsetAsync(t->B.net_flags, 0, net_tiles * 4, s));
     SVO_CUDA(ctx, cudaMemsetAsync(t->B.counters, 0, 64, s));
     SVO_CUDA(ctx, cudaMemsetAsync(t->B.bgrx, 0, N * 4, s));
     SVO_CUDA(ctx, cudaMemsetAsync(t->B.disp, 0xff, N * 4, s));
@@ -1223,7 +1262,7 @@ svo_status svo_target_destroy(svo_target* t) {
     for (auto& g : t->graphs) g.reset();
     void* ptrs[] = {t->B.col[0], t->B.col[1], t->B.col[2], t->B.xyz[0], t->B.xyz[1], t->B.xyz[2], t->B.disp, t->B.bgrx, t->B.keys, t->B.ids,
                     t->B.tile_mask, t->B.counters, t->d_params, t->full_col, t->full_xyzw, t->full_vox,
-                    t->B.req_mask, t->req_offs};
+                    t->B.req_mask, t->req_offs, t->d_guide, t->B.net_flags, t->B.net_list};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (auto& e : t->ev)
@@ -1400,7 +1439,7 @@ svo_status svo_warp_frame(svo_context* ctx, svo_target* t, const svo_view* view,
         t->n_events = 7;
         t->last_mode = 1;
     }
-    commit_planes(t, q);
+    commit_planes(t, q, *view);
     t->have_prev = true;
     t->prev_view = *view;
     t->have_prev_view = true;
@@ -1423,14 +1462,14 @@ svo_status svo_warp_frame_learned(svo_context* ctx, svo_target* t, const svo_vie
     const bool have_cache = frame >= 2 && t->have_prev;
     // learned frames keep one cache plane (the current plane of the last frame)
     const PlanePlan q = plan_planes(t, frame, have_cache, 0);
-    FrameParams p = make_params(t, *view, frame, q, have_cache);
+    FrameParams p = make_params(t, *view, frame, q, have_cache, true);
     st = run_frame(ctx, t, p, t->graphs[1], net, threshold, [&] { return enqueue_learned_body(ctx, t, net, logit); });
     if (st != SVO_OK) return st;
     if (t->profiling) {
         t->n_events = 5;
         t->last_mode = 3;
     }
-    commit_planes(t, q);
+    commit_planes(t, q, *view);
     t->have_prev = true;
     t->prev_view = *view;
     t->have_prev_view = true;
@@ -1720,6 +1759,18 @@ svo_status svo_target_set_cache_mode(svo_target* t, int mode) {
     if (!t || mode < 0 || mode > 1) return SVO_ERR_INVALID_ARGUMENT;
     t->cache_mode = mode;
     return SVO_OK;
+}
+
+svo_status svo_target_set_guided(svo_target* t, int enable) {
+    if (!t) return SVO_ERR_INVALID_ARGUMENT;
+    t->guided = enable != 0;
+    t->B.guide = t->guided ? t->d_guide : nullptr;
+    return SVO_OK;
+}
+
+svo_status svo_read_guide(svo_target* t, float* host) {
+    if (!t || !host) return SVO_ERR_INVALID_ARGUMENT;
+    return read_back(t, host, t->d_guide, t->N * 4);
 }
 
 svo_status svo_target_set_coarse_refresh(svo_target* t, int enable) {

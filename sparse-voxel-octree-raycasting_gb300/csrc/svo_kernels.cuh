@@ -44,6 +44,13 @@ struct FrameParams {
     // previous frame's camera (the reconstruction net's motion feature)
     float prev_pos[3], prev_vx[3], prev_vy[3], prev_vz[3];
     int have_prev_view;
+    // Learned frames: the camera wraps into the periodic volume, so a cache
+    // plane written under an earlier wrap holds points one period off. rebase
+    // adds src_shift[r] (whole periods) to the points of source plane r as
+    // they are reprojected; plain frames keep the reference's behaviour.
+    int rebase;
+    float src_shift[2][3];
+    uint32_t serial;  // frame serial of the target (stamps the net tile flags)
 };
 
 // Buffers of one render target.
@@ -57,7 +64,15 @@ struct TargetBuffers {
     uint64_t* tile_mask;  // per 16x16 tile, bit j*8+i = 2x2 block (i,j) empty
     uint32_t* req_mask;   // learned frames: per 8x4 packet, bit (x&7)+8*(y&3) = ray requested
     int packets_x, packets_y;  // ceil(res/8), ceil(res/4)
-    uint32_t* counters;   // [0] trace work counter, [1] hole entries, [2] coarse-pass work counter
+    // Guided learned frames: per pixel, the start distance of its walk in
+    // raypos units (>= 0) or -1 (unguided: the net decides); per net output
+    // tile, the serial of the last frame that needed the net there, and the
+    // list of those tiles (count in counters[3]). guide == nullptr: no walks.
+    float* guide;
+    uint32_t* net_flags;
+    uint32_t* net_list;
+    uint32_t* counters;   // [0] trace work counter, [1] hole entries, [2] coarse-pass work counter,
+                          // [3] net tiles listed
     int res_x, res_y;
     int tiles_x, tiles_y;  // whole 16x16 tiles (res/16)
 };
@@ -95,6 +110,7 @@ __global__ void k_set_params(FrameParams p, FrameParams* dst, uint32_t* counters
     counters[0] = 0;
     counters[1] = 0;
     counters[2] = 0;
+    counters[3] = 0;
 }
 
 __global__ void k_reset_counter(uint32_t* counter) { *counter = 0; }
@@ -140,15 +156,22 @@ __global__ void __launch_bounds__(256) k_project(const FrameParams* __restrict__
     const float hx = (float)res_x / 2.0f, hy = (float)res_y / 2.0f;
     const float fry = (float)res_y;
     const bool clear = P->clear_rejected != 0;
+    const bool rebase = P->rebase != 0;
     for (int r = 0; r < 2; ++r) {
         const int phys = P->src_plane[r];
         if (phys < 0) continue;
         uint32_t* __restrict__ col = plane_col(B, phys);
         const float4* __restrict__ xyz = plane_xyz(B, phys);
+        const float shx = P->src_shift[r][0], shy = P->src_shift[r][1], shz = P->src_shift[r][2];
         for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += gridDim.x * blockDim.x) {
             const uint32_t c = col[s];
             if (c == kEmptyPixel) continue;
-            const float4 q = __ldg(xyz + s);
+            float4 q = __ldg(xyz + s);
+            if (rebase) {
+                q.x = __fadd_rn(q.x, shx);
+                q.y = __fadd_rn(q.y, shy);
+                q.z = __fadd_rn(q.z, shz);
+            }
             const float ax = __fsub_rn(q.x, px), ay = __fsub_rn(q.y, py), az = __fsub_rn(q.z, pz);
             const float zz = dot3(ax, ay, az, vz);
             if (zz < 0.05f) {  // (double)z < 0.05 <=> z < 0.05f for a binary32 z
@@ -212,7 +235,13 @@ __global__ void __launch_bounds__(256) k_resolve_gather(const FrameParams* __res
                 const uint32_t src = (uint32_t)key;
                 const uint32_t hi = (uint32_t)(key >> 32);
                 const int phys = (hi & 1u) ? P->src_plane[1] : P->src_plane[0];
-                const float4 q = plane_xyz(B, phys)[src];
+                float4 q = plane_xyz(B, phys)[src];
+                if (P->rebase) {
+                    const int r = (int)(hi & 1u);
+                    q.x = __fadd_rn(q.x, P->src_shift[r][0]);
+                    q.y = __fadd_rn(q.y, P->src_shift[r][1]);
+                    q.z = __fadd_rn(q.z, P->src_shift[r][2]);
+                }
                 const float ax = __fsub_rn(q.x, P->ray.px), ay = __fsub_rn(q.y, P->ray.py),
                             az = __fsub_rn(q.z, P->ray.pz);
                 outc = (hi & ~255u) + (plane_col(B, phys)[src] & 255u);
@@ -377,7 +406,12 @@ __global__ void __launch_bounds__(BLOCK) k_trace_full(Octree o_in, const FullBat
     if (fault) atomicOr(fault_out, fault);
 }
 
-// kBgrx (learned frames): also writes the traced pixels' colourised output.
+// kBgrx (learned frames): also writes the traced pixels' colourised output,
+// and with a guide buffer walks every guided pixel after the requested rays
+// and the refresh tile: dense packets over the frame, each guided pixel's
+// ray starting at its guide distance (pixels of the refresh tile and
+// unguided pixels are skipped). Requested pixels are unguided, so every pixel
+// is written at most once and the walks read nothing the launch writes.
 template <int DEPTH, int BLOCK, bool kBgrx>
 __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FrameParams* __restrict__ P,
                                                     TargetBuffers B, uint32_t* fault_out) {
@@ -394,7 +428,10 @@ __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FramePa
     const int ax = P->add_x, ay = P->add_y, xe = P->x_end, ye = P->y_end;
     const int ps = P->pw_shift, pw = 1 << ps, ph = 32 >> ps;
     const uint32_t rpx = (uint32_t)max(0, (xe - ax + pw - 1) / pw), rpy = (uint32_t)max(0, (ye - ay + ph - 1) / ph);
-    const uint32_t total = hole_packets + rpx * rpy;
+    const uint32_t fixed = hole_packets + rpx * rpy;
+    const float* __restrict__ guide = kBgrx ? B.guide : nullptr;
+    const uint32_t wpx = (uint32_t)((res_x + pw - 1) / pw);
+    const uint32_t total = fixed + (guide ? wpx * (uint32_t)((res_y + ph - 1) / ph) : 0u);
     const RayCam cam = P->ray;
     float4* __restrict__ xyz = plane_xyz(B, P->cur);
     uint32_t* __restrict__ col = plane_col(B, P->cur);
@@ -405,7 +442,17 @@ __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FramePa
         if (p >= total) break;
         int x, y;
         bool valid;
-        if (p < hole_packets) {
+        float s0 = 0.0f;
+        if (kBgrx && p >= fixed) {
+            const uint32_t q = p - fixed;
+            x = (int)(q % wpx) * pw + (lane & (pw - 1));
+            y = (int)(q / wpx) * ph + (lane >> ps);
+            valid = x < res_x && y < res_y && !(x >= ax && x < xe && y >= ay && y < ye);
+            if (valid) {
+                s0 = __ldg(guide + (size_t)y * res_x + x);
+                valid = s0 >= 0.0f;
+            }
+        } else if (p < hole_packets) {
             const uint32_t e = p * 32u + (uint32_t)lane;
             valid = e < holes;
             const uint32_t xy = valid ? B.ids[2u * tiles + e] : 0u;
@@ -423,7 +470,8 @@ __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FramePa
             valid = x < xe && y < ye;
         }
         if (valid) {
-            const RayResult r = trace_ray<DEPTH, false>(o, cam, x, y, res_x, res_y, stk, BLOCK, fault);
+            // s0 = 0: the plain ray from the camera, bit for bit
+            const RayResult r = trace_ray<DEPTH, false, kBgrx>(o, cam, x, y, res_x, res_y, stk, BLOCK, fault, s0);
             const size_t ofs = (size_t)y * res_x + x;
             col[ofs] = r.colour;
             xyz[ofs] = make_float4(r.hx, r.hy, r.hz, r.dist);

@@ -394,6 +394,83 @@ constexpr int kNetPer = kNetPos / kNetThreads;  // input positions per thread an
 constexpr int kNetIssuers = 4;                   // threads (lane 0 of warps 0-3) issuing each layer's MMAs
 static_assert(kNetPer == kNetLayers, "one slice of the next tile's input per layer");
 
+// ------------------------------------------------- guided walks --
+// A guided learned frame walks a pixel's ray from just in front of the
+// nearest cached surface around it instead of from the camera: the start
+// distance is the smallest camera distance of the reprojected points in the
+// pixel's 3x3 neighbourhood, less kGuideMargin cells of the level of detail
+// at that distance. A cached point that is a ray end rather than a hit (the
+// ray left the volume through its top or bottom, or reached the view
+// distance limit) bounds its neighbours the same way: their rays are walked
+// from just in front of where it ended. A pixel with no cached point around
+// it is unguided and left to the net, which colours it or requests a full
+// ray. The walk is exact unless a surface the cache has not seen lies in
+// front of the start; the refresh tile and the requested rays keep tracing
+// from the camera.
+constexpr float kGuideMargin = 4.0f;        // cells of the start distance's level of detail
+constexpr int kGuideBW = 32, kGuideBH = 8;  // pixels per block
+
+// Also lists the net tiles (kNetOutW x kNetOutH) holding an unguided pixel:
+// the first block to find one in a tile stamps the tile with this frame's
+// serial and appends it (a block of 32 x 8 pixels touches at most 2 x 2
+// tiles).
+__global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams* __restrict__ P, TargetBuffers B) {
+    __shared__ float dist[kGuideBH + 2][kGuideBW + 2];
+    __shared__ uint32_t touched;
+    const int res_x = B.res_x, res_y = B.res_y;
+    const int x0 = blockIdx.x * kGuideBW, y0 = blockIdx.y * kGuideBH;
+    const float cx = P->ray.px, cy = P->ray.py, cz = P->ray.pz;
+    const uint32_t* __restrict__ col = plane_col(B, P->cur);
+    const float4* __restrict__ xyz = plane_xyz(B, P->cur);
+    if (threadIdx.x == 0) touched = 0;
+    for (int i = threadIdx.x; i < (kGuideBW + 2) * (kGuideBH + 2); i += kGuideBW * kGuideBH) {
+        const int wx = i % (kGuideBW + 2), wy = i / (kGuideBW + 2);
+        const int gx = x0 + wx - 1, gy = y0 + wy - 1;
+        float d = INFINITY;
+        if (gx >= 0 && gx < res_x && gy >= 0 && gy < res_y) {
+            const size_t o = (size_t)gy * res_x + gx;
+            if (__ldg(col + o) != kEmptyPixel) {
+                const float4 q = __ldg(xyz + o);
+                const float ax = q.x - cx, ay = q.y - cy, az = q.z - cz;
+                d = sqrtf(__fmaf_rn(ax, ax, __fmaf_rn(ay, ay, az * az)));
+            }
+        }
+        dist[wy][wx] = d;
+    }
+    __syncthreads();
+    const int tx = threadIdx.x % kGuideBW, ty = threadIdx.x / kGuideBW;
+    const int x = x0 + tx, y = y0 + ty;
+    if (x < res_x && y < res_y) {
+        float m = INFINITY;
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+#pragma unroll
+            for (int i = 0; i < 3; ++i) m = fminf(m, dist[ty + j][tx + i]);
+        float g = -1.0f;
+        if (m < INFINITY) {
+            const float s = m * 16.0f;  // raypos units
+            float sw = (float)(2 * res_x);
+            int lod = 1;
+            while (s > sw && lod < 24) {  // the walk's lodswitch doublings
+                sw *= 2.0f;
+                ++lod;
+            }
+            g = fmaxf(s - kGuideMargin * (float)(1 << lod), 0.0f);
+        } else {
+            const int ntx = x / kNetOutW - x0 / kNetOutW, nty = y / kNetOutH - y0 / kNetOutH;
+            atomicOr(&touched, 1u << (ntx + 2 * nty));
+        }
+        B.guide[(size_t)y * res_x + x] = g;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4 && ((touched >> threadIdx.x) & 1u)) {
+        const int tiles_x = (res_x + kNetOutW - 1) / kNetOutW;
+        const uint32_t tile = (uint32_t)((y0 / kNetOutH + (int)(threadIdx.x >> 1)) * tiles_x + x0 / kNetOutW +
+                                         (int)(threadIdx.x & 1));
+        if (atomicExch(B.net_flags + tile, P->serial) != P->serial) B.net_list[atomicAdd(B.counters + 3, 1u)] = tile;
+    }
+}
+
 struct NetInferArgs {
     const uint16_t* packed;  // tensor-core weight image
     const float* bias;       // 52 biases
@@ -509,9 +586,13 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_infer(NetInferArgs A) {
         for (int i = tid; i < 6 * kNetPlaneBytes / 16; i += kNetThreads) z[i] = make_uint4(0, 0, 0, 0);
     }
     __syncthreads();
+    // Work: every tile, or (guided frames) the listed tiles.
+    const uint32_t* __restrict__ list = kPipeline && A.B.guide ? A.B.net_list : nullptr;
+    const int n_work = list ? (int)A.B.counters[3] : A.tiles;
     // the first tile's input
-    int tile = blockIdx.x;
-    if (tile < A.tiles) {
+    int item = blockIdx.x;
+    if (item < n_work) {
+        const int tile = list ? (int)list[item] : item;
         const int wx = (tile % A.tiles_x) * kNetOutW - 4, wy = (tile / A.tiles_x) * kNetOutH - 4;
 #pragma unroll
         for (int k = 0; k < kNetPer; ++k) net_stage_input<kPipeline>(A, sP, smem, kNetSmemX, wx, wy, k);
@@ -530,12 +611,15 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_infer(NetInferArgs A) {
     bool aborted = false;  // block-uniform: an MMA wait timed out
     int xb = 0;            // which input plane holds this tile's input
 
-    for (; tile < A.tiles; tile += gridDim.x, xb ^= 1) {
+    for (; item < n_work; item += gridDim.x, xb ^= 1) {
+        const int tile = list ? (int)list[item] : item;
         const int ox = (tile % A.tiles_x) * kNetOutW, oy = (tile / A.tiles_x) * kNetOutH;
         const int wx = ox - 4, wy = oy - 4;  // image position of window position 0
         const uint32_t x_cur = kNetSmemX + (uint32_t)xb * kNetPlaneBytes;
         const uint32_t x_next = kNetSmemX + (uint32_t)(xb ^ 1) * kNetPlaneBytes;
-        const int next = tile + (int)gridDim.x;
+        const int next_item = item + (int)gridDim.x;
+        const bool has_next = next_item < n_work;
+        const int next = has_next ? (list ? (int)list[next_item] : next_item) : 0;
         const int nwx = (next % A.tiles_x) * kNetOutW - 4, nwy = (next / A.tiles_x) * kNetOutH - 4;
 
         for (int l = 0; l < kNetLayers; ++l) {
@@ -553,7 +637,7 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_infer(NetInferArgs A) {
                 tc_commit(smem_addr(&mbar[warp]));
             }
             // while the MMAs run: one slice of the next tile's input
-            if (next < A.tiles) net_stage_input<kPipeline>(A, sP, smem, x_next, nwx, nwy, l);
+            if (has_next) net_stage_input<kPipeline>(A, sP, smem, x_next, nwx, nwy, l);
             // each warp waits (bounded) for the MMAs of its own blocks only, so the
             // read-back of early blocks overlaps the MMAs of later ones
             const bool ready = mbar_wait_phase(bar, phase);
@@ -615,7 +699,11 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_infer(NetInferArgs A) {
                             const uint32_t gi = (uint32_t)__float2int_rn(fminf(fmaxf(gg, 0.0f), 1.0f) * 255.0f);
                             const uint32_t bi = (uint32_t)__float2int_rn(fminf(fmaxf(b, 0.0f), 1.0f) * 255.0f);
                             A.B.bgrx[ofs] = bi + (gi << 8) + (ri << 16);
-                            req = !(z >= A.logit_threshold);
+                            // guided pixels are walked, never requested; with no cache
+                            // (the first frames) every pixel is traced: pixels the net
+                            // fills are not cached, so they would stay unguided
+                            req = !sP.have_cache ||
+                                  (!(z >= A.logit_threshold) && !(list && __ldg(A.B.guide + ofs) >= 0.0f));
                         }
                         // Ray requests: bit (x&7) + 8*(y&3) of the pixel's 8x4 packet. The
                         // warp's lanes are consecutive pixels of one row, so the first lane

@@ -27,6 +27,7 @@ namespace svo {
 constexpr uint32_t kEmptyPixel = 0xffffff00u;
 constexpr float kViewDistMax = 400000.0f;  // VIEW_DIST_MAX, kernel.cl:15
 constexpr uint32_t kStepCap = 1u << 20;
+constexpr float kGuideTopMargin = 16.0f;   // raypos units a guided start keeps below the volume's top
 constexpr uint32_t kFaultFetch = 1u;       // node word index outside the octree
 constexpr uint32_t kFaultSteps = 2u;       // a ray exceeded kStepCap steps
 constexpr uint32_t kFaultHoleEntry = 4u;   // hole list entry outside the frame
@@ -233,13 +234,13 @@ __device__ __forceinline__ uint32_t load_word_sel(const Octree& o, uint32_t i, u
 template <int DEPTH, bool kFast>
 __device__ __forceinline__ void walk(const Octree& o, Walk& w, uint32_t sxyz, float g0y, float g0z, float g1x,
                                      float g1z, float g2x, float g2y, float lx, float ly, float lz, float lodswitch,
-                                     uint32_t* stk, int stride, uint32_t& fault) {
+                                     int lod, uint32_t* stk, int stride, uint32_t& fault) {
     constexpr int kDepthAnd = (1 << DEPTH) - 1;
     constexpr int kTopBit = 2 * kDepthAnd + 2;
     float rpx = w.rpx, rpy = w.rpy, rpz = w.rpz;
     int rix = float_to_int<kFast>(rpx), riy = float_to_int<kFast>(rpy), riz = float_to_int<kFast>(rpz);
-    int rek = DEPTH, lod = 1;
-    float distance = 0.0f;
+    int rek = DEPTH;
+    float distance = w.distance;
     const uint32_t root = o.root;
     uint32_t nodeid = root, nodeid_before = root, local_root = 0, node_test = 0;
     uint32_t steps = 0;
@@ -339,9 +340,19 @@ __device__ __forceinline__ void walk(const Octree& o, Walk& w, uint32_t sxyz, fl
 // Ray setup of raycast_fine_2/raycast_holes (kernel.cl:883-899) + CAST_RAY +
 // the colour fetch. `stk` points at this thread's column of the shared stack
 // (entry for level L at stk[L * stride]); levels 1..DEPTH-1 are used.
-template <int DEPTH, bool kVoxel>
+//
+// kGuided with s0 > 0: the walk starts s0 (raypos units, 16 per world unit)
+// along the ray instead of at the camera -- but at most up to
+// kGuideTopMargin before the ray leaves the volume's height -- with the
+// distance already at s0 and the level of detail advanced as far as the
+// lodswitch doublings below s0 reach. The start point is camera + s0 * d/|d|
+// in the mirrored frame, every operation rounded to nearest (the CPU oracle
+// repeats it). Everything the ray passes before s0 is skipped: the caller
+// guarantees, or accepts, that nothing lies there.
+template <int DEPTH, bool kVoxel, bool kGuided = false>
 __device__ __forceinline__ RayResult trace_ray(const Octree& o, const RayCam& c, int idx, int idy, int res_x,
-                                               int res_y, uint32_t* stk, int stride, uint32_t& fault) {
+                                               int res_y, uint32_t* stk, int stride, uint32_t& fault,
+                                               float s0 = 0.0f) {
     constexpr int kScaleMax = 1 << (DEPTH + 1);
     const float fscale = (float)kScaleMax;
 
@@ -369,20 +380,41 @@ __device__ __forceinline__ RayResult trace_ray(const Octree& o, const RayCam& c,
     const float lx = __fsqrt_rn(__fadd_rn(__fadd_rn(1.0f, __fmul_rn(g0y, g0y)), __fmul_rn(g0z, g0z)));
     const float ly = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(g1x, g1x), 1.0f), __fmul_rn(g1z, g1z)));
     const float lz = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(g2x, g2x), __fmul_rn(g2y, g2y)), 1.0f));
-    const float lodswitch = (float)(res_x * 2);  // res_x*LOD_ADJUST*2, kernel.cl:908
+    float lodswitch = (float)(res_x * 2);  // res_x*LOD_ADJUST*2, kernel.cl:908
+    int lod = 1;
+    float dist0 = 0.0f;
+    if (kGuided && s0 > 0.0f) {
+        const float nd = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+        // never past the point where the ray leaves the volume's height (the
+        // walk's exit test fires only on the step that crosses it; beyond it
+        // the ray would walk the periodic copy above)
+        const float t_top = __fmul_rn(__fdiv_rn(__fsub_rn(fscale, rpy), dy), nd);
+        s0 = fminf(s0, __fsub_rn(t_top, kGuideTopMargin));
+        if (s0 > 0.0f) {
+            rpx = __fadd_rn(rpx, __fmul_rn(__fdiv_rn(dx, nd), s0));
+            rpy = __fadd_rn(rpy, __fmul_rn(__fdiv_rn(dy, nd), s0));
+            rpz = __fadd_rn(rpz, __fmul_rn(__fdiv_rn(dz, nd), s0));
+            dist0 = s0;
+            while (dist0 > lodswitch && lod < DEPTH) {
+                lodswitch = __fmul_rn(lodswitch, 2.0f);
+                ++lod;
+            }
+        }
+    }
 
     Walk w;
     w.rpx = rpx;
     w.rpy = rpy;
     w.rpz = rpz;
+    w.distance = dist0;
     w.hit = false;
     w.hcx = w.hcy = w.hcz = 0;
     const float lim = 4194304.0f;  // 2^22
     const bool fast = rpx >= 0.0f && rpx < lim && rpy >= 0.0f && rpy < lim && rpz >= 0.0f && rpz < lim;
     if (fast)
-        walk<DEPTH, true>(o, w, sxyz, g0y, g0z, g1x, g1z, g2x, g2y, lx, ly, lz, lodswitch, stk, stride, fault);
+        walk<DEPTH, true>(o, w, sxyz, g0y, g0z, g1x, g1z, g2x, g2y, lx, ly, lz, lodswitch, lod, stk, stride, fault);
     else
-        walk<DEPTH, false>(o, w, sxyz, g0y, g0z, g1x, g1z, g2x, g2y, lx, ly, lz, lodswitch, stk, stride, fault);
+        walk<DEPTH, false>(o, w, sxyz, g0y, g0z, g1x, g1z, g2x, g2y, lx, ly, lz, lodswitch, lod, stk, stride, fault);
     rpx = w.rpx;
     rpy = w.rpy;
     rpz = w.rpz;

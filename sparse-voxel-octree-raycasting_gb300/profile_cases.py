@@ -2,6 +2,7 @@
 
     learned   8 learned warp frames, 1920x1024, depth-11 benchmark terrain,
               committed net weights, threshold 0.5 (orbit camera)
+    guided    the same frames with guided walks
     plain     8 plain warp frames of the same scene and camera
     full      4 full raycasts of the same scene and camera
     build     2 GPU octree builds of the depth-11 benchmark terrain's voxels
@@ -43,7 +44,8 @@ def main(case: str) -> None:
     ctx = svo.Context(0)
     ctx.upload(octree)
     t = ctx.target(W, H)
-    if case == "learned":
+    if case in ("learned", "guided"):
+        t.set_guided(case == "guided")
         net = svo.Net(ctx)
         net.load_file(os.path.join(HERE, "net_weights.npy"))
         for f in range(8):

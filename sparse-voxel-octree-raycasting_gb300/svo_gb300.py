@@ -48,7 +48,7 @@ EXPORTS = [
     "svo_net_destroy", "svo_net_init", "svo_net_set_params", "svo_net_get_params", "svo_net_get_grads",
     "svo_net_forward", "svo_net_infer", "svo_net_backward", "svo_net_adam", "svo_target_set_cache_mode",
     "svo_target_set_coarse_refresh", "svo_octree_build", "svo_octree_info", "svo_octree_download",
-    "svo_context_autotune",
+    "svo_context_autotune", "svo_target_set_guided", "svo_read_guide",
 ]
 
 NET_PARAMS = 6388
@@ -170,6 +170,8 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "svo_target_set_feature_tap": (i, [_P, _P]),
         "svo_target_set_cache_mode": (i, [_P, i]),
         "svo_target_set_coarse_refresh": (i, [_P, i]),
+        "svo_target_set_guided": (i, [_P, i]),
+        "svo_read_guide": (i, [_P, _P]),
         "svo_octree_build": (i, [_P, _P, _P, _P, _P, sz, i, sz]),
         "svo_octree_info": (i, [_P, ctypes.POINTER(sz), ctypes.POINTER(u32), ctypes.POINTER(i)]),
         "svo_octree_download": (i, [_P, _P, sz]),
@@ -512,6 +514,17 @@ class Target:
         """Device buffer (8 x res_y x res_x FP32) receiving the net's input
         features of every later frame; None stops it."""
         _check(self._lib.svo_target_set_feature_tap(self._h, _P(d_features) if d_features else None), self.ctx)
+
+    def set_guided(self, enable: bool = True) -> None:
+        """Guided learned frames: pixels with a cached surface point nearby are
+        walked from just in front of it; only the others go to the net."""
+        _check(self._lib.svo_target_set_guided(self._h, 1 if enable else 0), self.ctx)
+
+    def guide(self) -> np.ndarray:
+        """Start distances of the last guided frame (raypos units; -1 unguided)."""
+        out = np.empty(self.n, np.float32)
+        _check(self._lib.svo_read_guide(self._h, _ptr(out)), self.ctx)
+        return out
 
     def requested(self) -> int:
         """Rays the net requested in the last learned frame."""

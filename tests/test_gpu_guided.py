@@ -1,0 +1,165 @@
+"""GPU tests of guided learned frames: pixels with a cached surface point in
+their 3x3 neighbourhood are walked from just in front of it.
+
+* every walked pixel (and the refresh tile, traced from the camera) equals
+  the CPU oracle's walk from the same start distance, bit for bit (colour
+  word and hit position/distance) -- the start distances are read back from
+  the frame;
+* the start distances are conservative for nearly every pixel (in front of
+  the pixel's true hit);
+* the frames stay close to the full raycast of the same view.
+"""
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _weights(svo):
+    return os.path.join(os.path.dirname(svo.__file__), "net_weights.npy")
+
+
+def _refresh_rect(f, W, H):
+    # the 8x4 rolling refresh tile of raycast.h:363-366 (NDRange rounded up to 16)
+    ax, ay = (W // 8) * (f & 7), (H // 4) * ((f >> 3) & 3)
+    gx, gy = (W // 8 + 15) // 16 * 16, (H // 4 + 15) // 16 * 16
+    return ax, ay, min(W, ax + gx), min(H, ay + gy)
+
+
+@pytest.mark.parametrize("depth,kind,W,H,frames,graph", [
+    (9, 1, 160, 96, 14, False),
+    (9, 2, 160, 96, 14, True),
+    (10, 2, 200, 120, 10, True),
+])
+def test_guided_walks_match_oracle(svo, orc, scene, gpu_ctx, depth, kind, W, H, frames, graph):
+    octree = scene(depth, 77, True)
+    gpu_ctx.upload(octree)
+    net = gpu_ctx.net()
+    net.load_file(_weights(svo))
+    t = gpu_ctx.target(W, H)
+    t.set_guided(True)
+    t.use_graph(graph)
+    walked_total = 0
+    for f in range(frames):
+        v = svo.camera_path(kind, depth, f, W, H)
+        gpu_ctx.warp_frame_learned(t, v, f, net, 0.5)
+        gpu_ctx.synchronize()
+        g = t.guide()
+        col = t.colour(2)  # the frame's current plane (the next frame's cache)
+        xyz = t.coords(0)
+        s0 = g.copy()
+        ax, ay, xe, ye = _refresh_rect(f, W, H)
+        rect = np.zeros((H, W), bool)
+        rect[ay:ye, ax:xe] = True
+        rect = rect.ravel()
+        s0[rect] = 0.0  # the refresh tile is traced from the camera
+        check = (g >= 0) | rect
+        ocol, oxyz = orc.raycast_guided(depth, octree.words, octree.root, v.pos_array, v.m_array, W, H, s0)
+        assert np.array_equal(col[check], ocol[check]), f"frame {f}: walked colour words differ"
+        assert np.array_equal(xyz[check].view(np.uint32), oxyz[check].view(np.uint32)), f"frame {f}: hit bits differ"
+        walked_total += int((g >= 0).sum())
+        if f >= 3:
+            assert (g >= 0).mean() > 0.5, f"frame {f}: too few guided pixels"
+    assert walked_total > 0
+    t.close()
+    net.close()
+
+
+def test_guide_is_conservative(svo, orc, scene, gpu_ctx):
+    depth, W, H = 10, 320, 192
+    octree = scene(depth, 2024, True)
+    gpu_ctx.upload(octree)
+    net = gpu_ctx.net()
+    net.load_file(_weights(svo))
+    t, full = gpu_ctx.target(W, H), gpu_ctx.target(W, H)
+    t.set_guided(True)
+    for f in range(12):
+        v = svo.camera_path(1, depth, f, W, H)
+        gpu_ctx.warp_frame_learned(t, v, f, net, 0.5)
+        if f < 4:
+            continue
+        gpu_ctx.raycast_full(full, v)
+        gpu_ctx.synchronize()
+        g = t.guide()
+        _, xyzw = full.full()
+        guided = g > 0
+        hit = (xyzw[:, 3] < 20000.0) & (xyzw[:, 1] > 0.0) & (xyzw[:, 1] < 2 ** (depth + 1) / 16)
+        sel = guided & hit
+        # the start lies in front of the pixel's true hit (raypos units: 16 per world unit)
+        behind = (g[sel] > 16.0 * xyzw[sel, 3]).mean()
+        assert behind < 0.01, (f, behind)
+        assert set(np.unique(g[g < 0])) <= {-1.0}
+    t.close()
+    full.close()
+    net.close()
+
+
+def _psnr(a, b):
+    a = a.view(np.uint8).reshape(-1, 4)[:, :3].astype(np.float64)
+    b = b.view(np.uint8).reshape(-1, 4)[:, :3].astype(np.float64)
+    mse = ((a - b) ** 2).mean()
+    return 10 * np.log10(255.0 ** 2 / max(mse, 1e-9))
+
+
+@pytest.mark.parametrize("kind", [1, 2])
+def test_guided_frames_close_to_full_raycast(svo, gpu_ctx, kind):
+    depth, W, H = 10, 640, 384
+    octree = svo.build_terrain(depth, 2024, shell=True)
+    gpu_ctx.upload(octree)
+    net = gpu_ctx.net()
+    net.load_file(_weights(svo))
+    t, full = gpu_ctx.target(W, H), gpu_ctx.target(W, H)
+    t.set_guided(True)
+    t.use_graph(True)
+    psnr, guided, same, far = [], [], [], []
+    for f in range(40):
+        v = svo.camera_path(kind, depth, f, W, H)
+        gpu_ctx.warp_frame_learned(t, v, f, net, 0.5)
+        if f < 8:
+            continue
+        gpu_ctx.raycast_full(full, v)
+        gpu_ctx.synchronize()
+        a, b = t.bgrx(), full.bgrx()
+        psnr.append(_psnr(a, b))
+        same.append((a == b).mean())
+        g = t.guide()
+        guided.append((g >= 0).mean())
+        far.append((g == 0).mean())  # walked from the camera
+    print(f"kind {kind}: PSNR min {min(psnr):.2f} mean {np.mean(psnr):.2f} dB, guided {np.mean(guided):.3f}, "
+          f"identical pixels {np.mean(same):.4f}, from the camera {np.mean(far):.3f}")
+    print("per frame:", " ".join(f"{p:.1f}/{g:.3f}" for p, g in zip(psnr, guided)))
+    whole = 10 * np.log10(1.0 / np.mean([10 ** (-p / 10) for p in psnr]))
+    assert whole > 40.0 and min(psnr) > 30.0, (whole, min(psnr))
+    assert np.mean(guided) > 0.85
+    t.close()
+    full.close()
+    net.close()
+
+
+def test_guided_toggle_and_all_requested(svo, scene, gpu_ctx):
+    # Switching guidance off returns to the learned frame that traces every
+    # pixel below the threshold: with every pixel requested it is the full
+    # raycast again, bit for bit; switched on, the same call walks instead.
+    octree = scene(9, 77, True)
+    gpu_ctx.upload(octree)
+    net = gpu_ctx.net()
+    net.load_file(_weights(svo))
+    W, H = 160, 96
+    t, full = gpu_ctx.target(W, H), gpu_ctx.target(W, H)
+    t.use_graph(True)
+    for f in range(12):
+        t.set_guided(f % 4 >= 2)
+        v = svo.camera_path(2, 9, f, W, H)
+        gpu_ctx.warp_frame_learned(t, v, f, net, 0.999999)
+        gpu_ctx.raycast_full(full, v)
+        gpu_ctx.synchronize()
+        a, b = t.bgrx(), full.bgrx()
+        if f % 4 < 2:
+            assert np.array_equal(a, b), f
+        else:
+            assert (a == b).mean() > 0.98, (f, (a == b).mean())
+    t.close()
+    full.close()
+    net.close()
