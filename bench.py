@@ -515,8 +515,15 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     tgt3.close()
 
     # ---- quality against the full raycast of the same cameras
+    def net_tiles(g):
+        # 56x24 net tiles holding an unguided pixel (the tiles k_guide lists)
+        tw, th = -(-W // 56), -(-H // 24)
+        pad = np.zeros((th * 24, tw * 56), bool)
+        pad[:H, :W] = (g < 0).reshape(H, W)
+        return int(pad.reshape(th, 24, tw, 56).any(axis=(1, 3)).sum())
+
     def quality(render, t, kind, traced_of, walked=False):
-        mse, traced, worst, walk = [], [], [], []
+        mse, traced, worst, walk, tiles = [], [], [], [], []
         for f in range(args.warmup + args.steps):
             v = view(f, kind)
             render(f, v)
@@ -529,12 +536,15 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                 worst.append(int(np.abs(d).max()))
                 traced.append(traced_of(t) / (W * H))
                 if walked:
-                    walk.append(float((t.guide() >= 0).mean()))
+                    g = t.guide()
+                    walk.append(float((g >= 0).mean()))
+                    tiles.append(net_tiles(g))
         m = float(np.mean(mse))
         out = {"psnr_db": 10 * np.log10(255.0 ** 2 / m) if m > 0 else float("inf"),
                "max_abs_error": int(max(worst)), "traced_fraction": float(np.mean(traced))}
         if walked:
             out["walked_fraction"] = float(np.mean(walk))
+            out["net_tiles"] = float(np.mean(tiles))
         return out
 
     tq = ctx.target(W, H)
@@ -631,6 +641,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     # counts for the roofline's algorithmic bytes, and the CPU baseline.
     cpu = None
     bytes_per_ray = None
+    walk_bytes_per_ray = None
     parity = None
     if not args.no_cpu and rank == 0:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -665,6 +676,18 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
         _, _, _, st = oracle.raycast_full(depth, octree.words, octree.root, v.pos_array, v.m_array, W, H,
                                           1.0, 1.0, threads)
         bytes_per_ray = (4.0 * (float(st[1]) + float(st[2])) + 20.0 * float(st[0])) / float(st[0])
+        if args.guided:
+            # the same count for the guided walks of that frame, from the start
+            # distances the GPU used (read back after the frame)
+            tg = ctx.target(W, H)
+            tg.set_guided(True)
+            for f in range(args.warmup + args.steps):
+                ctx.warp_frame_learned(tg, view(f), f, net, thr)
+            g = tg.guide()
+            tg.close()
+            _, _, stw = oracle.raycast_guided(depth, octree.words, octree.root, v.pos_array, v.m_array, W, H,
+                                              np.where(g >= 0, g, -1.0).astype(np.float32), threads, stats=True)
+            walk_bytes_per_ray = (4.0 * (float(stw[1]) + float(stw[2])) + 20.0 * float(stw[0])) / max(float(stw[0]), 1.0)
 
     extras = {}
     if args.extras and rank == 0:
@@ -677,24 +700,34 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     tflops = peaks.get("bf16_tflops")
     roofline = None
     roofline_net = None
-    rays_learned = (q_learned["traced_fraction"] * W * H
-                    + (W // 8 + 15) // 16 * 16 * ((H // 4 + 15) // 16 * 16))
-    if bytes_per_ray is not None and stage_ms_learned["trace"] > 0:
-        algo = bytes_per_ray * rays_learned
+    # rays of one learned frame's trace launch: the requested pixels and the
+    # refresh tile from the camera, plus (guided) the walked pixels
+    rays_camera = (q_learned["traced_fraction"] * W * H
+                   + (W // 8 + 15) // 16 * 16 * ((H // 4 + 15) // 16 * 16))
+    rays_walked = q_learned.get("walked_fraction", 0.0) * W * H
+    if bytes_per_ray is not None and stage_ms_learned["trace"] > 0 and (walk_bytes_per_ray or not args.guided):
+        algo = bytes_per_ray * rays_camera + (walk_bytes_per_ray or 0.0) * rays_walked
         achieved = algo / (stage_ms_learned["trace"] * 1e-3) / 1e9
         peak = hbm if hbm else 6800.0
-        roofline = {"bound": "hbm", "kernel": "k_trace_warp (learned frame: requested pixels + refresh tile)",
+        roofline = {"bound": "hbm", "kernel": "k_trace_warp (learned frame: requested pixels, refresh tile"
+                                              + (", guided walks)" if args.guided else ")"),
                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                     "peak_source": "measured" if hbm else "fallback", "algorithmic_bytes_per_launch": algo,
-                    "bytes_per_ray": bytes_per_ray, "rays_per_launch": rays_learned, "traffic": None}
+                    "bytes_per_ray": bytes_per_ray, "walk_bytes_per_ray": walk_bytes_per_ray,
+                    "rays_per_launch": rays_camera + rays_walked, "walked_rays_per_launch": rays_walked,
+                    "traffic": None}
     if stage_ms_learned["net"] > 0:
-        flops = 12096.0 * W * H  # 2 * 9 * (8*16 + 16*16 + 16*16 + 16*4) per pixel
+        # 2 * 9 * (8*16 + 16*16 + 16*16 + 16*4) per output pixel, over the
+        # tiles the net ran on (every tile unless guided)
+        net_pixels = q_learned["net_tiles"] * 56 * 24 if "net_tiles" in q_learned else W * H
+        flops = 12096.0 * net_pixels
         ach = flops / (stage_ms_learned["net"] * 1e-3) / 1e12
         peak = tflops if tflops else 1900.0
         roofline_net = {"bound": "tensor", "kernel": "k_net_infer", "achieved": ach, "peak": peak,
                         "unit": "TFLOP/s", "frac": ach / peak, "peak_source": "measured" if tflops else "fallback",
-                        "hbm_gbs": 24.0 * W * H / (stage_ms_learned["net"] * 1e-3) / 1e9,
-                        "flops_per_launch": flops}
+                        "hbm_gbs": 24.0 * net_pixels / (stage_ms_learned["net"] * 1e-3) / 1e9,
+                        "flops_per_launch": flops, "net_pixels_per_launch": net_pixels,
+                        "note": "net stage events: k_net_infer plus the request scan"}
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,

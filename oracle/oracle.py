@@ -54,7 +54,7 @@ def oracle() -> ctypes.CDLL:
         lib.orc_octree_free.argtypes = [_P]
         lib.orc_raycast_full.argtypes = [i, _P, sz, u32, _P, _P, i, i, ctypes.c_float, ctypes.c_float, _P, _P, _P,
                                          _P, i]
-        lib.orc_raycast_guided.argtypes = [i, _P, sz, u32, _P, _P, i, i, _P, _P, _P, i]
+        lib.orc_raycast_guided.argtypes = [i, _P, sz, u32, _P, _P, i, i, _P, _P, _P, _P, i]
         lib.orc_warp_create.restype = _P
         lib.orc_warp_create.argtypes = [i, i]
         lib.orc_warp_free.argtypes = [_P]
@@ -152,10 +152,11 @@ def raycast_full(depth, words, root, pos, m, res_x, res_y, fovx=1.0, fovy=1.0, t
     return col, xyzw.reshape(n, 4), None, None
 
 
-def raycast_guided(depth, words, root, pos, m, res_x, res_y, s0, threads=0):
+def raycast_guided(depth, words, root, pos, m, res_x, res_y, s0, threads=0, stats=False):
     """Guided walks (the product's learned frames): pixel o's ray starts at
     s0[o] raypos units (0: from the camera; < 0: not traced, colour left at
-    the empty word and xyzw at 0). Returns colour words and float4 per pixel."""
+    the empty word and xyzw at 0). Returns colour words and float4 per pixel
+    (and, with stats, [rays walked, child fetches, colour fetches])."""
     words = np.ascontiguousarray(words, np.uint32)
     pos = np.ascontiguousarray(pos, np.float32)
     m = np.ascontiguousarray(m, np.float32)
@@ -164,10 +165,13 @@ def raycast_guided(depth, words, root, pos, m, res_x, res_y, s0, threads=0):
     assert s0.size == n
     col = np.full(n, 0xFFFFFF00, np.uint32)
     xyzw = np.zeros(n * 4, np.float32)
+    st = np.zeros(3, np.uint64)
     rc = oracle().orc_raycast_guided(depth, _ptr(words), words.size, root, _ptr(pos), _ptr(m), res_x, res_y, _ptr(s0),
-                                     _ptr(col), _ptr(xyzw), threads)
+                                     _ptr(col), _ptr(xyzw), _ptr(st), threads)
     if rc != 0:
         raise RuntimeError(f"orc_raycast_guided failed: {rc}")
+    if stats:
+        return col, xyzw.reshape(n, 4), st
     return col, xyzw.reshape(n, 4)
 
 

@@ -272,8 +272,8 @@ struct Tracer {
     // followed by CAST_RAY (kernel.cl:114-214) and the colour fetch (:911-921).
     // s0 > 0 (the product's guided walks, not in the reference): the walk
     // starts s0 raypos units along the ray -- at most up to 16 units before
-    // the ray leaves the volume's height -- at camera + s0 * d/|d| in the
-    // mirrored frame, with the distance at s0 and the level of detail
+    // the ray leaves the volume's height -- at camera + s0 * (1, g0y, g0z)/len0
+    // in the mirrored frame, with the distance at s0 and the level of detail
     // advanced over the lodswitch doublings below s0 (at most to the depth).
     Ray trace(const View& v, int idx, int idy, int res_x, int res_y, float fovx, float fovy, float s0 = 0.0f) const {
         Ray r{};
@@ -309,13 +309,13 @@ struct Tracer {
         float lodswitch = (float)(res_x * 1 * 2);  // LOD_ADJUST=1, kernel.cl:908
         float distance = 0.0f;
         if (s0 > 0.0f) {  // not past the ray's exit through the volume's top (16 raypos units margin)
-            const float nd = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-            const float t_top = (((float)scale_max - rp[1]) / d[1]) * nd;
+            const float t_top = ((float)scale_max - rp[1]) * len[1];
             s0 = std::fmin(s0, t_top - 16.0f);
         }
-        if (s0 > 0.0f) {
-            const float nd = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-            for (int a = 0; a < 3; ++a) rp[a] = rp[a] + (d[a] / nd) * s0;
+        if (s0 > 0.0f) {  // unit direction (1, g0y, g0z) / len[0]
+            const float ux = 1.0f / len[0];
+            const float u[3] = {ux, g[0][1] * ux, g[0][2] * ux};
+            for (int a = 0; a < 3; ++a) rp[a] = rp[a] + u[a] * s0;
             distance = s0;
             while (distance > lodswitch && lod < depth) {
                 lodswitch *= 2.0f;
@@ -673,20 +673,25 @@ int orc_raycast_full(int depth, const uint32_t* words, size_t n_words, uint32_t 
 
 // Guided walks over the whole frame: pixel o starts at s0[o] raypos units
 // (0: from the camera); pixels with s0[o] < 0 are not traced (outputs left
-// as they are).
+// as they are). stats (may be null): [0] rays walked, [1] child fetches,
+// [2] colour fetches.
 int orc_raycast_guided(int depth, const uint32_t* words, size_t n_words, uint32_t root, const float* pos4,
                        const float* m16, int res_x, int res_y, const float* s0, uint32_t* colour, float* xyzw,
-                       int threads) {
+                       uint64_t* stats, int threads) {
     if (res_x <= 0 || res_y <= 0 || res_x > 65535 || res_y > 65535 || !s0) return -1;
     Tracer tr{words, n_words, root, depth};
     View v = make_view(pos4, m16);
+    uint64_t rays = 0, child = 0, col = 0;
     if (threads > 0) omp_set_num_threads(threads);
-#pragma omp parallel for schedule(dynamic, 4)
+#pragma omp parallel for schedule(dynamic, 4) reduction(+ : rays, child, col)
     for (int y = 0; y < res_y; ++y)
         for (int x = 0; x < res_x; ++x) {
             size_t o = (size_t)y * res_x + x;
             if (s0[o] < 0.0f) continue;
             Ray r = tr.trace(v, x, y, res_x, res_y, 1.0f, 1.0f, s0[o]);
+            ++rays;
+            child += r.child_fetches;
+            col += r.colour_fetches;
             if (colour) colour[o] = r.colour;
             if (xyzw) {
                 xyzw[o * 4 + 0] = r.hit[0];
@@ -695,6 +700,11 @@ int orc_raycast_guided(int depth, const uint32_t* words, size_t n_words, uint32_
                 xyzw[o * 4 + 3] = r.dist;
             }
         }
+    if (stats) {
+        stats[0] = rays;
+        stats[1] = child;
+        stats[2] = col;
+    }
     return 0;
 }
 

@@ -345,9 +345,9 @@ __device__ __forceinline__ void walk(const Octree& o, Walk& w, uint32_t sxyz, fl
 // along the ray instead of at the camera -- but at most up to
 // kGuideTopMargin before the ray leaves the volume's height -- with the
 // distance already at s0 and the level of detail advanced as far as the
-// lodswitch doublings below s0 reach. The start point is camera + s0 * d/|d|
-// in the mirrored frame, every operation rounded to nearest (the CPU oracle
-// repeats it). Everything the ray passes before s0 is skipped: the caller
+// lodswitch doublings below s0 reach. The start point is camera + s0 *
+// (1, g0y, g0z)/lx (the unit direction) in the mirrored frame, every
+// operation rounded to nearest (the CPU oracle repeats it). Everything the ray passes before s0 is skipped: the caller
 // guarantees, or accepts, that nothing lies there.
 template <int DEPTH, bool kVoxel, bool kGuided = false>
 __device__ __forceinline__ RayResult trace_ray(const Octree& o, const RayCam& c, int idx, int idy, int res_x,
@@ -384,16 +384,19 @@ __device__ __forceinline__ RayResult trace_ray(const Octree& o, const RayCam& c,
     int lod = 1;
     float dist0 = 0.0f;
     if (kGuided && s0 > 0.0f) {
-        const float nd = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
-        // never past the point where the ray leaves the volume's height (the
-        // walk's exit test fires only on the step that crosses it; beyond it
-        // the ray would walk the periodic copy above)
-        const float t_top = __fmul_rn(__fdiv_rn(__fsub_rn(fscale, rpy), dy), nd);
+        // lx = |d|/dx and ly = |d|/dy (the walk's step lengths per unit of x
+        // and y) give the unit direction (1, g0y, g0z)/lx and the distance
+        // to the top of the volume without another square root.
+        // Never start past the point where the ray leaves the volume's height
+        // (the walk's exit test fires only on the step that crosses it;
+        // beyond it the ray would walk the periodic copy above).
+        const float t_top = __fmul_rn(__fsub_rn(fscale, rpy), ly);
         s0 = fminf(s0, __fsub_rn(t_top, kGuideTopMargin));
         if (s0 > 0.0f) {
-            rpx = __fadd_rn(rpx, __fmul_rn(__fdiv_rn(dx, nd), s0));
-            rpy = __fadd_rn(rpy, __fmul_rn(__fdiv_rn(dy, nd), s0));
-            rpz = __fadd_rn(rpz, __fmul_rn(__fdiv_rn(dz, nd), s0));
+            const float ux = __fdiv_rn(1.0f, lx);
+            rpx = __fadd_rn(rpx, __fmul_rn(ux, s0));
+            rpy = __fadd_rn(rpy, __fmul_rn(__fmul_rn(g0y, ux), s0));
+            rpz = __fadd_rn(rpz, __fmul_rn(__fmul_rn(g0z, ux), s0));
             dist0 = s0;
             while (dist0 > lodswitch && lod < DEPTH) {
                 lodswitch = __fmul_rn(lodswitch, 2.0f);
