@@ -69,6 +69,7 @@ struct TargetBuffers {
     // tile, the serial of the last frame that needed the net there, and the
     // list of those tiles (count in counters[3]). guide == nullptr: no walks.
     float* guide;
+    uint8_t* walk_long;  // per walk packet (pw x ph): 1 = expected to be long (traced first)
     uint32_t* net_flags;
     uint32_t* net_list;
     uint32_t* counters;   // [0] trace work counter, [1] hole entries, [2] coarse-pass work counter,
@@ -411,7 +412,10 @@ __global__ void __launch_bounds__(BLOCK) k_trace_full(Octree o_in, const FullBat
 // and the refresh tile: dense packets over the frame, each guided pixel's
 // ray starting at its guide distance (pixels of the refresh tile and
 // unguided pixels are skipped). Requested pixels are unguided, so every pixel
-// is written at most once and the walks read nothing the launch writes.
+// is written at most once and the walks read nothing the launch writes. The
+// walk packets are swept twice: first those k_guide expects to be long (a
+// depth edge inside: some pixel walks from the near side), then the rest, so
+// the launch does not end on a long packet.
 template <int DEPTH, int BLOCK, bool kBgrx>
 __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FrameParams* __restrict__ P,
                                                     TargetBuffers B, uint32_t* fault_out) {
@@ -431,7 +435,8 @@ __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FramePa
     const uint32_t fixed = hole_packets + rpx * rpy;
     const float* __restrict__ guide = kBgrx ? B.guide : nullptr;
     const uint32_t wpx = (uint32_t)((res_x + pw - 1) / pw);
-    const uint32_t total = fixed + (guide ? wpx * (uint32_t)((res_y + ph - 1) / ph) : 0u);
+    const uint32_t nwalk = guide ? wpx * (uint32_t)((res_y + ph - 1) / ph) : 0u;
+    const uint32_t total = fixed + 2u * nwalk;
     const RayCam cam = P->ray;
     float4* __restrict__ xyz = plane_xyz(B, P->cur);
     uint32_t* __restrict__ col = plane_col(B, P->cur);
@@ -444,7 +449,10 @@ __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FramePa
         bool valid;
         float s0 = 0.0f;
         if (kBgrx && p >= fixed) {
-            const uint32_t q = p - fixed;
+            uint32_t q = p - fixed;
+            const bool first_sweep = q < nwalk;
+            if (!first_sweep) q -= nwalk;
+            if ((B.walk_long[q] != 0) != first_sweep) continue;  // packet belongs to the other sweep
             x = (int)(q % wpx) * pw + (lane & (pw - 1));
             y = (int)(q / wpx) * ph + (lane >> ps);
             valid = x < res_x && y < res_y && !(x >= ax && x < xe && y >= ay && y < ye);

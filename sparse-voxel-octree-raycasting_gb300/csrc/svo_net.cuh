@@ -408,21 +408,29 @@ static_assert(kNetPer == kNetLayers, "one slice of the next tile's input per lay
 // front of the start; the refresh tile and the requested rays keep tracing
 // from the camera.
 constexpr float kGuideMargin = 4.0f;        // cells of the start distance's level of detail
-constexpr int kGuideBW = 32, kGuideBH = 8;  // pixels per block
+constexpr float kGuideLong = 64.0f;         // cells between the start and the pixel's own point: a long walk
+constexpr int kGuideBW = 32, kGuideBH = 8;  // pixels per block (whole ray packets of every packet shape)
 
 // Also lists the net tiles (kNetOutW x kNetOutH) holding an unguided pixel:
 // the first block to find one in a tile stamps the tile with this frame's
 // serial and appends it (a block of 32 x 8 pixels touches at most 2 x 2
-// tiles).
+// tiles). And it flags the walk packets (pw x ph, eight per block) that hold
+// a long walk: a pixel whose own reprojected point (else the farthest around
+// it) lies more than kGuideLong cells beyond its start -- a depth edge, where
+// the start comes from the near side. The tracer walks those packets first.
 __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams* __restrict__ P, TargetBuffers B) {
     __shared__ float dist[kGuideBH + 2][kGuideBW + 2];
     __shared__ uint32_t touched;
+    __shared__ uint32_t long_packets;  // bit k: packet k of this block holds a long walk
     const int res_x = B.res_x, res_y = B.res_y;
     const int x0 = blockIdx.x * kGuideBW, y0 = blockIdx.y * kGuideBH;
     const float cx = P->ray.px, cy = P->ray.py, cz = P->ray.pz;
     const uint32_t* __restrict__ col = plane_col(B, P->cur);
     const float4* __restrict__ xyz = plane_xyz(B, P->cur);
-    if (threadIdx.x == 0) touched = 0;
+    if (threadIdx.x == 0) {
+        touched = 0;
+        long_packets = 0;
+    }
     for (int i = threadIdx.x; i < (kGuideBW + 2) * (kGuideBH + 2); i += kGuideBW * kGuideBH) {
         const int wx = i % (kGuideBW + 2), wy = i / (kGuideBW + 2);
         const int gx = x0 + wx - 1, gy = y0 + wy - 1;
@@ -441,11 +449,16 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
     const int tx = threadIdx.x % kGuideBW, ty = threadIdx.x / kGuideBW;
     const int x = x0 + tx, y = y0 + ty;
     if (x < res_x && y < res_y) {
-        float m = INFINITY;
+        float m = INFINITY, far = 0.0f;
 #pragma unroll
         for (int j = 0; j < 3; ++j)
 #pragma unroll
-            for (int i = 0; i < 3; ++i) m = fminf(m, dist[ty + j][tx + i]);
+            for (int i = 0; i < 3; ++i) {
+                const float d = dist[ty + j][tx + i];
+                m = fminf(m, d);
+                if (d < INFINITY) far = fmaxf(far, d);
+            }
+        const float own = dist[ty + 1][tx + 1];
         float g = -1.0f;
         if (m < INFINITY) {
             const float s = m * 16.0f;  // raypos units
@@ -455,7 +468,13 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
                 sw *= 2.0f;
                 ++lod;
             }
-            g = fmaxf(s - kGuideMargin * (float)(1 << lod), 0.0f);
+            const float cell = (float)(1 << lod);
+            g = fmaxf(s - kGuideMargin * cell, 0.0f);
+            const float ahead = (own < INFINITY ? own : far) * 16.0f - g;
+            if (ahead > kGuideLong * cell) {
+                const int ps = P->pw_shift, pw = 1 << ps, ph = 32 >> ps;
+                atomicOr(&long_packets, 1u << ((tx >> ps) + (ty / ph) * (kGuideBW / pw)));
+            }
         } else {
             const int ntx = x / kNetOutW - x0 / kNetOutW, nty = y / kNetOutH - y0 / kNetOutH;
             atomicOr(&touched, 1u << (ntx + 2 * nty));
@@ -463,6 +482,13 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
         B.guide[(size_t)y * res_x + x] = g;
     }
     __syncthreads();
+    if (threadIdx.x < 8) {  // the block's eight walk packets
+        const int ps = P->pw_shift, pw = 1 << ps, ph = 32 >> ps;
+        const int per_row = kGuideBW / pw;
+        const int px = x0 / pw + (int)threadIdx.x % per_row, py = y0 / ph + (int)threadIdx.x / per_row;
+        const int wpx = (res_x + pw - 1) / pw, wpy = (res_y + ph - 1) / ph;
+        if (px < wpx && py < wpy) B.walk_long[(size_t)py * wpx + px] = (uint8_t)((long_packets >> threadIdx.x) & 1u);
+    }
     if (threadIdx.x < 4 && ((touched >> threadIdx.x) & 1u)) {
         const int tiles_x = (res_x + kNetOutW - 1) / kNetOutW;
         const uint32_t tile = (uint32_t)((y0 / kNetOutH + (int)(threadIdx.x >> 1)) * tiles_x + x0 / kNetOutW +
