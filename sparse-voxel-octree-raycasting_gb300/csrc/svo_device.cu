@@ -47,6 +47,7 @@ struct svo_context {
     bool stage_normal = true;               // stage the normal-node region in shared memory
     int pw_shift = 3;                       // ray packets (1<<pw_shift) x (32>>pw_shift): 8x4
     int block_pref = 0;                     // trace block size, 0: chosen by the staging size
+    int learned_block_pref = 0;             // the same for learned frames' tracer (not autotuned)
     uint64_t config_gen = 0;                // bumped by every option change (captured graphs re-capture)
     uint64_t launches = 0;
     std::vector<svo_target*> targets;  // live targets, destroyed with the context
@@ -325,9 +326,10 @@ svo_status plan_trace(svo_context* ctx, int kind, TraceLaunch& L) {
             stage_bytes = (uint32_t)bytes;
         }
     }
+    const int pref = kind == kTraceWarpBgrx ? ctx->learned_block_pref : ctx->block_pref;
     L.block = stage_bytes > kStageSmallBytes ? 1024 : 256;
-    if (ctx->block_pref == 1024) L.block = 1024;
-    if (ctx->block_pref == 256 && L.block == 1024) {  // the staged region does not fit a 256-thread block
+    if (pref == 1024) L.block = 1024;
+    if (pref == 256 && L.block == 1024) {  // the staged region does not fit a 256-thread block
         L.block = 256;
         L.o.n_smem = 0;
         stage_bytes = 0;
@@ -892,6 +894,11 @@ svo_status svo_context_set_option(svo_context* ctx, int option, int64_t value) {
             if (value != 0 && value != 256 && value != 1024)
                 return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "trace block 0 (auto), 256 or 1024");
             ctx->block_pref = (int)value;
+            return SVO_OK;
+        case SVO_OPT_LEARNED_TRACE_BLOCK:
+            if (value != 0 && value != 256 && value != 1024)
+                return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "learned trace block 0 (auto), 256 or 1024");
+            ctx->learned_block_pref = (int)value;
             return SVO_OK;
         default:
             return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "unknown option");

@@ -24,6 +24,7 @@ EMPTY_PIXEL = 0xFFFFFF00
 OPT_STAGE_NODES = 1
 OPT_PACKET_WIDTH = 2
 OPT_TRACE_BLOCK = 3
+OPT_LEARNED_TRACE_BLOCK = 4
 NOALLOC_MAX_VIEWS = 64
 DEFAULT_INITIAL_WORDS = 2097152
 STATUS = {
