@@ -166,8 +166,8 @@ __global__ void __launch_bounds__(256) k_project(const FrameParams* __restrict__
         const float shx = P->src_shift[r][0], shy = P->src_shift[r][1], shz = P->src_shift[r][2];
         for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += gridDim.x * blockDim.x) {
             const uint32_t c = col[s];
+            float4 q = __ldg(xyz + s);  // issued with the colour load, used only for non-empty pixels
             if (c == kEmptyPixel) continue;
-            float4 q = __ldg(xyz + s);
             if (rebase) {
                 q.x = __fadd_rn(q.x, shx);
                 q.y = __fadd_rn(q.y, shy);

@@ -437,11 +437,10 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
         float d = INFINITY;
         if (gx >= 0 && gx < res_x && gy >= 0 && gy < res_y) {
             const size_t o = (size_t)gy * res_x + gx;
-            if (__ldg(col + o) != kEmptyPixel) {
-                const float4 q = __ldg(xyz + o);
-                const float ax = q.x - cx, ay = q.y - cy, az = q.z - cz;
-                d = sqrtf(__fmaf_rn(ax, ax, __fmaf_rn(ay, ay, az * az)));
-            }
+            const uint32_t c = __ldg(col + o);  // both loads in flight together
+            const float4 q = __ldg(xyz + o);
+            const float ax = q.x - cx, ay = q.y - cy, az = q.z - cz;
+            if (c != kEmptyPixel) d = fast_len(__fmaf_rn(ax, ax, __fmaf_rn(ay, ay, az * az)));
         }
         dist[wy][wx] = d;
     }
