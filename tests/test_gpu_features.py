@@ -276,6 +276,37 @@ def test_trace_configurations_give_identical_frames(svo, scene, gpu_ctx):
     warp.close()
 
 
+def test_learned_trace_configurations_give_identical_frames(svo, scene, gpu_ctx):
+    # guided learned frames under every packet shape and learned-tracer block
+    # size: the same image (the walk and its start do not depend on them)
+    import os
+    octree = scene(9, 77, True)
+    gpu_ctx.upload(octree)
+    W, H = 160, 96
+    net = gpu_ctx.net()
+    net.load_file(os.path.join(os.path.dirname(svo.__file__), "net_weights.npy"))
+    frames = [svo.camera_path(2, 9, f, W, H) for f in range(6)]
+    want = None
+    for pw in (4, 8, 32):
+        for block in (0, 256, 1024):
+            gpu_ctx.set_option(svo.OPT_PACKET_WIDTH, pw)
+            gpu_ctx.set_option(svo.OPT_LEARNED_TRACE_BLOCK, block)
+            t = gpu_ctx.target(W, H)
+            t.set_guided(True)
+            for f, fv in enumerate(frames):
+                gpu_ctx.warp_frame_learned(t, fv, f, net, 0.5)
+            img = t.bgrx()
+            t.close()
+            if want is None:
+                want = img
+            assert np.array_equal(img, want), (pw, block)
+    gpu_ctx.set_option(svo.OPT_PACKET_WIDTH, 8)
+    gpu_ctx.set_option(svo.OPT_LEARNED_TRACE_BLOCK, 0)
+    with pytest.raises(svo.SvoError):
+        gpu_ctx.set_option(svo.OPT_LEARNED_TRACE_BLOCK, 512)
+    net.close()
+
+
 def test_autotune_picks_a_measured_configuration(svo, scene, gpu_ctx):
     octree = scene(9, 77, True)
     gpu_ctx.upload(octree)
