@@ -32,6 +32,8 @@ def _refresh_rect(f, W, H):
     (9, 1, 160, 96, 14, False),
     (9, 2, 160, 96, 14, True),
     (10, 2, 200, 120, 10, True),
+    (9, 2, 130, 70, 10, True),  # ragged: partial walk packets, guide blocks and net tiles
+    (8, 1, 37, 29, 10, False),
 ])
 def test_guided_walks_match_oracle(svo, orc, scene, gpu_ctx, depth, kind, W, H, frames, graph):
     octree = scene(depth, 77, True)
