@@ -385,6 +385,15 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     # trace packet shape / block size / node staging: measured on this GPU and scene
     tune = ctx.autotune(full, view(args.warmup), repeats=3) if args.autotune else []
     tuned = min(tune, key=lambda r: r["ms"]) if tune else None
+    # and the learned frames' tracer, on 16 learned frames of the same path
+    tune_l = []
+    if args.autotune:
+        tt = ctx.target(W, H)
+        tt.set_guided(bool(args.guided))
+        tt.use_graph(bool(args.graph))
+        tune_l = ctx.autotune_learned(tt, [view(f) for f in range(16)], net, thr)
+        tt.close()
+    tuned_l = min(tune_l, key=lambda r: r["ms"]) if tune_l else None
 
     def flush_l2():
         flush.zero_()
@@ -778,6 +787,9 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
             "autotune": {"chosen": tuned, "default_8x4_ms": next((r["ms"] for r in tune if r["packet_w"] == 8 and
                                                                  r["stage_nodes"] == 1 and r["block"] == 256), None),
                          "candidates": len(tune)} if tune else None,
+            "autotune_learned": {"chosen": tuned_l, "ms_per_frame": {f'{r["packet_w"]}x{r["packet_h"]}/{r["block"]}':
+                                                                    round(r["ms"], 4) for r in tune_l}}
+                                if tune_l else None,
             "parity_plain_vs_oracle": parity,
             "octree_build_s": t_build,
             **extras,

@@ -103,6 +103,10 @@ uint64_t svo_launch_count(const svo_context* ctx);
  * where it beat 1024 by 9% on guided frames), 256 or 1024.
  * svo_context_autotune, which times full raycasts, does not change it. */
 #define SVO_OPT_LEARNED_TRACE_BLOCK 4
+/* SVO_OPT_LEARNED_PACKET_WIDTH: ray packets of learned frames' tracer (and
+ * of their guide's long-walk flags): 0 (default: as SVO_OPT_PACKET_WIDTH),
+ * 4, 8, 16 or 32. */
+#define SVO_OPT_LEARNED_PACKET_WIDTH 5
 svo_status svo_context_set_option(svo_context* ctx, int option, int64_t value);
 
 /* Autotuner (no reference counterpart): times `repeats` full raycasts of
@@ -116,6 +120,15 @@ typedef struct svo_tune_result {
 } svo_tune_result;
 svo_status svo_context_autotune(svo_context* ctx, svo_target* t, const svo_view* view, int repeats,
                                 svo_tune_result* results, int cap, int* n_results);
+/* The same for learned frames' tracer (no reference counterpart): renders
+ * the n_views (>= 6) views as learned frames 0..n_views-1 into `t` (with the
+ * target's guided setting, the net and threshold given) for every packet
+ * shape and block size, times frames 4.. with CUDA events, and keeps the
+ * fastest as SVO_OPT_LEARNED_PACKET_WIDTH / SVO_OPT_LEARNED_TRACE_BLOCK.
+ * results[i].ms = milliseconds per frame. Synchronises. */
+svo_status svo_context_autotune_learned(svo_context* ctx, svo_target* t, const svo_view* views, int n_views,
+                                        const svo_net* net, float threshold, svo_tune_result* results, int cap,
+                                        int* n_results);
 
 /* ------------------------------------------------------------ octree -- */
 

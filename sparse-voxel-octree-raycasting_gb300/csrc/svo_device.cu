@@ -47,7 +47,8 @@ struct svo_context {
     bool stage_normal = true;               // stage the normal-node region in shared memory
     int pw_shift = 3;                       // ray packets (1<<pw_shift) x (32>>pw_shift): 8x4
     int block_pref = 0;                     // trace block size, 0: chosen by the staging size
-    int learned_block_pref = 0;             // the same for learned frames' tracer (not autotuned)
+    int learned_block_pref = 0;             // the same for learned frames' tracer
+    int learned_pw_shift = -1;              // learned frames' ray packets; -1: as pw_shift
     uint64_t config_gen = 0;                // bumped by every option change (captured graphs re-capture)
     uint64_t launches = 0;
     std::vector<svo_target*> targets;  // live targets, destroyed with the context
@@ -467,7 +468,7 @@ FrameParams make_params(const svo_target* t, const svo_view& v, int frame, const
     const int gx = (rx / 8 + 15) / 16 * 16, gy = (ry / 4 + 15) / 16 * 16;
     p.x_end = std::min(rx, p.add_x + gx);
     p.y_end = std::min(ry, p.add_y + gy);
-    p.pw_shift = t->ctx->pw_shift;
+    p.pw_shift = (learned && t->ctx->learned_pw_shift >= 0) ? t->ctx->learned_pw_shift : t->ctx->pw_shift;
     p.coarse_x = (rx / 2) * (frame & 1);
     p.coarse_y = (ry / 2) * ((frame >> 1) & 1);
     p.have_prev_view = t->have_prev_view ? 1 : 0;
@@ -899,6 +900,11 @@ svo_status svo_context_set_option(svo_context* ctx, int option, int64_t value) {
             if (value != 0 && value != 256 && value != 1024)
                 return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "learned trace block 0 (auto), 256 or 1024");
             ctx->learned_block_pref = (int)value;
+            return SVO_OK;
+        case SVO_OPT_LEARNED_PACKET_WIDTH:
+            if (value != 0 && value != 4 && value != 8 && value != 16 && value != 32)
+                return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "learned packet width 0 (as the others), 4, 8, 16 or 32");
+            ctx->learned_pw_shift = value == 0 ? -1 : value == 4 ? 2 : value == 8 ? 3 : value == 16 ? 4 : 5;
             return SVO_OK;
         default:
             return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "unknown option");
@@ -1425,6 +1431,55 @@ svo_status svo_context_autotune(svo_context* ctx, svo_target* t, const svo_view*
     ctx->pw_shift = best_cfg.pw == 4 ? 2 : best_cfg.pw == 8 ? 3 : best_cfg.pw == 16 ? 4 : best_cfg.pw == 32 ? 5 : pw0;
     ctx->block_pref = best_cfg.block;
     ctx->stage_normal = best_cfg.stage != 0;
+    ++ctx->config_gen;
+    if (n_results) *n_results = k;
+    return st;
+}
+
+svo_status svo_context_autotune_learned(svo_context* ctx, svo_target* t, const svo_view* views, int n_views,
+                                        const svo_net* net, float threshold, svo_tune_result* results, int cap,
+                                        int* n_results) {
+    if (!ctx || !t || !views || !net || t->ctx != ctx || net->ctx != ctx || n_views < 6)
+        return SVO_ERR_INVALID_ARGUMENT;
+    const int pw0 = ctx->learned_pw_shift, block0 = ctx->learned_block_pref;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    SVO_CUDA(ctx, cudaEventCreate(&e0));
+    SVO_CUDA(ctx, cudaEventCreate(&e1));
+    const int skip = 4;  // frames 0-1 have no cache; two more to settle the cache
+    svo_status st = SVO_OK;
+    float best = 1e30f;
+    int best_pw = pw0, best_block = block0, k = 0;
+    for (int pw : {4, 8, 16, 32})
+        for (int block : {256, 1024}) {
+            ctx->learned_pw_shift = pw == 4 ? 2 : pw == 8 ? 3 : pw == 16 ? 4 : 5;
+            ctx->learned_block_pref = block;
+            ++ctx->config_gen;
+            float ms = 0.0f;
+            for (int f = 0; f < n_views && st == SVO_OK; ++f) {
+                if (f == skip && cudaEventRecord(e0, ctx->stream) != cudaSuccess)
+                    st = fail(ctx, SVO_ERR_CUDA, "autotune timing");
+                if (st == SVO_OK) st = svo_warp_frame_learned(ctx, t, &views[f], f, net, threshold);
+            }
+            if (st == SVO_OK) {
+                if (cudaEventRecord(e1, ctx->stream) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess &&
+                    cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess)
+                    ms /= (float)(n_views - skip);
+                else
+                    st = fail(ctx, SVO_ERR_CUDA, "autotune timing");
+            }
+            if (st != SVO_OK) break;
+            if (results && k < cap) results[k] = svo_tune_result{pw, 32 / pw, block, ctx->stage_normal ? 1 : 0, ms};
+            ++k;
+            if (ms < best) {
+                best = ms;
+                best_pw = ctx->learned_pw_shift;
+                best_block = block;
+            }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->learned_pw_shift = best_pw;
+    ctx->learned_block_pref = best_block;
     ++ctx->config_gen;
     if (n_results) *n_results = k;
     return st;

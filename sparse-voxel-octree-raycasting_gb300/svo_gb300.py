@@ -25,6 +25,7 @@ OPT_STAGE_NODES = 1
 OPT_PACKET_WIDTH = 2
 OPT_TRACE_BLOCK = 3
 OPT_LEARNED_TRACE_BLOCK = 4
+OPT_LEARNED_PACKET_WIDTH = 5
 NOALLOC_MAX_VIEWS = 64
 DEFAULT_INITIAL_WORDS = 2097152
 STATUS = {
@@ -49,7 +50,7 @@ EXPORTS = [
     "svo_net_destroy", "svo_net_init", "svo_net_set_params", "svo_net_get_params", "svo_net_get_grads",
     "svo_net_forward", "svo_net_infer", "svo_net_backward", "svo_net_adam", "svo_target_set_cache_mode",
     "svo_target_set_coarse_refresh", "svo_octree_build", "svo_octree_info", "svo_octree_download",
-    "svo_context_autotune", "svo_target_set_guided", "svo_read_guide",
+    "svo_context_autotune", "svo_target_set_guided", "svo_read_guide", "svo_context_autotune_learned",
 ]
 
 NET_PARAMS = 6388
@@ -172,6 +173,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "svo_target_set_cache_mode": (i, [_P, i]),
         "svo_target_set_coarse_refresh": (i, [_P, i]),
         "svo_target_set_guided": (i, [_P, i]),
+        "svo_context_autotune_learned": (i, [_P, _P, _P, i, _P, ctypes.c_float, _P, i, ctypes.POINTER(i)]),
         "svo_read_guide": (i, [_P, _P]),
         "svo_octree_build": (i, [_P, _P, _P, _P, _P, sz, i, sz]),
         "svo_octree_info": (i, [_P, ctypes.POINTER(sz), ctypes.POINTER(u32), ctypes.POINTER(i)]),
@@ -380,6 +382,19 @@ class Context:
         n = ctypes.c_int()
         _check(self._lib.svo_context_autotune(self._h, target._h, ctypes.byref(view), repeats, ctypes.cast(res, _P),
                                               32, ctypes.byref(n)), self)
+        return [{"packet_w": r.packet_w, "packet_h": r.packet_h, "block": r.block, "stage_nodes": r.stage_nodes,
+                 "ms": r.ms} for r in res[:n.value]]
+
+    def autotune_learned(self, target: "Target", views: Sequence[View], net: "Net",
+                         threshold: float = 0.5) -> list[dict]:
+        """Times learned frames of `views` (>= 6, rendered as frames 0..n-1 with the
+        target's guided setting) for every packet shape and block size of their
+        tracer, keeps the fastest; returns the measurements (ms per frame)."""
+        arr = (View * len(views))(*views)
+        res = (TuneResult * 32)()
+        n = ctypes.c_int()
+        _check(self._lib.svo_context_autotune_learned(self._h, target._h, ctypes.cast(arr, _P), len(views), net._h,
+                                                      threshold, ctypes.cast(res, _P), 32, ctypes.byref(n)), self)
         return [{"packet_w": r.packet_w, "packet_h": r.packet_h, "block": r.block, "stage_nodes": r.stage_nodes,
                  "ms": r.ms} for r in res[:n.value]]
 

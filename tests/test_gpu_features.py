@@ -307,6 +307,30 @@ def test_learned_trace_configurations_give_identical_frames(svo, scene, gpu_ctx)
     net.close()
 
 
+def test_learned_autotune_picks_a_measured_configuration(svo, scene, gpu_ctx):
+    import os
+    octree = scene(9, 77, True)
+    gpu_ctx.upload(octree)
+    W, H = 160, 96
+    net = gpu_ctx.net()
+    net.load_file(os.path.join(os.path.dirname(svo.__file__), "net_weights.npy"))
+    t = gpu_ctx.target(W, H)
+    t.set_guided(True)
+    views = [svo.camera_path(1, 9, f, W, H) for f in range(8)]
+    res = gpu_ctx.autotune_learned(t, views, net, 0.5)
+    assert len(res) == 8 and all(r["ms"] > 0 for r in res)
+    assert {(r["packet_w"], r["block"]) for r in res} == {(w, b) for w in (4, 8, 16, 32) for b in (256, 1024)}
+    with pytest.raises(svo.SvoError):
+        gpu_ctx.autotune_learned(t, views[:5], net, 0.5)  # needs 6 views at least
+    for f, v in enumerate(views):  # frames render with the chosen configuration
+        gpu_ctx.warp_frame_learned(t, v, f, net, 0.5)
+    gpu_ctx.synchronize()
+    gpu_ctx.set_option(svo.OPT_LEARNED_PACKET_WIDTH, 0)
+    gpu_ctx.set_option(svo.OPT_LEARNED_TRACE_BLOCK, 0)
+    t.close()
+    net.close()
+
+
 def test_autotune_picks_a_measured_configuration(svo, scene, gpu_ctx):
     octree = scene(9, 77, True)
     gpu_ctx.upload(octree)
