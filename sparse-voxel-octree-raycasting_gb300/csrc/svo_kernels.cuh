@@ -552,19 +552,35 @@ __device__ __forceinline__ uint32_t read_lin(const uint32_t* __restrict__ s, con
     return kEmptyPixel;
 }
 
+// The block's 32x8 pixels and a 2-pixel halo are staged in shared memory
+// once; the neighbour reads of the filter come from there. A read the tile
+// cannot answer -- the reference's linear address running past the end of a
+// row (into the next one) or past the last row (into plane 1) -- goes to
+// global memory as read_lin has it.
 __global__ void __launch_bounds__(256) k_fill_colorize(const FrameParams* __restrict__ P, TargetBuffers B) {
-    const int idx = blockIdx.x * 32 + (threadIdx.x & 31);
-    const int idy = blockIdx.y * 8 + (threadIdx.x >> 5);
+    constexpr int kTW = 32, kTH = 8, kHalo = 2;
+    __shared__ uint32_t tile[kTH + 2 * kHalo][kTW + 2 * kHalo];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int x0 = blockIdx.x * kTW, y0 = blockIdx.y * kTH;
+    const int idx = x0 + tx, idy = y0 + ty;
     const int res_x = B.res_x, res_y = B.res_y;
-    if (idx >= res_x || idy >= res_y) return;
     const uint32_t* __restrict__ s = plane_col(B, P->cur);
     const uint32_t* __restrict__ next = P->fill_past >= 0 ? plane_col(B, P->fill_past) : nullptr;
+    for (int i = threadIdx.x; i < (kTH + 2 * kHalo) * (kTW + 2 * kHalo); i += 256) {
+        const int wx = i % (kTW + 2 * kHalo), wy = i / (kTW + 2 * kHalo);
+        const int gx = x0 + wx - kHalo, gy = y0 + wy - kHalo;
+        tile[wy][wx] = (gx >= 0 && gx < res_x && gy >= 0 && gy < res_y) ? __ldg(s + (size_t)gy * res_x + gx)
+                                                                         : kEmptyPixel;
+    }
+    __syncthreads();
+    if (idx >= res_x || idy >= res_y) return;
+    auto at = [&](int dx, int dy) -> uint32_t { return tile[ty + kHalo + dy][tx + kHalo + dx]; };
     const long long n = (long long)res_x * res_y;
     const long long ofs = (long long)idy * res_x + idx;
-    uint32_t col = __ldg(s + ofs);
+    uint32_t col = at(0, 0);
     if (col == kEmptyPixel && idx < res_x - 1 && idy < res_y - 1 && idx > 1 && idy > 1) {
-        const int c1 = (int)__ldg(s + ofs + 1), c2 = (int)__ldg(s + ofs - 1);
-        const int c3 = (int)__ldg(s + ofs + res_x), c4 = (int)__ldg(s + ofs - res_x);
+        const int c1 = (int)at(1, 0), c2 = (int)at(-1, 0);
+        const int c3 = (int)at(0, 1), c4 = (int)at(0, -1);
         const bool s1 = (uint32_t)c1 != kEmptyPixel, s2 = (uint32_t)c2 != kEmptyPixel;
         const bool s3 = (uint32_t)c3 != kEmptyPixel, s4 = (uint32_t)c4 != kEmptyPixel;
         if (s1 && s2 && s3 && s4) {
@@ -574,14 +590,16 @@ __global__ void __launch_bounds__(256) k_fill_colorize(const FrameParams* __rest
         } else if (s3 && s4) {
             col = (uint32_t)((c3 & 3) + ((((c3 & 0xfc) + (c4 & 0xfc)) >> 1) & 0xfc));
         } else {
-            for (int i = 0; i < 4; ++i) {
-                col = read_lin(s, next, ofs + (i & 1) + ((i >> 1) & 1) * res_x, n);
+            for (int i = 0; i < 4; ++i) {  // all four inside the frame here
+                col = at(i & 1, (i >> 1) & 1);
                 if (col != kEmptyPixel) break;
             }
             if (col == kEmptyPixel) {
                 for (int i = -2; i < 3 && col == kEmptyPixel; ++i)
                     for (int j = -2; j < 3; ++j) {
-                        col = read_lin(s, next, ofs + i + (long long)j * res_x, n);
+                        const int xi = idx + i, yj = idy + j;
+                        col = (xi < res_x && yj < res_y) ? at(i, j)
+                                                         : read_lin(s, next, ofs + i + (long long)j * res_x, n);
                         if (col != kEmptyPixel) break;
                     }
             }
