@@ -55,6 +55,13 @@ def oracle() -> ctypes.CDLL:
         lib.orc_raycast_full.argtypes = [i, _P, sz, u32, _P, _P, i, i, ctypes.c_float, ctypes.c_float, _P, _P, _P,
                                          _P, i]
         lib.orc_raycast_guided.argtypes = [i, _P, sz, u32, _P, _P, i, i, _P, _P, _P, _P, i]
+        lib.orc_guided_create.restype = _P
+        lib.orc_guided_create.argtypes = [i, i, i]
+        lib.orc_guided_free.argtypes = [_P]
+        lib.orc_guided_frame.argtypes = [_P, _P, sz, u32, _P, _P, i, i]
+        for name in ("orc_guided_colour", "orc_guided_coords", "orc_guided_guide"):
+            getattr(lib, name).restype = _P
+            getattr(lib, name).argtypes = [_P]
         lib.orc_warp_create.restype = _P
         lib.orc_warp_create.argtypes = [i, i]
         lib.orc_warp_free.argtypes = [_P]
@@ -173,6 +180,45 @@ def raycast_guided(depth, words, root, pos, m, res_x, res_y, s0, threads=0, stat
     if stats:
         return col, xyzw.reshape(n, 4), st
     return col, xyzw.reshape(n, 4)
+
+
+class Guided:
+    """Guided learned frames with every unguided pixel traced (the product's
+    learned frames on a guided target with a threshold no confidence reaches):
+    reprojection of the last frame's plane re-based by whole periods, start
+    distances, rays from the camera and walks. Test infrastructure only."""
+
+    def __init__(self, depth: int, res_x: int, res_y: int):
+        self.n = res_x * res_y
+        self._lib = oracle()
+        self._h = self._lib.orc_guided_create(depth, res_x, res_y)
+        if not self._h:
+            raise ValueError("guided frames: resolution must be at least 16x16")
+
+    def frame(self, words, root, pos, m, frame: int, threads: int = 0) -> None:
+        words = np.ascontiguousarray(words, np.uint32)
+        pos = np.ascontiguousarray(pos, np.float32)
+        m = np.ascontiguousarray(m, np.float32)
+        rc = self._lib.orc_guided_frame(self._h, _ptr(words), words.size, root, _ptr(pos), _ptr(m), frame, threads)
+        if rc != 0:
+            raise RuntimeError(f"orc_guided_frame failed: {rc}")
+
+    def colour(self) -> np.ndarray:
+        return np.ctypeslib.as_array(ctypes.cast(self._lib.orc_guided_colour(self._h), ctypes.POINTER(ctypes.c_uint32)),
+                                     (self.n,)).copy()
+
+    def coords(self) -> np.ndarray:
+        return np.ctypeslib.as_array(ctypes.cast(self._lib.orc_guided_coords(self._h), ctypes.POINTER(ctypes.c_float)),
+                                     (self.n * 4,)).copy().reshape(self.n, 4)
+
+    def guide(self) -> np.ndarray:
+        return np.ctypeslib.as_array(ctypes.cast(self._lib.orc_guided_guide(self._h), ctypes.POINTER(ctypes.c_float)),
+                                     (self.n,)).copy()
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.orc_guided_free(self._h)
+            self._h = None
 
 
 class Warp:

@@ -438,6 +438,14 @@ struct Warp {
     uint64_t rays = 0, child_fetches = 0, colour_fetches = 0, boundary_rays = 0;
 };
 
+inline void store_ray_plane(uint32_t* col, float* xyz, size_t ofs, const Ray& r) {
+    col[ofs] = r.colour;
+    xyz[ofs * 4 + 0] = r.hit[0];
+    xyz[ofs * 4 + 1] = r.hit[1];
+    xyz[ofs * 4 + 2] = r.hit[2];
+    xyz[ofs * 4 + 3] = r.dist;
+}
+
 inline void store_ray(Warp& w, size_t ofs, const Ray& r) {
     w.screen[ofs] = r.colour;
     w.back[ofs * 4 + 0] = r.hit[0];
@@ -705,6 +713,159 @@ int orc_raycast_guided(int depth, const uint32_t* words, size_t n_words, uint32_
         stats[1] = child;
         stats[2] = col;
     }
+    return 0;
+}
+
+// Guided learned frames with every unguided pixel traced: the product's
+// svo_warp_frame_learned on a guided target with a confidence threshold no
+// pixel reaches (the net then decides nothing; the reference has no such
+// frame). Two planes: the frame's plane and the last frame's, whose points are
+// reprojected after re-basing them by whole periods of the volume (the camera
+// wraps into it, src/raycast.h:136-145); then the start distances, then rays
+// from the camera for the refresh tile and the unguided pixels and walks for
+// the rest. Test infrastructure for the product's guided frames.
+struct Guided {
+    int res_x = 0, res_y = 0, depth = 0;
+    size_t N = 0;
+    std::vector<uint32_t> col[2];
+    std::vector<float> xyz[2];
+    std::vector<uint64_t> keys;
+    std::vector<float> guide;
+    float cache_pos[3] = {0, 0, 0};
+    int cache = -1;  // plane holding the last frame, -1 before the first frame
+};
+
+void* orc_guided_create(int depth, int res_x, int res_y) {
+    if (res_x < 16 || res_y < 16 || res_x > 65535 || res_y > 65535 || depth < 1 || depth > 20) return nullptr;
+    Guided* g = new Guided;
+    g->res_x = res_x;
+    g->res_y = res_y;
+    g->depth = depth;
+    g->N = (size_t)res_x * res_y;
+    for (int i = 0; i < 2; ++i) {
+        g->col[i].assign(g->N, kEmpty);
+        g->xyz[i].assign(g->N * 4, 0.0f);
+    }
+    g->keys.assign(g->N, ~0ull);
+    g->guide.assign(g->N, -1.0f);
+    return g;
+}
+void orc_guided_free(void* h) { delete static_cast<Guided*>(h); }
+const uint32_t* orc_guided_colour(void* h) {
+    Guided* g = static_cast<Guided*>(h);
+    return g->col[g->cache < 0 ? 0 : g->cache].data();
+}
+const float* orc_guided_coords(void* h) {
+    Guided* g = static_cast<Guided*>(h);
+    return g->xyz[g->cache < 0 ? 0 : g->cache].data();
+}
+const float* orc_guided_guide(void* h) { return static_cast<Guided*>(h)->guide.data(); }
+
+int orc_guided_frame(void* h, const uint32_t* words, size_t n_words, uint32_t root, const float* pos4,
+                     const float* m16, int frame, int threads) {
+    Guided& g = *static_cast<Guided*>(h);
+    const int res_x = g.res_x, res_y = g.res_y;
+    const size_t N = g.N;
+    View v = make_view(pos4, m16);
+    Tracer tr{words, n_words, root, g.depth};
+    if (threads > 0) omp_set_num_threads(threads);
+    const bool have_cache = frame >= 2 && g.cache >= 0;
+    const int cur = g.cache == 0 ? 1 : 0;
+    std::vector<uint32_t>& col = g.col[cur];
+    std::vector<float>& xyz = g.xyz[cur];
+    std::fill(col.begin(), col.end(), kEmpty);
+    if (have_cache) {
+        const std::vector<uint32_t>& sc = g.col[g.cache];
+        const std::vector<float>& sx = g.xyz[g.cache];
+        const float period = (float)(1u << (g.depth + 1)) / 16.0f;
+        float shift[3];
+        for (int i = 0; i < 3; ++i)
+            shift[i] = (float)std::nearbyint(((double)v.pos[i] - (double)g.cache_pos[i]) / period) * period;
+        std::atomic<uint64_t>* keys = reinterpret_cast<std::atomic<uint64_t>*>(g.keys.data());
+#pragma omp parallel for schedule(static)
+        for (long s0 = 0; s0 < (long)N; ++s0) {
+            if (sc[s0] == kEmpty) continue;
+            const float q[3] = {sx[s0 * 4 + 0] + shift[0], sx[s0 * 4 + 1] + shift[1], sx[s0 * 4 + 2] + shift[2]};
+            float p[3] = {q[0] - v.pos[0], q[1] - v.pos[1], q[2] - v.pos[2]};
+            float ph[3] = {dot3(p, v.vx), dot3(p, v.vy), dot3(p, v.vz)};
+            if (ph[2] < 0.05f) continue;
+            int px = proj_coord(ph[0] * (float)res_y, ph[2], (float)res_x / 2);
+            int py = proj_coord(ph[1] * (float)res_y, ph[2], (float)res_y / 2);
+            if (px >= res_x - 1 || px < 0 || py >= res_y - 1 || py < 0) continue;
+            uint32_t sz = (uint32_t)(int)(ph[2] * 1000.0f) << 8;
+            if (sz >= kEmpty) continue;
+            // the product reprojects the last frame's plane as cache plane 2 (plane bit 1)
+            uint64_t key = ((uint64_t)(sz | 1u) << 32) | (uint64_t)s0;
+            size_t t = (size_t)py * res_x + px;
+            uint64_t c = keys[t].load(std::memory_order_relaxed);
+            while (key < c && !keys[t].compare_exchange_weak(c, key, std::memory_order_relaxed)) {
+            }
+        }
+#pragma omp parallel for schedule(static)
+        for (long t = 0; t < (long)N; ++t) {
+            uint64_t key = g.keys[t];
+            if (key == ~0ull) continue;
+            g.keys[t] = ~0ull;
+            uint32_t src = (uint32_t)key, hi = (uint32_t)(key >> 32);
+            const float q[3] = {sx[(size_t)src * 4 + 0] + shift[0], sx[(size_t)src * 4 + 1] + shift[1],
+                                sx[(size_t)src * 4 + 2] + shift[2]};
+            float p[3] = {q[0] - v.pos[0], q[1] - v.pos[1], q[2] - v.pos[2]};
+            col[t] = (hi & ~255u) + (sc[src] & 255u);
+            xyz[t * 4 + 0] = q[0];
+            xyz[t * 4 + 1] = q[1];
+            xyz[t * 4 + 2] = q[2];
+            xyz[t * 4 + 3] = dot3(p, v.vz);
+        }
+    }
+    // start distances: the 3x3 minimum of the reprojected points' camera
+    // distances, less 4 cells of the level of detail there
+    std::vector<float> dist(N);
+#pragma omp parallel for schedule(static)
+    for (long t = 0; t < (long)N; ++t) {
+        float d = INFINITY;
+        if (col[t] != kEmpty) {
+            const float ax = xyz[t * 4 + 0] - v.pos[0], ay = xyz[t * 4 + 1] - v.pos[1], az = xyz[t * 4 + 2] - v.pos[2];
+            d = std::sqrt(ax * ax + ay * ay + az * az);
+        }
+        dist[t] = d;
+    }
+#pragma omp parallel for schedule(static)
+    for (long t = 0; t < (long)N; ++t) {
+        const int x = (int)(t % res_x), y = (int)(t / res_x);
+        float m = INFINITY;
+        for (int j = -1; j <= 1; ++j)
+            for (int i = -1; i <= 1; ++i) {
+                const int xi = x + i, yj = y + j;
+                if (xi >= 0 && xi < res_x && yj >= 0 && yj < res_y) m = std::fmin(m, dist[(size_t)yj * res_x + xi]);
+            }
+        float gd = -1.0f;
+        if (m < INFINITY) {
+            const float s = m * 16.0f;
+            float sw = (float)(2 * res_x);
+            int lod = 1;
+            while (s > sw && lod < 24) {
+                sw *= 2.0f;
+                ++lod;
+            }
+            gd = std::fmax(s - 4.0f * (float)(1 << lod), 0.0f);
+        }
+        g.guide[t] = gd;
+    }
+    // rays: the refresh tile (raycast.h:363-366) and the unguided pixels (all of
+    // them without a cache) from the camera, every other pixel walked
+    const int ax = (res_x / 8) * (frame & 7), ay = (res_y / 4) * ((frame >> 3) & 3);
+    const int xe = std::min(res_x, ax + (res_x / 8 + 15) / 16 * 16);
+    const int ye = std::min(res_y, ay + (res_y / 4 + 15) / 16 * 16);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int y = 0; y < res_y; ++y)
+        for (int x = 0; x < res_x; ++x) {
+            const size_t t = (size_t)y * res_x + x;
+            const bool rect = x >= ax && x < xe && y >= ay && y < ye;
+            const float s0 = (rect || !have_cache || g.guide[t] < 0.0f) ? 0.0f : g.guide[t];
+            store_ray_plane(col.data(), xyz.data(), t, tr.trace(v, x, y, res_x, res_y, 1.0f, 1.0f, s0));
+        }
+    g.cache = cur;
+    for (int i = 0; i < 3; ++i) g.cache_pos[i] = v.pos[i];
     return 0;
 }
 

@@ -439,8 +439,10 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
             const size_t o = (size_t)gy * res_x + gx;
             const uint32_t c = __ldg(col + o);  // both loads in flight together
             const float4 q = __ldg(xyz + o);
-            const float ax = q.x - cx, ay = q.y - cy, az = q.z - cz;
-            if (c != kEmptyPixel) d = fast_len(__fmaf_rn(ax, ax, __fmaf_rn(ay, ay, az * az)));
+            // exact IEEE operations, so the CPU oracle finds the same start distances
+            const float ax = __fsub_rn(q.x, cx), ay = __fsub_rn(q.y, cy), az = __fsub_rn(q.z, cz);
+            if (c != kEmptyPixel)
+                d = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(ax, ax), __fmul_rn(ay, ay)), __fmul_rn(az, az)));
         }
         dist[wy][wx] = d;
     }
@@ -460,7 +462,7 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
         const float own = dist[ty + 1][tx + 1];
         float g = -1.0f;
         if (m < INFINITY) {
-            const float s = m * 16.0f;  // raypos units
+            const float s = __fmul_rn(m, 16.0f);  // raypos units
             float sw = (float)(2 * res_x);
             int lod = 1;
             while (s > sw && lod < 24) {  // the walk's lodswitch doublings
@@ -468,7 +470,7 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
                 ++lod;
             }
             const float cell = (float)(1 << lod);
-            g = fmaxf(s - kGuideMargin * cell, 0.0f);
+            g = fmaxf(__fsub_rn(s, __fmul_rn(kGuideMargin, cell)), 0.0f);
             const float ahead = (own < INFINITY ? own : far) * 16.0f - g;
             if (ahead > kGuideLong * cell) {
                 const int ps = P->pw_shift, pw = 1 << ps, ph = 32 >> ps;

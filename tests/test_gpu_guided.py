@@ -69,6 +69,32 @@ def test_guided_walks_match_oracle(svo, orc, scene, gpu_ctx, depth, kind, W, H, 
     net.close()
 
 
+@pytest.mark.parametrize("depth,kind,W,H,frames", [(9, 2, 160, 96, 12), (9, 1, 200, 120, 10), (10, 2, 130, 70, 8)])
+def test_guided_frames_match_oracle_end_to_end(svo, orc, scene, gpu_ctx, depth, kind, W, H, frames):
+    # With a threshold no confidence reaches, a guided learned frame is fully
+    # determined without the net: reprojection (re-based across wraps), start
+    # distances, rays and walks. Every frame's start distances, colour words
+    # and hit bits equal the oracle's.
+    octree = scene(depth, 77, True)
+    gpu_ctx.upload(octree)
+    net = gpu_ctx.net()
+    net.load_file(_weights(svo))
+    t = gpu_ctx.target(W, H)
+    t.set_guided(True)
+    t.use_graph(True)
+    og = orc.Guided(depth, W, H)
+    for f in range(frames):
+        v = svo.camera_path(kind, depth, f, W, H)
+        gpu_ctx.warp_frame_learned(t, v, f, net, 0.999999)
+        og.frame(octree.words, octree.root, v.pos_array, v.m_array, f)
+        gpu_ctx.synchronize()
+        assert np.array_equal(t.guide().view(np.uint32), og.guide().view(np.uint32)), f"frame {f}: start distances"
+        assert np.array_equal(t.colour(2), og.colour()), f"frame {f}: colour words"
+        assert np.array_equal(t.coords(0).view(np.uint32), og.coords().view(np.uint32)), f"frame {f}: hit bits"
+    t.close()
+    net.close()
+
+
 def test_guide_is_conservative(svo, orc, scene, gpu_ctx):
     depth, W, H = 10, 320, 192
     octree = scene(depth, 2024, True)

@@ -33,3 +33,22 @@ def test_guided_walk_from_in_front_of_the_hit(svo, orc, scene):
     assert np.isclose(x1[hit, 3], x0[hit, 3], rtol=1e-4).mean() > 0.97
     # pixels with s0 < 0 are left alone
     assert np.all(c1[~hit] == 0xFFFFFF00)
+
+
+def test_oracle_guided_frames(svo, orc, scene):
+    # the oracle's guided frames (every unguided pixel traced): frames without a
+    # cache are the full raycast; afterwards most pixels are walked and nearly
+    # all of them land where the full raycast does
+    octree = scene(9, 77, True)
+    W, H = 96, 64
+    g = orc.Guided(9, W, H)
+    for f in range(8):
+        v = svo.camera_path(2, 9, f, W, H)
+        g.frame(octree.words, octree.root, v.pos_array, v.m_array, f)
+        full, _, _, _ = orc.raycast_full(9, octree.words, octree.root, v.pos_array, v.m_array, W, H)
+        col, gd = g.colour(), g.guide()
+        if f < 2:
+            assert np.all(gd == -1.0) and np.array_equal(col, full)
+        else:
+            assert (gd >= 0).mean() > 0.7
+            assert (col == full).mean() > 0.99
