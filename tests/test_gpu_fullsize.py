@@ -64,6 +64,33 @@ def test_warp_fullsize_bit_exact_and_consistent(svo, orc, big, gpu_ctx):
     full.close()
 
 
+def test_guided_frames_fullsize_match_oracle(svo, orc, big, gpu_ctx):
+    # the benchmark's guided learned frames with every unguided pixel traced
+    # (a threshold no confidence reaches): start distances, colour words and
+    # hit bits equal the oracle's guided frames at 1920x1024, on both camera paths
+    import os
+    gpu_ctx.upload(big)
+    net = gpu_ctx.net()
+    net.load_file(os.path.join(os.path.dirname(svo.__file__), "net_weights.npy"))
+    for kind in (1, 2):
+        t = gpu_ctx.target(W, H)
+        t.set_guided(True)
+        t.use_graph(True)
+        og = orc.Guided(DEPTH, W, H)
+        for f in range(6):
+            v = svo.camera_path(kind, DEPTH, 28 + f, W, H)
+            gpu_ctx.warp_frame_learned(t, v, f, net, 0.999999)
+            og.frame(big.words, big.root, v.pos_array, v.m_array, f)
+            gpu_ctx.synchronize()
+            g = t.guide()
+            assert np.array_equal(g.view(np.uint32), og.guide().view(np.uint32)), (kind, f)
+            assert np.array_equal(t.colour(2), og.colour()), (kind, f, int((t.colour(2) != og.colour()).sum()))
+            assert np.array_equal(t.coords(0).view(np.uint32), og.coords().view(np.uint32)), (kind, f)
+        assert (g >= 0).mean() > 0.8
+        t.close()
+    net.close()
+
+
 def test_warped_image_quality_is_reported(svo, big, gpu_ctx):
     gpu_ctx.upload(big)
     t = gpu_ctx.target(W, H)
