@@ -44,6 +44,8 @@ METRIC = "Mrays/s; 1920x1024 frames/s warped+learned vs full raycast at ≥38 dB
 WORKLOAD = ("warped + learned pipeline 1920x1024, depth-11 terrain octree, 256-frame orbit (0.5 deg/frame), "
             "confidence threshold 0.5")
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+# k_trace_warp of a guided learned frame at 1920x1024, depth 11: 16.62 MB read + 1.94 MB written
+GUIDED_TRACE_DRAM_BYTES = 16_619_776 + 1_937_152
 
 
 def parse_args(argv=None):
@@ -737,9 +739,13 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                     "peak_source": "measured" if hbm else "fallback", "algorithmic_bytes_per_launch": algo,
                     "bytes_per_ray": bytes_per_ray, "walk_bytes_per_ray": walk_bytes_per_ray,
                     "rays_per_launch": rays_camera + rays_walked, "walked_rays_per_launch": rays_walked,
-                    "traffic": None,
-                    "note": "issue-bound, not HBM-bound: 80% issue active, 37% SIMT lanes, 18 MB DRAM per "
-                            "launch (ncu); the node words stay in L2 and the staged shared-memory prefix"}
+                    # DRAM bytes read + written by this kernel in one ncu capture of the same
+                    # frame (the default configuration at 1920x1024; profile summary
+                    # k_trace_warp_guided_1920x1024_depth11.md); not measured in this run
+                    "traffic": GUIDED_TRACE_DRAM_BYTES if args.guided and (W, H, depth) == (1920, 1024, 11) else None,
+                    "traffic_source": "ncu capture (dram__bytes_read.sum + dram__bytes_write.sum), not this run",
+                    "note": "issue-bound, not HBM-bound: 83% issue active, 38% SIMT lanes (ncu); the node words "
+                            "stay in L2 and the staged shared-memory prefix"}
     if stage_ms_learned["net"] > 0:
         # 2 * 9 * (8*16 + 16*16 + 16*16 + 16*4) per output pixel, over the
         # tiles the net ran on (every tile unless guided)
