@@ -52,3 +52,25 @@ def test_oracle_guided_frames(svo, orc, scene):
         else:
             assert (gd >= 0).mean() > 0.7
             assert (col == full).mean() > 0.99
+
+
+def test_oracle_guided_frames_across_camera_wraps(svo, orc, scene):
+    # The camera wraps into the periodic volume (src/raycast.h:136-145); the
+    # guided frames re-base the cached points by whole periods, so a frame right
+    # after a wrap is still guided and still lands on the full raycast's voxels.
+    depth, W, H = 9, 96, 64
+    octree = scene(depth, 77, True)
+    period = 2 ** (depth + 1) / 16
+    g = orc.Guided(depth, W, H)
+    prev, wraps = None, 0
+    for f in range(60):
+        v = svo.camera_path(2, depth, f, W, H)
+        g.frame(octree.words, octree.root, v.pos_array, v.m_array, f)
+        p = v.pos_array[:3]
+        if prev is not None and np.any(np.abs(p - prev) > period / 2):
+            wraps += 1
+            full, _, _, _ = orc.raycast_full(depth, octree.words, octree.root, v.pos_array, v.m_array, W, H)
+            assert (g.guide() >= 0).mean() > 0.8, f
+            assert (g.colour() == full).mean() > 0.98, f
+        prev = p
+    assert wraps >= 2
