@@ -1,8 +1,10 @@
 """Benchmark: warped + learned sparse-voxel-octree frames/s at 1920x1024 on GB300.
 
-Workload (one step = one learned warp frame: the reference's raycast_draw
-reprojection, then the reconstruction net, then rays for the pixels the net is
-not confident about plus the 8x4 refresh tile): 1920x1024, depth-11 (2048^3)
+Workload (one step = one guided learned warp frame: the reference's
+raycast_draw reprojection, start distances from the reprojected depth, the
+reconstruction net on the tiles holding a pixel without one, then rays from the
+camera for the pixels the net is not confident about and the 8x4 refresh tile
+and walks from the start distance for the rest): 1920x1024, depth-11 (2048^3)
 seeded fBm terrain octree (visible shell), orbit camera at 1.5x extent, 0.5
 degrees yaw per frame, height sinusoid 0.02x extent over 64 frames; the net's
 weights are the committed ones (train_net.py). Reported beside it: the plain
@@ -41,8 +43,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "sparse-voxel-octree-raycasting_gb300"))
 
 METRIC = "Mrays/s; 1920x1024 frames/s warped+learned vs full raycast at ≥38 dB PSNR"
-WORKLOAD = ("warped + learned pipeline 1920x1024, depth-11 terrain octree, 256-frame orbit (0.5 deg/frame), "
-            "confidence threshold 0.5")
+WORKLOAD = ("warped + learned pipeline 1920x1024 (guided walks from the reprojected depth, the net on the "
+            "unguided pixels), depth-11 terrain octree, 256-frame orbit (0.5 deg/frame), confidence threshold 0.5")
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # k_trace_warp of a guided learned frame at 1920x1024, depth 11: 16.62 MB read + 1.94 MB written
 GUIDED_TRACE_DRAM_BYTES = 16_619_776 + 1_937_152
