@@ -43,6 +43,16 @@ def test_context_without_gpu_fails_loudly(svo):
         svo.Context(0)
 
 
+def test_null_handles_are_rejected(svo):
+    # the guided-frame and autotuner entry points check their handles before
+    # touching a device (1 = SVO_ERR_INVALID_ARGUMENT)
+    lib = svo.load()
+    assert lib.svo_target_set_guided(None, 1) == 1
+    assert lib.svo_read_guide(None, None) == 1
+    assert lib.svo_context_autotune_learned(None, None, None, 0, None, 0.5, None, 0, None) == 1
+    assert lib.svo_context_set_option(None, svo.OPT_LEARNED_PACKET_WIDTH, 8) == 1
+
+
 def test_look_at_rows_are_orthonormal_and_aim(svo):
     pos = np.array([10.0, 40.0, -30.0], np.float32)
     tgt = np.array([32.0, 20.0, 32.0], np.float32)
