@@ -164,10 +164,8 @@ __global__ void __launch_bounds__(256) k_project(const FrameParams* __restrict__
         uint32_t* __restrict__ col = plane_col(B, phys);
         const float4* __restrict__ xyz = plane_xyz(B, phys);
         const float shx = P->src_shift[r][0], shy = P->src_shift[r][1], shz = P->src_shift[r][2];
-        for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += gridDim.x * blockDim.x) {
-            const uint32_t c = col[s];
-            float4 q = __ldg(xyz + s);  // issued with the colour load, used only for non-empty pixels
-            if (c == kEmptyPixel) continue;
+        auto project_one = [&](uint32_t s, uint32_t c, float4 q) {
+            if (c == kEmptyPixel) return;
             if (rebase) {
                 q.x = __fadd_rn(q.x, shx);
                 q.y = __fadd_rn(q.y, shy);
@@ -177,18 +175,31 @@ __global__ void __launch_bounds__(256) k_project(const FrameParams* __restrict__
             const float zz = dot3(ax, ay, az, vz);
             if (zz < 0.05f) {  // (double)z < 0.05 <=> z < 0.05f for a binary32 z
                 if (clear) col[s] = kEmptyPixel;
-                continue;
+                return;
             }
             const int sx = proj_coord(__fmul_rn(dot3(ax, ay, az, vx), fry), zz, hx);
             const int sy = proj_coord(__fmul_rn(dot3(ax, ay, az, vy), fry), zz, hy);
             if (sx >= res_x - 1 || sx < 0 || sy >= res_y - 1 || sy < 0) {
                 if (clear) col[s] = kEmptyPixel;
-                continue;
+                return;
             }
             const uint32_t sz = (uint32_t)__float2int_rz(__fmul_rn(zz, 1000.0f)) << 8;
-            if (sz >= kEmptyPixel) continue;  // cannot beat the cleared value (kernel.cl:571)
+            if (sz >= kEmptyPixel) return;  // cannot beat the cleared value (kernel.cl:571)
             const uint32_t t = (uint32_t)sy * (uint32_t)res_x + (uint32_t)sx;
             atomicMin((unsigned long long*)(B.keys + t), (unsigned long long)(((uint64_t)(sz | (uint32_t)r) << 32) | s));
+        };
+        // two sources per thread and iteration, their loads in flight together
+        // (the atomicMin outcome does not depend on the order)
+        const uint32_t stride = gridDim.x * blockDim.x;
+        for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += 2u * stride) {
+            const uint32_t s2 = s + stride;
+            const bool two = s2 < N;
+            const uint32_t c1 = col[s];
+            const float4 q1 = __ldg(xyz + s);
+            const uint32_t c2 = two ? col[s2] : kEmptyPixel;
+            const float4 q2 = two ? __ldg(xyz + s2) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            project_one(s, c1, q1);
+            if (two) project_one(s2, c2, q2);
         }
     }
 }
