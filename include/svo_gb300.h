@@ -347,11 +347,16 @@ svo_status svo_net_adam(svo_net* net, float lr, float beta1, float beta2, float 
  * of views, 7 KiB -- is a static device array that exists once per device
  * while the library is loaded; the views beyond SVO_NOALLOC_MAX_VIEWS do not
  * fit in it and are rejected with SVO_ERR_CAPACITY.
- * The first call on a device looks up that array's device address; make the
- * first call before any stream capture. Every call shares the array (it keeps
- * the last call's contents; the counter and fault flags are cleared at the
- * start of each call), so calls that overlap on the GPU -- from two host
- * threads or on two streams at once -- race; issue them one after another.
+ * Alignment: d_words 4 bytes, colour and bgrx 4, voxel 8, xyzw 16 (one
+ * float4 store per pixel); a misaligned pointer, like a null one, is rejected
+ * with SVO_ERR_INVALID_ARGUMENT before any CUDA call.
+ * The first call in a CUDA context (normally the device's primary context;
+ * a context the host made current through the driver API counts as its own)
+ * looks up that array's device address in it; make the first call before any
+ * stream capture. Every call shares the array (it keeps the last call's
+ * contents; the counter and fault flags are cleared at the start of each
+ * call), so calls that overlap on the GPU -- from two host threads or on two
+ * streams at once -- race; issue them one after another.
  * The call runs on `stream` (null = the default stream) and returns when the
  * rays are written, with SVO_ERR_DEVICE_FAULT if a kernel flagged an
  * out-of-range node word. */

@@ -7,10 +7,14 @@
 # copy of them is written anywhere). TEST INFRASTRUCTURE ONLY: the library is
 # the checker that pins the oracle restatement and makes the golden fixtures.
 #
-# usage: oracle/build_ref.sh [reference_dir]   (default /root/reference)
-# Exits 0 without building when the reference tree is absent.
+# usage: oracle/build_ref.sh <reference_dir>   (or SVO_REFERENCE_DIR set)
+# Exits 0 without building when no reference tree is given or it is absent.
 set -euo pipefail
-REF="${1:-${SVO_REFERENCE_DIR:-/root/reference}}"
+REF="${1:-${SVO_REFERENCE_DIR:-}}"
+if [ -z "$REF" ]; then
+    echo "build_ref: no reference directory given (argument or SVO_REFERENCE_DIR); skipped"
+    exit 0
+fi
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 KCL="$REF/kernel/kernel.cl"

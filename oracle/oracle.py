@@ -27,6 +27,13 @@ def _ptr(a):
     return a.ctypes.data_as(_P)
 
 
+def reference_dir() -> str | None:
+    """The reference source tree: SVO_REFERENCE_DIR, else a checkout named
+    `reference` beside this repository; None when neither exists."""
+    cand = os.environ.get("SVO_REFERENCE_DIR") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+    return cand if os.path.isfile(os.path.join(cand, "kernel", "kernel.cl")) else None
+
+
 def build(force: bool = False) -> None:
     """Compiles the oracle restatement (always possible) and, when the
     reference tree is present, the reference's own sources (_ref)."""
@@ -35,7 +42,9 @@ def build(force: bool = False) -> None:
         subprocess.run(["bash", os.path.join(HERE, "build_oracle.sh")], check=True, capture_output=True)
     ref_inputs = [os.path.join(HERE, f) for f in ("ref_shim.h", "ref_driver.inc", "ref_capi.inc", "build_ref.sh")]
     if force or not os.path.exists(REF_LIB) or os.path.getmtime(REF_LIB) < max(os.path.getmtime(f) for f in ref_inputs):
-        subprocess.run(["bash", os.path.join(HERE, "build_ref.sh")], check=True, capture_output=True)
+        ref = reference_dir()
+        if ref:
+            subprocess.run(["bash", os.path.join(HERE, "build_ref.sh"), ref], check=True, capture_output=True)
 
 
 def oracle() -> ctypes.CDLL:

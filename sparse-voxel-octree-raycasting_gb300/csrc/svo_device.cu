@@ -1321,6 +1321,11 @@ int svo_target_stage_times(svo_target* t, float* ms, int cap) {
     return k;
 }
 
+// Largest packet count of one trace launch: the warps' work counter runs past
+// the total by at most one increment per resident warp before they stop, and
+// must not wrap around 2^32.
+constexpr uint64_t kMaxBatchPackets = 0xFF000000ull;
+
 static svo_status check_view(svo_context* ctx, const svo_target* t, const svo_view* v) {
     if (!v) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "null view");
     if (v->res_x != t->res_x || v->res_y != t->res_y) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "view resolution differs from the target");
@@ -1340,6 +1345,13 @@ svo_status svo_raycast_full_batch(svo_context* ctx, svo_target* const* targets, 
     ctx->batch_slot = (slot + 1) % svo_context::kRing;
     // The slot's previous copy must have left the staging buffer.
     SVO_CUDA(ctx, cudaEventSynchronize(ctx->batch_done[slot]));
+    {  // the packet numbers of the whole batch must fit the 32-bit work counter
+        const int pw = 1 << ctx->pw_shift, ph = 32 >> ctx->pw_shift;
+        uint64_t total = 0;
+        for (int i = 0; i < n; ++i)
+            total += (uint64_t)((views[i].res_x + pw - 1) / pw) * (uint64_t)((views[i].res_y + ph - 1) / ph);
+        if (total > kMaxBatchPackets) return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "batch has too many ray packets");
+    }
     FullBatch* hb = ctx->h_batch[slot];
     hb->n_views = n;
     uint32_t packets = 0;
@@ -1910,20 +1922,58 @@ static_assert(SVO_NOALLOC_MAX_VIEWS <= kMaxBatchViews, "view table larger than t
 // the symbol; its device address comes from cudaGetSymbolAddress.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-constexpr int kMaxDevices = 64;
+// The device address of a __device__ array belongs to the CUDA context that
+// was current when it was looked up; a host that makes its own driver-API
+// context current, or resets the device, gets another one. So the address is
+// cached per context, keyed by the context's process-unique id (a handle
+// value can be reused after a context is destroyed).
+typedef int (*PfnCtxGetCurrent)(void** ctx);
+typedef int (*PfnCtxGetId)(void* ctx, unsigned long long* id);
+constexpr int kMaxContexts = 64;
+struct ScratchEntry {
+    unsigned long long ctx_id;
+    unsigned char* ptr;
+};
 std::mutex g_setup_mutex;
-unsigned char* g_scratch_ptr[kMaxDevices] = {};
+ScratchEntry g_scratch[kMaxContexts] = {};
+int g_scratch_used = 0, g_scratch_next = 0;
+PfnCtxGetCurrent g_ctx_get_current = nullptr;
+PfnCtxGetId g_ctx_get_id = nullptr;
 
-// Device address of g_noalloc_scratch on the current device, looked up once
-// per device.
+// Device address of g_noalloc_scratch in the current context, looked up the
+// first time a context calls (with that context current).
 svo_status scratch_address(int device, unsigned char** out) {
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_ptr[device]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return SVO_ERR_CUDA;
-        g_scratch_ptr[device] = static_cast<unsigned char*>(p);
+    if (!g_ctx_get_current || !g_ctx_get_id) {
+        cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 4000, cudaEnableDefault, &q1) != cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+            q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            return SVO_ERR_CUDA;
+        g_ctx_get_current = reinterpret_cast<PfnCtxGetCurrent>(f1);
+        g_ctx_get_id = reinterpret_cast<PfnCtxGetId>(f2);
     }
-    *out = g_scratch_ptr[device];
+    void* ctx = nullptr;
+    unsigned long long id = 0;
+    if (g_ctx_get_current(&ctx) != 0) return SVO_ERR_CUDA;
+    if (!ctx) {
+        // No context current on this thread yet: bind the device's primary
+        // context, the one the runtime would use.
+        if (cudaSetDevice(device) != cudaSuccess || g_ctx_get_current(&ctx) != 0) return SVO_ERR_CUDA;
+    }
+    if (!ctx || g_ctx_get_id(ctx, &id) != 0) return SVO_ERR_CUDA;
+    for (int i = 0; i < g_scratch_used; ++i)
+        if (g_scratch[i].ctx_id == id) {
+            *out = g_scratch[i].ptr;
+            return SVO_OK;
+        }
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return SVO_ERR_CUDA;
+    const int slot = g_scratch_used < kMaxContexts ? g_scratch_used++ : (g_scratch_next++ % kMaxContexts);
+    g_scratch[slot] = ScratchEntry{id, static_cast<unsigned char*>(p)};
+    *out = static_cast<unsigned char*>(p);
     return SVO_OK;
 }
 
@@ -1948,14 +1998,25 @@ extern "C" svo_status svo_raycast_full_noalloc(const uint32_t* d_words, size_t n
         return SVO_ERR_INVALID_ARGUMENT;
     if (depth < SVO_MIN_DEPTH || depth > SVO_MAX_DEPTH) return SVO_ERR_INVALID_ARGUMENT;
     if (n_views > SVO_NOALLOC_MAX_VIEWS) return SVO_ERR_CAPACITY;
+    // Every pointer is checked before any CUDA call: the kernel reads the
+    // words as uint32 and stores uint32, uint64 and float4 per pixel, so a
+    // caller buffer at an offset (a sub-allocation from its own pool) that is
+    // not aligned for those would fault the GPU instead of returning an error.
+    if (reinterpret_cast<uintptr_t>(d_words) & 3u) return SVO_ERR_INVALID_ARGUMENT;
+    uint64_t packets_total = 0;
     for (int i = 0; i < n_views; ++i) {
         const svo_view& v = views[i];
         const svo_frame_buffers& o = outputs[i];
         if (v.res_x < 1 || v.res_y < 1 || v.res_x > 65535 || v.res_y > 65535) return SVO_ERR_INVALID_ARGUMENT;
         if (!o.colour || !o.xyzw || !o.voxel || !o.bgrx) return SVO_ERR_INVALID_ARGUMENT;
+        if ((reinterpret_cast<uintptr_t>(o.xyzw) & 15u) || (reinterpret_cast<uintptr_t>(o.voxel) & 7u) ||
+            (reinterpret_cast<uintptr_t>(o.colour) & 3u) || (reinterpret_cast<uintptr_t>(o.bgrx) & 3u))
+            return SVO_ERR_INVALID_ARGUMENT;
+        packets_total += (uint64_t)((v.res_x + 7) / 8) * (uint64_t)((v.res_y + 3) / 4);
     }
+    if (packets_total > kMaxBatchPackets) return SVO_ERR_INVALID_ARGUMENT;
     int device = 0;
-    if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= kMaxDevices) return SVO_ERR_CUDA;
+    if (cudaGetDevice(&device) != cudaSuccess) return SVO_ERR_CUDA;
     unsigned char* scratch = nullptr;
     svo_status st = scratch_address(device, &scratch);
     if (st != SVO_OK) return st;

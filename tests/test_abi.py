@@ -116,3 +116,31 @@ def test_terrain_is_periodic_and_colours_nonzero(svo):
     # every column has its surface voxel
     cols = np.unique(z.astype(np.int64) * 256 + x)
     assert cols.size == 256 * 256
+
+
+def test_noalloc_rejects_misaligned_pointers_before_any_launch(svo):
+    # Caller buffers at an offset (a sub-allocation from the caller's own pool)
+    # that are not aligned for the kernel's stores are refused with
+    # SVO_ERR_INVALID_ARGUMENT before any CUDA call, so this runs without a
+    # GPU: the pointers are never dereferenced.
+    import ctypes
+
+    lib = svo.load()
+    v = svo.camera_path(3, 9, 0, 16, 16)
+    base = 1 << 20  # a fake, suitably aligned device address
+
+    def call(words, colour, xyzw, voxel, bgrx, n_views=1, view=v):
+        varr = (svo.View * n_views)(*([view] * n_views))
+        fb = svo.FrameBuffers(colour, xyzw, voxel, bgrx)
+        oarr = (svo.FrameBuffers * n_views)(*([fb] * n_views))
+        return lib.svo_raycast_full_noalloc(ctypes.c_void_p(words), 100, 0, 9, ctypes.cast(varr, ctypes.c_void_p),
+                                            ctypes.cast(oarr, ctypes.c_void_p), n_views, None)
+
+    ok = (base, base + 4096, base + 8192, base + 16384, base + 32768)
+    for which, off in ((0, 2), (1, 2), (2, 8), (2, 4), (3, 4), (4, 1)):
+        args = list(ok)
+        args[which] += off
+        assert call(*args) == 1, (which, off)
+    # a batch whose packet count would wrap the 32-bit work counter
+    big = svo.camera_path(3, 9, 0, 65535, 65535)
+    assert call(*ok, n_views=svo.NOALLOC_MAX_VIEWS, view=big) == 1
