@@ -109,6 +109,14 @@ uint64_t svo_launch_count(const svo_context* ctx);
 #define SVO_OPT_LEARNED_PACKET_WIDTH 5
 svo_status svo_context_set_option(svo_context* ctx, int option, int64_t value);
 
+/* Read-bandwidth probe (no reference counterpart; a measurement aid): reads
+ * `bytes` of the device buffer d_buf (16-byte aligned) `passes` times on the
+ * context's stream with L1-bypassing 16-byte loads, after one untimed pass,
+ * and returns the achieved GB/s (device events around the timed launch). A
+ * buffer that fits in L2 measures the L2 read bandwidth the trace and warp
+ * kernels' rooflines are quoted against. Synchronises the stream. */
+svo_status svo_measure_read_bandwidth(svo_context* ctx, const void* d_buf, size_t bytes, int passes, double* gbs);
+
 /* Autotuner (no reference counterpart): times `repeats` full raycasts of
  * `view` into `t` for every packet shape (4x8, 8x4, 16x2, 32x1), block size
  * (256, 1024) and node staging (on, off), keeps the fastest in the context

@@ -818,7 +818,8 @@ int orc_guided_frame(void* h, const uint32_t* words, size_t n_words, uint32_t ro
         }
     }
     // start distances: the 3x3 minimum of the reprojected points' camera
-    // distances, less 4 cells of the level of detail there
+    // distances, less 4 cells of the level of detail there; half that minimum
+    // for a pixel with a hole (a pixel of the frame without a point) in its 3x3
     std::vector<float> dist(N);
 #pragma omp parallel for schedule(static)
     for (long t = 0; t < (long)N; ++t) {
@@ -833,10 +834,15 @@ int orc_guided_frame(void* h, const uint32_t* words, size_t n_words, uint32_t ro
     for (long t = 0; t < (long)N; ++t) {
         const int x = (int)(t % res_x), y = (int)(t / res_x);
         float m = INFINITY;
+        bool near_hole = false;
         for (int j = -1; j <= 1; ++j)
             for (int i = -1; i <= 1; ++i) {
                 const int xi = x + i, yj = y + j;
-                if (xi >= 0 && xi < res_x && yj >= 0 && yj < res_y) m = std::fmin(m, dist[(size_t)yj * res_x + xi]);
+                if (xi >= 0 && xi < res_x && yj >= 0 && yj < res_y) {
+                    const size_t o = (size_t)yj * res_x + xi;
+                    m = std::fmin(m, dist[o]);
+                    near_hole |= col[o] == kEmpty;
+                }
             }
         float gd = -1.0f;
         if (m < INFINITY) {
@@ -847,7 +853,7 @@ int orc_guided_frame(void* h, const uint32_t* words, size_t n_words, uint32_t ro
                 sw *= 2.0f;
                 ++lod;
             }
-            gd = std::fmax(s - 4.0f * (float)(1 << lod), 0.0f);
+            gd = near_hole ? s * 0.5f : std::fmax(s - 4.0f * (float)(1 << lod), 0.0f);
         }
         g.guide[t] = gd;
     }

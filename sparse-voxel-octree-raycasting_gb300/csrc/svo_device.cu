@@ -839,7 +839,8 @@ svo_status svo_context_create(int device, svo_context** out) {
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) return cleanup(SVO_ERR_CUDA);
     if (cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
         return cleanup(SVO_ERR_CUDA);
-    if (cudaMalloc(&ctx->d_fault, sizeof(uint32_t)) != cudaSuccess) return cleanup(SVO_ERR_OUT_OF_MEMORY);
+    // [0] fault flags, [1] sink word of the read-bandwidth probe
+    if (cudaMalloc(&ctx->d_fault, 2 * sizeof(uint32_t)) != cudaSuccess) return cleanup(SVO_ERR_OUT_OF_MEMORY);
     if (cudaMalloc(&ctx->d_counter, sizeof(uint32_t)) != cudaSuccess) return cleanup(SVO_ERR_OUT_OF_MEMORY);
     for (int i = 0; i < svo_context::kRing; ++i) {
         if (cudaMalloc(&ctx->d_batch[i], sizeof(FullBatch)) != cudaSuccess) return cleanup(SVO_ERR_OUT_OF_MEMORY);
@@ -847,7 +848,7 @@ svo_status svo_context_create(int device, svo_context** out) {
         if (cudaEventCreateWithFlags(&ctx->batch_done[i], cudaEventDisableTiming) != cudaSuccess)
             return cleanup(SVO_ERR_CUDA);
     }
-    if (cudaMemsetAsync(ctx->d_fault, 0, sizeof(uint32_t), ctx->stream) != cudaSuccess) return cleanup(SVO_ERR_CUDA);
+    if (cudaMemsetAsync(ctx->d_fault, 0, 2 * sizeof(uint32_t), ctx->stream) != cudaSuccess) return cleanup(SVO_ERR_CUDA);
     if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return cleanup(SVO_ERR_CUDA);
     *out = ctx;
     return SVO_OK;
@@ -909,6 +910,53 @@ svo_status svo_context_set_option(svo_context* ctx, int option, int64_t value) {
         default:
             return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "unknown option");
     }
+}
+
+// Read-bandwidth probe (the L2 roofline's denominator): every block sums
+// 16-byte loads over the buffer in a grid-stride loop, `passes` times, with
+// L1-bypassing loads, so a buffer that fits in L2 but not in the SMs' L1s is
+// read from L2 on every pass. One word per block keeps the loads live.
+__global__ void __launch_bounds__(512) k_read_probe(const uint4* __restrict__ p, size_t n16, int passes,
+                                                    uint32_t* __restrict__ sink) {
+    uint32_t acc = 0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (int r = 0; r < passes; ++r) {
+        size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+        for (; i + 3 * stride < n16; i += 4 * stride) {  // four loads in flight per thread
+            const uint4 a = __ldcg(p + i), b = __ldcg(p + i + stride), c = __ldcg(p + i + 2 * stride),
+                        d = __ldcg(p + i + 3 * stride);
+            acc += a.x ^ b.y ^ c.z ^ d.w;
+        }
+        for (; i < n16; i += stride) acc += __ldcg(p + i).x;
+    }
+    acc = __reduce_xor_sync(0xffffffffu, acc);
+    if ((threadIdx.x & 31) == 0 && acc == 0x9e3779b9u) atomicAdd(sink, 1u);  // almost never stores
+}
+
+svo_status svo_measure_read_bandwidth(svo_context* ctx, const void* d_buf, size_t bytes, int passes, double* gbs) {
+    if (!ctx || !d_buf || !gbs || bytes < 16 || passes < 1 || (reinterpret_cast<uintptr_t>(d_buf) & 15u))
+        return SVO_ERR_INVALID_ARGUMENT;
+    const int sms = ctx->sm_count;
+    cudaEvent_t e0, e1;
+    SVO_CUDA(ctx, cudaEventCreate(&e0));
+    SVO_CUDA(ctx, cudaEventCreate(&e1));
+    const size_t n16 = bytes / 16;
+    const dim3 grid((unsigned)(sms * 4)), block(512);
+    // one untimed launch warms the buffer into L2 (when it fits there)
+    k_read_probe<<<grid, block, 0, ctx->stream>>>(static_cast<const uint4*>(d_buf), n16, 1, ctx->d_fault + 1);
+    SVO_LAUNCHED(ctx);
+    cudaEventRecord(e0, ctx->stream);
+    k_read_probe<<<grid, block, 0, ctx->stream>>>(static_cast<const uint4*>(d_buf), n16, passes, ctx->d_fault + 1);
+    SVO_LAUNCHED(ctx);
+    cudaEventRecord(e1, ctx->stream);
+    svo_status st = SVO_OK;
+    if (cudaEventSynchronize(e1) != cudaSuccess) st = fail(ctx, SVO_ERR_CUDA, "read probe");
+    float ms = 0.0f;
+    if (st == SVO_OK && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) st = fail(ctx, SVO_ERR_CUDA, "read probe events");
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st == SVO_OK) *gbs = (double)(n16 * 16) * passes / ((double)ms * 1e-3) / 1e9;
+    return st;
 }
 
 svo_status svo_synchronize(svo_context* ctx) {

@@ -399,7 +399,7 @@ static_assert(kNetPer == kNetLayers, "one slice of the next tile's input per lay
 // nearest cached surface around it instead of from the camera: the start
 // distance is the smallest camera distance of the reprojected points in the
 // pixel's 3x3 neighbourhood, less kGuideMargin cells of the level of detail
-// at that distance. A cached point that is a ray end rather than a hit (the
+// at that distance (half that smallest distance next to a hole). A cached point that is a ray end rather than a hit (the
 // ray left the volume through its top or bottom, or reached the view
 // distance limit) bounds its neighbours the same way: their rays are walked
 // from just in front of where it ended. A pixel with no cached point around
@@ -407,7 +407,15 @@ static_assert(kNetPer == kNetLayers, "one slice of the next tile's input per lay
 // ray. The walk is exact unless a surface the cache has not seen lies in
 // front of the start; the refresh tile and the requested rays keep tracing
 // from the camera.
+// A pixel next to a hole (a pixel of the frame that reprojection left
+// without a point) is where a surface the cache never saw -- newly uncovered
+// by the camera's motion -- most often lies in front of the cached points:
+// its walk starts at half the 3x3 minimum distance instead. (On the
+// fast-motion camera path at 1920x1024 this took whole guided frames from
+// 35.5 to 39.2 dB against the full raycast, with every unguided pixel traced,
+// for 3% more node fetches than starting there at the usual margin.)
 constexpr float kGuideMargin = 4.0f;        // cells of the start distance's level of detail
+constexpr float kGuideNearHole = 0.5f;      // start distance factor of a pixel next to a hole
 constexpr float kGuideLong = 64.0f;         // cells between the start and the pixel's own point: a long walk
 constexpr int kGuideBW = 32, kGuideBH = 8;  // pixels per block (whole ray packets of every packet shape)
 
@@ -420,6 +428,7 @@ constexpr int kGuideBW = 32, kGuideBH = 8;  // pixels per block (whole ray packe
 // the start comes from the near side. The tracer walks those packets first.
 __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams* __restrict__ P, TargetBuffers B) {
     __shared__ float dist[kGuideBH + 2][kGuideBW + 2];
+    __shared__ uint8_t hole[kGuideBH + 2][kGuideBW + 2];  // a pixel of the frame without a point
     __shared__ uint32_t touched;
     __shared__ uint32_t long_packets;  // bit k: packet k of this block holds a long walk
     const int res_x = B.res_x, res_y = B.res_y;
@@ -435,6 +444,7 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
         const int wx = i % (kGuideBW + 2), wy = i / (kGuideBW + 2);
         const int gx = x0 + wx - 1, gy = y0 + wy - 1;
         float d = INFINITY;
+        uint8_t h = 0;
         if (gx >= 0 && gx < res_x && gy >= 0 && gy < res_y) {
             const size_t o = (size_t)gy * res_x + gx;
             const uint32_t c = __ldg(col + o);  // both loads in flight together
@@ -443,14 +453,18 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
             const float ax = __fsub_rn(q.x, cx), ay = __fsub_rn(q.y, cy), az = __fsub_rn(q.z, cz);
             if (c != kEmptyPixel)
                 d = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(ax, ax), __fmul_rn(ay, ay)), __fmul_rn(az, az)));
+            else
+                h = 1;
         }
         dist[wy][wx] = d;
+        hole[wy][wx] = h;
     }
     __syncthreads();
     const int tx = threadIdx.x % kGuideBW, ty = threadIdx.x / kGuideBW;
     const int x = x0 + tx, y = y0 + ty;
     if (x < res_x && y < res_y) {
         float m = INFINITY, far = 0.0f;
+        bool near_hole = false;
 #pragma unroll
         for (int j = 0; j < 3; ++j)
 #pragma unroll
@@ -458,6 +472,7 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
                 const float d = dist[ty + j][tx + i];
                 m = fminf(m, d);
                 if (d < INFINITY) far = fmaxf(far, d);
+                near_hole |= hole[ty + j][tx + i] != 0;
             }
         const float own = dist[ty + 1][tx + 1];
         float g = -1.0f;
@@ -470,7 +485,7 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
                 ++lod;
             }
             const float cell = (float)(1 << lod);
-            g = fmaxf(__fsub_rn(s, __fmul_rn(kGuideMargin, cell)), 0.0f);
+            g = near_hole ? __fmul_rn(s, kGuideNearHole) : fmaxf(__fsub_rn(s, __fmul_rn(kGuideMargin, cell)), 0.0f);
             const float ahead = (own < INFINITY ? own : far) * 16.0f - g;
             if (ahead > kGuideLong * cell) {
                 const int ps = P->pw_shift, pw = 1 << ps, ph = 32 >> ps;

@@ -51,6 +51,7 @@ EXPORTS = [
     "svo_net_forward", "svo_net_infer", "svo_net_backward", "svo_net_adam", "svo_target_set_cache_mode",
     "svo_target_set_coarse_refresh", "svo_octree_build", "svo_octree_info", "svo_octree_download",
     "svo_context_autotune", "svo_target_set_guided", "svo_read_guide", "svo_context_autotune_learned",
+    "svo_measure_read_bandwidth",
 ]
 
 NET_PARAMS = 6388
@@ -125,6 +126,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "svo_last_error": (ctypes.c_char_p, [_P]),
         "svo_context_stream": (_P, [_P]),
         "svo_synchronize": (i, [_P]),
+        "svo_measure_read_bandwidth": (i, [_P, _P, ctypes.c_size_t, i, ctypes.POINTER(ctypes.c_double)]),
         "svo_launch_count": (ctypes.c_uint64, [_P]),
         "svo_context_set_option": (i, [_P, i, ctypes.c_int64]),
         "svo_octree_upload": (i, [_P, _P, sz, u32, i, i]),
@@ -403,6 +405,14 @@ class Context:
 
     def set_l2_window(self, nbytes: int) -> None:
         _check(self._lib.svo_octree_set_l2_window(self._h, nbytes), self)
+
+    def read_bandwidth(self, d_buf: int, nbytes: int, passes: int = 20) -> float:
+        """GB/s of the library's read probe over a device buffer (see
+        svo_measure_read_bandwidth); an L2-resident buffer gives the L2 read
+        bandwidth."""
+        g = ctypes.c_double()
+        _check(self._lib.svo_measure_read_bandwidth(self._h, _P(d_buf), nbytes, passes, ctypes.byref(g)), self)
+        return g.value
 
     def synchronize(self) -> None:
         _check(self._lib.svo_synchronize(self._h), self)
