@@ -179,6 +179,13 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def _json_default(o):
+    """numpy scalars in the JSON line as plain numbers."""
+    if hasattr(o, "item"):
+        return o.item()
+    raise TypeError(f"{type(o).__name__} is not JSON serialisable")
+
+
 def measured_peaks() -> dict:
     try:
         with open(PEAKS_FILE) as f:
@@ -998,7 +1005,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                                                      f"of the orbit at {W}x{H} (the reference's algorithm)",
                     "gpu_frames_per_s": plain_fps, "cpu_frames_per_s": cpu["value"], "cpu_cores": cpu["cores"],
                     "ratio": plain_fps / cpu["value"]}
-        fast_gate = q_fast["psnr_db"] >= 38.0
+        fast_gate = bool(q_fast["psnr_db"] >= 38.0)
         line = {
             "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -1048,7 +1055,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
             "octree_build_s": t_build,
             **extras,
         }
-        print(json.dumps(line), flush=True)
+        print(json.dumps(line, default=_json_default), flush=True)
     for t in (tgt_l, full):
         t.close()
     net.close()

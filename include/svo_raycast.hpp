@@ -49,6 +49,7 @@ struct State {
     int res_x = 0, res_y = 0;
     int frame = -1;  // the static frame counter of raycast_draw (raycast.h:104)
     std::vector<uint32_t> framebuffer;
+    svo_view view{};  // the camera of the last frame
 };
 inline State& state() {
     static State s;
@@ -125,11 +126,15 @@ inline void raycast_draw(int res_x, int res_y) {
     for (int i = 0; i < 3; ++i) camera.pos[i] = p[i];
     svo_view v;
     check(svo_view_from_euler(camera.rot[0], camera.rot[1], camera.rot[2], p, res_x, res_y, 1.0f, &v), "camera");
+    s.view = v;
     check(svo_warp_frame(s.ctx, s.target, &v, s.frame), "raycast_draw");
     check(svo_read_bgrx(s.target, s.framebuffer.data()), "framebuffer readback");
 }
 
 inline const std::vector<uint32_t>& raycast_framebuffer() { return state().framebuffer; }
+// The camera raycast_draw derived for the last frame (position wrapped into
+// the volume, view matrix from svo::camera.rot).
+inline const svo_view& raycast_last_view() { return state().view; }
 
 inline void raycast_exit() {
     State& s = state();

@@ -146,7 +146,7 @@ def raycast_full(depth, words, root, pos, m, res_x, res_y, fovx=1.0, fovy=1.0, t
     """raycast_fine_2 over the whole frame. Returns colour words, float4 per
     pixel (xyz hit, distance; the reference path leaves w at 0), packed hit
     voxels (oracle only) and [rays, child fetches, colour fetches, boundary rays,
-    loop iterations, longest walk]."""
+    loop iterations, longest walk, hit-boundary rays]."""
     words = np.ascontiguousarray(words, np.uint32)
     pos = np.ascontiguousarray(pos, np.float32)
     m = np.ascontiguousarray(m, np.float32)
@@ -155,7 +155,7 @@ def raycast_full(depth, words, root, pos, m, res_x, res_y, fovx=1.0, fovy=1.0, t
     xyzw = np.zeros(n * 4, np.float32)
     if which == "oracle":
         vox = np.empty(n, np.uint64)
-        st = np.zeros(6, np.uint64)
+        st = np.zeros(7, np.uint64)
         rc = oracle().orc_raycast_full(depth, _ptr(words), words.size, root, _ptr(pos), _ptr(m), res_x, res_y, fovx,
                                        fovy, _ptr(col), _ptr(xyzw), _ptr(vox), _ptr(st), threads)
         if rc != 0:

@@ -201,6 +201,7 @@ struct Ray {
     uint64_t voxel;    // packed hit cell, see encode_voxel
     uint32_t child_fetches, colour_fetches, steps;
     bool boundary;     // a non-stepping coordinate landed within 1 ulp of an integer
+    bool hit_boundary; // the hit point lies within 1 ulp of a face of its hit cell (other than the entry face)
 };
 
 struct Tracer {
@@ -331,6 +332,7 @@ struct Tracer {
         for (int i = 0; i < 20; ++i) stack[i] = root;
         bool hit = false;
         int hit_cell[3] = {0, 0, 0};
+        int last_axis = -1;  // axis of the last step (the hit cell's entry face)
         const uint32_t step_cap = 1u << 22;
 
         do {
@@ -346,6 +348,13 @@ struct Tracer {
                 if (rek <= lod) {
                     hit = true;
                     for (int a = 0; a < 3; ++a) hit_cell[a] = p0i[a];
+                    const float cell = (float)(1 << rek);
+                    for (int a = 0; a < 3; ++a) {
+                        if (a == last_axis) continue;
+                        const float c = rp[a], f = cell * std::nearbyint(c / cell);
+                        if (std::fabs(c - f) <= std::nextafter(std::fabs(c), INFINITY) - std::fabs(c))
+                            r.hit_boundary = true;
+                    }
                     break;
                 }
                 --rek;
@@ -359,6 +368,7 @@ struct Tracer {
             int axis = 0;
             if (isec_dist[1] < isec_dist[axis]) axis = 1;
             if (isec_dist[2] < isec_dist[axis]) axis = 2;
+            last_axis = axis;
             for (int a = 0; a < 3; ++a) rp[a] = rp[a] + g[axis][a] * mul0[axis];
             for (int a = 0; a < 3; ++a) {
                 rpi[a] = (int)rp[a];
@@ -639,17 +649,19 @@ void orc_octree_free(void* h) { delete static_cast<OrcOctree*>(h); }
 
 // raycast_fine_2 over the whole frame. Outputs per pixel: colour word, float4
 // (hit xyz, distance), packed hit cell and per-ray counters. Any output may be
-// null. stats[0..5] = rays, child fetches, colour fetches, boundary rays,
-// loop iterations, longest walk (iterations).
+// null. stats[0..6] = rays, child fetches, colour fetches, boundary rays (a
+// step landed a coordinate within 1 ulp of a leaf face), loop iterations,
+// longest walk (iterations), hit-boundary rays (the hit point within 1 ulp of
+// a face of its hit cell other than the entry face).
 int orc_raycast_full(int depth, const uint32_t* words, size_t n_words, uint32_t root, const float* pos4,
                      const float* m16, int res_x, int res_y, float fovx, float fovy, uint32_t* colour, float* xyzw,
                      uint64_t* voxel, uint64_t* stats, int threads) {
     if (res_x <= 0 || res_y <= 0 || res_x > 65535 || res_y > 65535) return -1;
     Tracer tr{words, n_words, root, depth};
     View v = make_view(pos4, m16);
-    uint64_t child = 0, col = 0, bnd = 0, steps = 0, max_steps = 0;
+    uint64_t child = 0, col = 0, bnd = 0, hbnd = 0, steps = 0, max_steps = 0;
     if (threads > 0) omp_set_num_threads(threads);
-#pragma omp parallel for schedule(dynamic, 4) reduction(+ : child, col, bnd, steps) reduction(max : max_steps)
+#pragma omp parallel for schedule(dynamic, 4) reduction(+ : child, col, bnd, hbnd, steps) reduction(max : max_steps)
     for (int y = 0; y < res_y; ++y)
         for (int x = 0; x < res_x; ++x) {
             Ray r = tr.trace(v, x, y, res_x, res_y, fovx, fovy);
@@ -665,6 +677,7 @@ int orc_raycast_full(int depth, const uint32_t* words, size_t n_words, uint32_t 
             child += r.child_fetches;
             col += r.colour_fetches;
             bnd += r.boundary ? 1 : 0;
+            hbnd += r.hit_boundary ? 1 : 0;
             steps += r.steps;
             if (r.steps > max_steps) max_steps = r.steps;
         }
@@ -675,6 +688,7 @@ int orc_raycast_full(int depth, const uint32_t* words, size_t n_words, uint32_t 
         stats[3] = bnd;
         stats[4] = steps;
         stats[5] = max_steps;
+        stats[6] = hbnd;
     }
     return 0;
 }

@@ -56,6 +56,16 @@ WARP_CASES = [
     (8, 5, True, 1, 10, 64, 48),
     (9, 7, True, 2, 6, 80, 56),
 ]
+# The benchmark's own size and depths (digests only): the depth-11 terrain of
+# the 1920x1024 benchmark, and depth 12 (4096^3), whose terrain needs more
+# pointer nodes than the reference builder allows (octree.h:78), so its words
+# come from the product builder (their digest is stored) and only the
+# raycast and warp frames are the reference's.
+FULLSIZE_CASES = [
+    # depth, seed, shell, full-raycast frame, warp frames, W, H
+    (11, 2024, True, 40, 4, 1920, 1024),
+    (12, 2024, True, 40, 4, 1920, 1024),
+]
 
 
 def main() -> None:
@@ -110,6 +120,38 @@ def main() -> None:
         out[key + "_last_tex"] = w.tex()
         meta["warp"].append({"key": key, "depth": depth, "seed": seed, "shell": shell, "kind": kind,
                              "frames": frames, "W": W, "H": H, "per_frame": per_frame})
+    meta["fullsize"] = []
+    for depth, seed, shell, frame, frames, W, H in FULLSIZE_CASES:
+        x, y, z, c = svo.terrain_voxels(seed, depth, shell)
+        if depth <= 11:
+            words, root = oracle.build_octree(depth, x, y, z, c, which="reference")
+            builder = "reference"
+        else:
+            o = svo.build_terrain(depth, seed, shell)
+            words, root = o.words, o.root
+            builder = "product"
+        case = {"depth": depth, "seed": seed, "shell": shell, "W": W, "H": H, "voxel_digest": digest(x, y, z, c),
+                "builder": builder, "n_words": int(words.size), "root": int(root), "words_digest": digest(words),
+                "frame": frame}
+        del x, y, z, c
+        v = svo.camera_path(1, depth, frame, W, H)
+        col, xyzw, _, _ = oracle.raycast_full(depth, words, root, v.pos_array, v.m_array, W, H, 1.0, 1.0,
+                                              which="reference")
+        case["camera_digest"] = digest(v.pos_array, v.m_array)
+        case["colour_digest"] = digest(col)
+        case["xyz_digest"] = digest(np.ascontiguousarray(xyzw[:, :3]))
+        w = oracle.Warp(depth, W, H, which="reference")
+        per_frame = []
+        for f in range(frames):
+            v = svo.camera_path(1, depth, f, W, H)
+            w.frame(words, root, v.pos_array, v.m_array, f)
+            screen = w.screen()
+            per_frame.append({"camera_digest": digest(v.pos_array, v.m_array), "holes": w.hole_count(),
+                              "ids_digest": digest(w.ids()), "plane0_digest": digest(screen[0]),
+                              "plane2_digest": digest(screen[2]), "tex_digest": digest(w.tex())})
+        case["warp"] = per_frame
+        meta["fullsize"].append(case)
+        print("fullsize case", depth, "done", flush=True)
     np.savez_compressed(os.path.join(HERE, "golden.npz"), **out)
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(meta, f, indent=1)

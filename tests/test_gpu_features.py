@@ -183,11 +183,26 @@ def test_reference_named_cpp_interface(svo, tmp_path):
     subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
                     os.path.join(ROOT, "tests", "cpp", "raycast_mirror.cpp"), "-o", exe, "-L", lib_dir,
                     "-lsvo_gb300", f"-Wl,-rpath,{lib_dir}"], check=True)
-    out = subprocess.run([exe, "6"], capture_output=True, text=True, timeout=120)
+    dump = str(tmp_path / "frames.bin")
+    frames, W, H = 6, 256, 160
+    out = subprocess.run([exe, str(frames), dump], capture_output=True, text=True, timeout=120)
     assert out.returncode == 0, out.stderr
-    assert "frames=6" in out.stdout
+    assert f"frames={frames}" in out.stdout
     nonblack = int(out.stdout.split("nonblack=")[1])
-    assert nonblack > 256 * 160 // 4
+    assert nonblack > W * H // 4
+    # every frame the C++ layer drew equals the oracle's warp frame for the
+    # same camera, bit for bit (the layer's default scene: the depth-8 seeded
+    # terrain, seed 2024, visible shell)
+    import oracle
+
+    octree = svo.build_terrain(8, 2024, True)
+    rec = np.fromfile(dump, np.uint32).reshape(frames, 20 + W * H)
+    w = oracle.Warp(8, W, H)
+    for f in range(frames):
+        pos = rec[f, :4].view(np.float32)
+        m = rec[f, 4:20].view(np.float32)
+        w.frame(octree.words, octree.root, pos, m, f)
+        assert np.array_equal(rec[f, 20:], w.tex()), f"frame {f}: BGRX differs from the oracle"
 
 
 def test_concurrent_camera_streams_share_one_octree(svo, scene, gpu_ctx):

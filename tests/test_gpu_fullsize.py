@@ -24,9 +24,55 @@ def test_full_raycast_fullsize_bit_exact(svo, orc, big, gpu_ctx):
     assert np.array_equal(col, ocol), f"{int((col != ocol).sum())} of {W * H} colour words differ"
     assert np.array_equal(xyzw.view(np.uint32), oxyzw.view(np.uint32))
     assert np.array_equal(t.voxels(), ovox)
-    # boundary rays (a coordinate within 1 ulp of a leaf face) are reported,
-    # not excused: every ray above matched bit for bit
-    assert stats[3] < stats[0]
+    # Rays a step of which landed a coordinate within 1 ulp of a leaf face
+    # (stats[3]; 5% at this depth, the walks being hundreds of steps long) and
+    # rays whose hit point lies within 1 ulp of a face of its cell (stats[6])
+    # are counted; none is excused: every ray above matched bit for bit, the
+    # flagged ones included.
+    assert stats[3] > 0 and stats[6] < 1e-3 * stats[0]
+    t.close()
+
+
+def _digest(*arrays):
+    import hashlib
+
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+@pytest.mark.parametrize("idx", [0, 1])
+def test_fullsize_gpu_matches_reference_golden(svo, scene, gpu_ctx, idx):
+    """The GPU against the reference's own outputs (digests in tests/golden,
+    made by kernel.cl/octree.h compiled for the host) at the benchmark's size:
+    depth 11 and depth 12 at 1920x1024, one full raycast and four warp frames."""
+    import json
+    import os
+
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "golden.json")) as f:
+        case = json.load(f)["fullsize"][idx]
+    depth = case["depth"]
+    octree = scene(depth, case["seed"], case["shell"])
+    assert _digest(octree.words) == case["words_digest"], "octree words differ from the reference builder's"
+    gpu_ctx.upload(octree)
+    t = gpu_ctx.target(W, H)
+    v = svo.camera_path(1, depth, case["frame"], W, H)
+    gpu_ctx.raycast_full(t, v)
+    gpu_ctx.synchronize()
+    col, xyzw = t.full()
+    assert _digest(col) == case["colour_digest"], "full raycast colour words"
+    assert _digest(np.ascontiguousarray(xyzw[:, :3])) == case["xyz_digest"], "full raycast hit positions"
+    for f, want in enumerate(case["warp"]):
+        v = svo.camera_path(1, depth, f, W, H)
+        gpu_ctx.warp_frame(t, v, f)
+        gpu_ctx.synchronize()
+        ids, n = t.holes()
+        assert n == want["holes"], f"frame {f}: hole count"
+        assert _digest(ids) == want["ids_digest"], f"frame {f}: hole list"
+        assert _digest(t.colour(0)) == want["plane0_digest"], f"frame {f}: displayed plane"
+        assert _digest(t.colour(2)) == want["plane2_digest"], f"frame {f}: cache plane"
+        assert _digest(t.bgrx()) == want["tex_digest"], f"frame {f}: BGRX"
     t.close()
 
 

@@ -36,6 +36,10 @@ def test_full_raycast_bit_exact(svo, orc, scene, gpu_ctx, depth, shell, kind, W,
     assert np.array_equal(xyzw.view(np.uint32), oxyzw.view(np.uint32)), "hit position/distance bits differ"
     assert np.array_equal(vox, ovox), "hit voxels differ"
     assert np.array_equal(tgt.bgrx(), orc.colorize(ocol))
+    if (W, H, depth, shell) == (512, 512, 9, False):
+        # the plain full raycast configuration: rays whose hit point lies within
+        # 1 ulp of a face of its cell stay under 1e-4 of all rays (and match anyway)
+        assert stats[6] < 1e-4 * stats[0], int(stats[6])
     tgt.close()
 
 

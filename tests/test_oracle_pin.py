@@ -219,3 +219,54 @@ def test_oracle_coarse_refresh_fills_holes(svo, orc):
         a.frame(words, root, v.pos_array, v.m_array, f)
         b.frame(words, root, v.pos_array, v.m_array, f, coarse=True)
     assert b.hole_count() <= a.hole_count()
+
+
+# ------------------------------------------------ the benchmark's own size --
+@pytest.mark.parametrize("idx", [0, 1])
+def test_oracle_fullsize_matches_golden(svo, orc, golden, idx):
+    """1920x1024 at depth 11 (the benchmark's terrain; words from the
+    reference builder) and depth 12: one full raycast and four warp frames
+    against the reference's digests -- where the compact format's offsets and
+    local roots span their full range and horizon rays run to VIEW_DIST_MAX."""
+    meta, _ = golden
+    case = meta["fullsize"][idx]
+    depth, W, H = case["depth"], case["W"], case["H"]
+    x, y, z, c = svo.terrain_voxels(case["seed"], depth, case["shell"])
+    assert _digest(x, y, z, c) == case["voxel_digest"], "the synthetic terrain generator changed"
+    if case["builder"] == "reference":
+        words, root = orc.build_octree(depth, x, y, z, c)
+    else:
+        o = svo.build_terrain(depth, case["seed"], case["shell"])
+        words, root = o.words, o.root
+    del x, y, z, c
+    assert words.size == case["n_words"] and root == case["root"] and _digest(words) == case["words_digest"]
+    v = svo.camera_path(1, depth, case["frame"], W, H)
+    assert _digest(v.pos_array, v.m_array) == case["camera_digest"]
+    col, xyzw, _, st = orc.raycast_full(depth, words, root, v.pos_array, v.m_array, W, H)
+    assert _digest(col) == case["colour_digest"], "full raycast colour words"
+    assert _digest(np.ascontiguousarray(xyzw[:, :3])) == case["xyz_digest"], "full raycast hit positions"
+    w = orc.Warp(depth, W, H)
+    for f, want in enumerate(case["warp"]):
+        v = svo.camera_path(1, depth, f, W, H)
+        assert _digest(v.pos_array, v.m_array) == want["camera_digest"]
+        w.frame(words, root, v.pos_array, v.m_array, f)
+        screen = w.screen()
+        assert w.hole_count() == want["holes"], f"frame {f}"
+        assert _digest(w.ids()) == want["ids_digest"], f"frame {f}: hole list"
+        assert _digest(screen[0]) == want["plane0_digest"], f"frame {f}: displayed plane"
+        assert _digest(screen[2]) == want["plane2_digest"], f"frame {f}: cache plane"
+        assert _digest(w.tex()) == want["tex_digest"], f"frame {f}: BGRX"
+
+
+@needs_ref
+def test_oracle_fullsize_depth11_matches_reference_directly(svo, orc):
+    """The depth-11 benchmark scene at 1920x1024, oracle against the compiled
+    reference itself on a frame the golden set does not hold."""
+    depth, W, H = 11, 1920, 1024
+    o = svo.build_terrain(depth, 2024, True)
+    v = svo.camera_path(1, depth, 131, W, H)
+    rc, rx, _, _ = orc.raycast_full(depth, o.words, o.root, v.pos_array, v.m_array, W, H, which="reference")
+    oc, ox, _, _ = orc.raycast_full(depth, o.words, o.root, v.pos_array, v.m_array, W, H)
+    assert np.array_equal(rc, oc)
+    assert np.array_equal(np.ascontiguousarray(rx[:, :3]).view(np.uint32),
+                          np.ascontiguousarray(ox[:, :3]).view(np.uint32))
