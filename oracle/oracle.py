@@ -64,6 +64,7 @@ def oracle() -> ctypes.CDLL:
         lib.orc_raycast_full.argtypes = [i, _P, sz, u32, _P, _P, i, i, ctypes.c_float, ctypes.c_float, _P, _P, _P,
                                          _P, i]
         lib.orc_raycast_guided.argtypes = [i, _P, sz, u32, _P, _P, i, i, _P, _P, _P, _P, i]
+        lib.orc_raycast_guided_steps.argtypes = [i, _P, sz, u32, _P, _P, i, i, _P, _P, i]
         lib.orc_guided_create.restype = _P
         lib.orc_guided_create.argtypes = [i, i, i]
         lib.orc_guided_free.argtypes = [_P]
@@ -189,6 +190,20 @@ def raycast_guided(depth, words, root, pos, m, res_x, res_y, s0, threads=0, stat
     if stats:
         return col, xyzw.reshape(n, 4), st
     return col, xyzw.reshape(n, 4)
+
+
+def raycast_guided_steps(depth, words, root, pos, m, res_x, res_y, s0, threads=0):
+    """Loop iterations of each pixel's guided walk (0 where s0 < 0)."""
+    words = np.ascontiguousarray(words, np.uint32)
+    s0 = np.ascontiguousarray(s0, np.float32)
+    steps = np.zeros(res_x * res_y, np.uint32)
+    rc = oracle().orc_raycast_guided_steps(depth, _ptr(words), words.size, root,
+                                           _ptr(np.ascontiguousarray(pos, np.float32)),
+                                           _ptr(np.ascontiguousarray(m, np.float32)), res_x, res_y, _ptr(s0),
+                                           _ptr(steps), threads)
+    if rc != 0:
+        raise RuntimeError(f"orc_raycast_guided_steps failed: {rc}")
+    return steps
 
 
 class Guided:

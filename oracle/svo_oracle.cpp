@@ -730,6 +730,23 @@ int orc_raycast_guided(int depth, const uint32_t* words, size_t n_words, uint32_
     return 0;
 }
 
+// Loop iterations of every guided walk (s0 as orc_raycast_guided; 0 where
+// s0 < 0): the per-lane cost a model of the tracer's warps sums over.
+int orc_raycast_guided_steps(int depth, const uint32_t* words, size_t n_words, uint32_t root, const float* pos4,
+                             const float* m16, int res_x, int res_y, const float* s0, uint32_t* steps, int threads) {
+    if (res_x <= 0 || res_y <= 0 || res_x > 65535 || res_y > 65535 || !s0 || !steps) return -1;
+    Tracer tr{words, n_words, root, depth};
+    View v = make_view(pos4, m16);
+    if (threads > 0) omp_set_num_threads(threads);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int y = 0; y < res_y; ++y)
+        for (int x = 0; x < res_x; ++x) {
+            size_t o = (size_t)y * res_x + x;
+            steps[o] = s0[o] < 0.0f ? 0u : tr.trace(v, x, y, res_x, res_y, 1.0f, 1.0f, s0[o]).steps;
+        }
+    return 0;
+}
+
 // Guided learned frames with every unguided pixel traced: the product's
 // svo_warp_frame_learned on a guided target with a confidence threshold no
 // pixel reaches (the net then decides nothing; the reference has no such
@@ -833,7 +850,8 @@ int orc_guided_frame(void* h, const uint32_t* words, size_t n_words, uint32_t ro
     }
     // start distances: the 3x3 minimum of the reprojected points' camera
     // distances, less 4 cells of the level of detail there; half that minimum
-    // for a pixel with a hole (a pixel of the frame without a point) in its 3x3
+    // for a pixel with at least 3 holes (pixels of the frame without a point)
+    // in its 3x3
     std::vector<float> dist(N);
 #pragma omp parallel for schedule(static)
     for (long t = 0; t < (long)N; ++t) {
@@ -848,14 +866,14 @@ int orc_guided_frame(void* h, const uint32_t* words, size_t n_words, uint32_t ro
     for (long t = 0; t < (long)N; ++t) {
         const int x = (int)(t % res_x), y = (int)(t / res_x);
         float m = INFINITY;
-        bool near_hole = false;
+        int holes = 0;
         for (int j = -1; j <= 1; ++j)
             for (int i = -1; i <= 1; ++i) {
                 const int xi = x + i, yj = y + j;
                 if (xi >= 0 && xi < res_x && yj >= 0 && yj < res_y) {
                     const size_t o = (size_t)yj * res_x + xi;
                     m = std::fmin(m, dist[o]);
-                    near_hole |= col[o] == kEmpty;
+                    holes += col[o] == kEmpty ? 1 : 0;
                 }
             }
         float gd = -1.0f;
@@ -867,7 +885,7 @@ int orc_guided_frame(void* h, const uint32_t* words, size_t n_words, uint32_t ro
                 sw *= 2.0f;
                 ++lod;
             }
-            gd = near_hole ? s * 0.5f : std::fmax(s - 4.0f * (float)(1 << lod), 0.0f);
+            gd = holes >= 3 ? s * 0.5f : std::fmax(s - 4.0f * (float)(1 << lod), 0.0f);
         }
         g.guide[t] = gd;
     }

@@ -1283,7 +1283,8 @@ svo_status svo_target_create(svo_context* ctx, int res_x, int res_y, svo_target*
     const size_t net_tiles = (size_t)((res_x + kNetOutW - 1) / kNetOutW) * ((res_y + kNetOutH - 1) / kNetOutH);
     A((void**)&t->d_guide, N * 4);
     // walk packets of any shape pw x (32/pw), pw in 4..32: at most N/32 + res_x/4 + res_y + 1
-    A((void**)&t->B.walk_long, N / 32 + res_x / 4 + res_y + 64);
+    t->B.walk_cap = (uint32_t)(N / 32 + res_x / 4 + res_y + 64);
+    A((void**)&t->B.walk_list, (size_t)t->B.walk_cap * 4);
     A((void**)&t->B.net_flags, net_tiles * 4);
     A((void**)&t->B.net_list, net_tiles * 4);
     A((void**)&t->B.counters, 64);
@@ -1325,7 +1326,7 @@ svo_status svo_target_destroy(svo_target* t) {
     for (auto& g : t->graphs) g.reset();
     void* ptrs[] = {t->B.col[0], t->B.col[1], t->B.col[2], t->B.xyz[0], t->B.xyz[1], t->B.xyz[2], t->B.disp, t->B.bgrx, t->B.keys, t->B.ids,
                     t->B.tile_mask, t->B.counters, t->d_params, t->full_col, t->full_xyzw, t->full_vox,
-                    t->B.req_mask, t->req_offs, t->d_guide, t->B.net_flags, t->B.net_list, t->B.walk_long};
+                    t->B.req_mask, t->req_offs, t->d_guide, t->B.net_flags, t->B.net_list, t->B.walk_list};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (auto& e : t->ev)

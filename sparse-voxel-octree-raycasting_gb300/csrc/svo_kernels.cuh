@@ -69,11 +69,15 @@ struct TargetBuffers {
     // tile, the serial of the last frame that needed the net there, and the
     // list of those tiles (count in counters[3]). guide == nullptr: no walks.
     float* guide;
-    uint8_t* walk_long;  // per walk packet (pw x ph): 1 = expected to be long (traced first)
+    // The walk packets (pw x ph) holding at least one walk, listed by k_guide:
+    // those expected to hold a long walk from the front (counters[4] of them),
+    // the others from the back (counters[5]); walk_cap entries.
+    uint32_t* walk_list;
+    uint32_t walk_cap;
     uint32_t* net_flags;
     uint32_t* net_list;
     uint32_t* counters;   // [0] trace work counter, [1] hole entries, [2] coarse-pass work counter,
-                          // [3] net tiles listed
+                          // [3] net tiles listed, [4] long walk packets listed, [5] other walk packets listed
     int res_x, res_y;
     int tiles_x, tiles_y;  // whole 16x16 tiles (res/16)
 };
@@ -108,10 +112,8 @@ __device__ __forceinline__ float4* plane_xyz(const TargetBuffers& B, int i) {
 
 __global__ void k_set_params(FrameParams p, FrameParams* dst, uint32_t* counters) {
     *dst = p;
-    counters[0] = 0;
-    counters[1] = 0;
-    counters[2] = 0;
-    counters[3] = 0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i) counters[i] = 0;
 }
 
 __global__ void k_reset_counter(uint32_t* counter) { *counter = 0; }
@@ -420,13 +422,13 @@ __global__ void __launch_bounds__(BLOCK) k_trace_full(Octree o_in, const FullBat
 
 // kBgrx (learned frames): also writes the traced pixels' colourised output,
 // and with a guide buffer walks every guided pixel after the requested rays
-// and the refresh tile: dense packets over the frame, each guided pixel's
-// ray starting at its guide distance (pixels of the refresh tile and
-// unguided pixels are skipped). Requested pixels are unguided, so every pixel
-// is written at most once and the walks read nothing the launch writes. The
-// walk packets are swept twice: first those k_guide expects to be long (a
-// depth edge inside: some pixel walks from the near side), then the rest, so
-// the launch does not end on a long packet.
+// and the refresh tile: the walk packets k_guide listed (those holding a
+// walk), each guided pixel's ray starting at its guide distance (pixels of
+// the refresh tile and unguided pixels are skipped). Requested pixels are
+// unguided, so every pixel is written at most once and the walks read
+// nothing the launch writes. The packets k_guide expects to be long (a depth
+// edge inside: some pixel walks from the near side) come first in the list,
+// so the launch does not end on a long packet.
 template <int DEPTH, int BLOCK, bool kBgrx>
 __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FrameParams* __restrict__ P,
                                                     TargetBuffers B, uint32_t* fault_out) {
@@ -446,8 +448,9 @@ __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FramePa
     const uint32_t fixed = hole_packets + rpx * rpy;
     const float* __restrict__ guide = kBgrx ? B.guide : nullptr;
     const uint32_t wpx = (uint32_t)((res_x + pw - 1) / pw);
-    const uint32_t nwalk = guide ? wpx * (uint32_t)((res_y + ph - 1) / ph) : 0u;
-    const uint32_t total = fixed + 2u * nwalk;
+    const uint32_t n_long = guide ? min(B.counters[4], B.walk_cap) : 0u;
+    const uint32_t n_walk = guide ? min(n_long + B.counters[5], B.walk_cap) : 0u;
+    const uint32_t total = fixed + n_walk;
     const RayCam cam = P->ray;
     float4* __restrict__ xyz = plane_xyz(B, P->cur);
     uint32_t* __restrict__ col = plane_col(B, P->cur);
@@ -460,10 +463,8 @@ __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FramePa
         bool valid;
         float s0 = 0.0f;
         if (kBgrx && p >= fixed) {
-            uint32_t q = p - fixed;
-            const bool first_sweep = q < nwalk;
-            if (!first_sweep) q -= nwalk;
-            if ((B.walk_long[q] != 0) != first_sweep) continue;  // packet belongs to the other sweep
+            const uint32_t k = p - fixed;
+            const uint32_t q = __ldg(B.walk_list + (k < n_long ? k : B.walk_cap - 1u - (k - n_long)));
             x = (int)(q % wpx) * pw + (lane & (pw - 1));
             y = (int)(q / wpx) * ph + (lane >> ps);
             valid = x < res_x && y < res_y && !(x >= ax && x < xe && y >= ay && y < ye);

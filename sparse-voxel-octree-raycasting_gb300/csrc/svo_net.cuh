@@ -399,7 +399,7 @@ static_assert(kNetPer == kNetLayers, "one slice of the next tile's input per lay
 // nearest cached surface around it instead of from the camera: the start
 // distance is the smallest camera distance of the reprojected points in the
 // pixel's 3x3 neighbourhood, less kGuideMargin cells of the level of detail
-// at that distance (half that smallest distance next to a hole). A cached point that is a ray end rather than a hit (the
+// at that distance (half that smallest distance at the edge of a hole region). A cached point that is a ray end rather than a hit (the
 // ray left the volume through its top or bottom, or reached the view
 // distance limit) bounds its neighbours the same way: their rays are walked
 // from just in front of where it ended. A pixel with no cached point around
@@ -407,30 +407,38 @@ static_assert(kNetPer == kNetLayers, "one slice of the next tile's input per lay
 // ray. The walk is exact unless a surface the cache has not seen lies in
 // front of the start; the refresh tile and the requested rays keep tracing
 // from the camera.
-// A pixel next to a hole (a pixel of the frame that reprojection left
-// without a point) is where a surface the cache never saw -- newly uncovered
-// by the camera's motion -- most often lies in front of the cached points:
-// its walk starts at half the 3x3 minimum distance instead. (On the
-// fast-motion camera path at 1920x1024 this took whole guided frames from
-// 35.5 to 39.2 dB against the full raycast, with every unguided pixel traced,
-// for 3% more node fetches than starting there at the usual margin.)
+// A pixel at the edge of a hole region -- at least kGuideHoleCount of its
+// 3x3 neighbourhood are pixels of the frame that reprojection left without a
+// point -- is where a surface the cache never saw, newly uncovered by the
+// camera's motion, most often lies in front of the cached points, and often
+// far in front: its walk starts at half the 3x3 minimum distance instead.
+// (Oracle experiment on the fast-motion camera path, 1920x1024, frames 2-21,
+// every unguided pixel traced: 35.5 dB against the full raycast without the
+// rule, 38.5 dB with it, 39.2 dB when any single hole counts; a wider margin
+// of 16 or 32 cells gains nothing. On the orbit the rule costs 4% more node
+// fetches, 12% when any single hole -- a splat crack -- counts.)
 constexpr float kGuideMargin = 4.0f;        // cells of the start distance's level of detail
-constexpr float kGuideNearHole = 0.5f;      // start distance factor of a pixel next to a hole
+constexpr float kGuideNearHole = 0.5f;      // start distance factor at the edge of a hole region
+constexpr int kGuideHoleCount = 3;          // holes in the 3x3 that make a hole region
 constexpr float kGuideLong = 64.0f;         // cells between the start and the pixel's own point: a long walk
 constexpr int kGuideBW = 32, kGuideBH = 8;  // pixels per block (whole ray packets of every packet shape)
 
 // Also lists the net tiles (kNetOutW x kNetOutH) holding an unguided pixel:
 // the first block to find one in a tile stamps the tile with this frame's
 // serial and appends it (a block of 32 x 8 pixels touches at most 2 x 2
-// tiles). And it flags the walk packets (pw x ph, eight per block) that hold
-// a long walk: a pixel whose own reprojected point (else the farthest around
-// it) lies more than kGuideLong cells beyond its start -- a depth edge, where
-// the start comes from the near side. The tracer walks those packets first.
+// tiles). And it lists the walk packets (pw x ph, eight per block) that hold
+// a walk -- a guided pixel outside the refresh tile -- for the tracer: from
+// the front those holding a long walk (a pixel whose own reprojected point,
+// else the farthest around it, lies more than kGuideLong cells beyond its
+// start: a depth edge, where the start comes from the near side), which the
+// tracer walks first, from the back the others. Packets without a walk are
+// not listed, so the tracer never pulls them.
 __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams* __restrict__ P, TargetBuffers B) {
     __shared__ float dist[kGuideBH + 2][kGuideBW + 2];
     __shared__ uint8_t hole[kGuideBH + 2][kGuideBW + 2];  // a pixel of the frame without a point
     __shared__ uint32_t touched;
     __shared__ uint32_t long_packets;  // bit k: packet k of this block holds a long walk
+    __shared__ uint32_t walk_packets;  // bit k: packet k of this block holds a walk
     const int res_x = B.res_x, res_y = B.res_y;
     const int x0 = blockIdx.x * kGuideBW, y0 = blockIdx.y * kGuideBH;
     const float cx = P->ray.px, cy = P->ray.py, cz = P->ray.pz;
@@ -439,6 +447,7 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
     if (threadIdx.x == 0) {
         touched = 0;
         long_packets = 0;
+        walk_packets = 0;
     }
     for (int i = threadIdx.x; i < (kGuideBW + 2) * (kGuideBH + 2); i += kGuideBW * kGuideBH) {
         const int wx = i % (kGuideBW + 2), wy = i / (kGuideBW + 2);
@@ -464,7 +473,7 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
     const int x = x0 + tx, y = y0 + ty;
     if (x < res_x && y < res_y) {
         float m = INFINITY, far = 0.0f;
-        bool near_hole = false;
+        int holes = 0;
 #pragma unroll
         for (int j = 0; j < 3; ++j)
 #pragma unroll
@@ -472,7 +481,7 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
                 const float d = dist[ty + j][tx + i];
                 m = fminf(m, d);
                 if (d < INFINITY) far = fmaxf(far, d);
-                near_hole |= hole[ty + j][tx + i] != 0;
+                holes += hole[ty + j][tx + i];
             }
         const float own = dist[ty + 1][tx + 1];
         float g = -1.0f;
@@ -485,11 +494,15 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
                 ++lod;
             }
             const float cell = (float)(1 << lod);
-            g = near_hole ? __fmul_rn(s, kGuideNearHole) : fmaxf(__fsub_rn(s, __fmul_rn(kGuideMargin, cell)), 0.0f);
+            g = holes >= kGuideHoleCount ? __fmul_rn(s, kGuideNearHole)
+                                         : fmaxf(__fsub_rn(s, __fmul_rn(kGuideMargin, cell)), 0.0f);
             const float ahead = (own < INFINITY ? own : far) * 16.0f - g;
-            if (ahead > kGuideLong * cell) {
-                const int ps = P->pw_shift, pw = 1 << ps, ph = 32 >> ps;
-                atomicOr(&long_packets, 1u << ((tx >> ps) + (ty / ph) * (kGuideBW / pw)));
+            const int ps = P->pw_shift, pw = 1 << ps, ph = 32 >> ps;
+            const uint32_t bit = 1u << ((tx >> ps) + (ty / ph) * (kGuideBW / pw));
+            const bool in_tile = x >= P->add_x && x < P->x_end && y >= P->add_y && y < P->y_end;
+            if (!in_tile) {  // the refresh tile traces its pixels from the camera
+                atomicOr(&walk_packets, bit);
+                if (ahead > kGuideLong * cell) atomicOr(&long_packets, bit);
             }
         } else {
             const int ntx = x / kNetOutW - x0 / kNetOutW, nty = y / kNetOutH - y0 / kNetOutH;
@@ -498,12 +511,31 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
         B.guide[(size_t)y * res_x + x] = g;
     }
     __syncthreads();
-    if (threadIdx.x < 8) {  // the block's eight walk packets
+    if (threadIdx.x < 32) {  // the block's eight walk packets, appended by lanes 0-7 of warp 0
+        const int k = (int)threadIdx.x;
         const int ps = P->pw_shift, pw = 1 << ps, ph = 32 >> ps;
         const int per_row = kGuideBW / pw;
-        const int px = x0 / pw + (int)threadIdx.x % per_row, py = y0 / ph + (int)threadIdx.x / per_row;
+        const int px = x0 / pw + k % per_row, py = y0 / ph + k / per_row;
         const int wpx = (res_x + pw - 1) / pw, wpy = (res_y + ph - 1) / ph;
-        if (px < wpx && py < wpy) B.walk_long[(size_t)py * wpx + px] = (uint8_t)((long_packets >> threadIdx.x) & 1u);
+        const bool walk = k < 8 && px < wpx && py < wpy && ((walk_packets >> k) & 1u);
+        const bool lng = walk && ((long_packets >> k) & 1u);
+        const uint32_t bl = __ballot_sync(0xffffffffu, lng), bs = __ballot_sync(0xffffffffu, walk && !lng);
+        uint32_t base_l = 0, base_s = 0;
+        if (k == 0) {
+            if (bl) base_l = atomicAdd(B.counters + 4, (uint32_t)__popc(bl));
+            if (bs) base_s = atomicAdd(B.counters + 5, (uint32_t)__popc(bs));
+        }
+        base_l = __shfl_sync(0xffffffffu, base_l, 0);
+        base_s = __shfl_sync(0xffffffffu, base_s, 0);
+        const uint32_t below = (1u << k) - 1u;
+        const uint32_t id = (uint32_t)py * (uint32_t)wpx + (uint32_t)px;
+        if (lng) {
+            const uint32_t at = base_l + (uint32_t)__popc(bl & below);
+            if (at < B.walk_cap) B.walk_list[at] = id;
+        } else if (walk) {
+            const uint32_t at = base_s + (uint32_t)__popc(bs & below);
+            if (at < B.walk_cap) B.walk_list[B.walk_cap - 1u - at] = id;
+        }
     }
     if (threadIdx.x < 4 && ((touched >> threadIdx.x) & 1u)) {
         const int tiles_x = (res_x + kNetOutW - 1) / kNetOutW;
