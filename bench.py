@@ -458,6 +458,39 @@ def measure_large(svo, torch, args, device, frames=16, views=8):
     return out
 
 
+def measure_training(svo, torch, args, device, W=1920, H=1024, steps=6):
+    """One training step of the net at the benchmark's frame size: the
+    tensor-core forward keeping its activations, the loss, the tensor-core
+    backward convolutions (data and weight gradients) and Adam, on seeded
+    features and targets already on the device; device events per step."""
+    ctx = svo.Context(device.index)
+    net = svo.Net(ctx)
+    net.load_file(args.weights)
+    g = torch.Generator(device=device).manual_seed(7)
+    feat = torch.rand((8, H, W), generator=g, device=device)
+    tgt = torch.randint(0, 1 << 24, (H * W,), generator=g, device=device, dtype=torch.int32)
+    torch.cuda.synchronize(device)
+    ext = torch.cuda.ExternalStream(ctx.stream, device=device)
+    ms = []
+    for i in range(steps + 2):
+        s_ev, e_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s_ev.record(ext)
+        net.backward(feat.data_ptr(), tgt.data_ptr(), W, H, 0.015, 0.1, read_loss=False)
+        net.adam(1e-5)
+        e_ev.record(ext)
+        e_ev.synchronize()
+        if i >= 2:
+            ms.append(s_ev.elapsed_time(e_ev))
+    net.close()
+    ctx.close()
+    t = float(np.mean(ms))
+    # forward 12,096 + data gradients of layers 3-1 10,368 + weight gradients 12,096 FLOP per pixel
+    flops = 34560.0 * W * H
+    return {"workload": f"net training step {W}x{H} (forward, loss, backward, Adam)", "ms_per_step": t,
+            "tflops_algorithmic": flops / (t * 1e-3) / 1e12,
+            "note": "tensor-core forward and backward convolutions; gradients enter the MMAs as two bf16 parts"}
+
+
 def measure_config1(svo, torch, device, seed, no_cpu: bool, steps: int = 20):
     """The plain full raycast configuration: 512x512, depth-9 (512^3) solid
     terrain (the GPU builder from the seeded voxels), one camera at 1.5x
@@ -928,6 +961,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     extras = {}
     if args.extras and rank == 0:
         extras["config1"] = measure_config1(svo, torch, device, args.seed, args.no_cpu)
+        extras["net_training"] = measure_training(svo, torch, args, device)
         extras["octree_builder"] = measure_builder(svo, torch, octree, depth, args.seed, device)
         extras["batch_64_views"] = measure_batch(svo, torch, ctx, depth, device)
         extras["large"] = measure_large(svo, torch, args, device)

@@ -329,15 +329,19 @@ svo_status svo_net_get_params(svo_net* net, float* host, size_t n);
 svo_status svo_net_get_grads(svo_net* net, float* host, size_t n);
 /* Forward passes over a planar feature image (device pointers; features
  * [8][h*w], outputs [4][h*w]: R, G, B, confidence logit). svo_net_forward is
- * the FP32 CUDA-core path used in training; svo_net_infer is the tensor-core
- * kernel of learned frames. */
+ * an FP32 CUDA-core reference; svo_net_infer is the tensor-core kernel of
+ * learned frames and of training. */
 svo_status svo_net_forward(svo_net* net, const float* d_features, int w, int h, float* d_out);
 svo_status svo_net_infer(svo_net* net, const float* d_features, int w, int h, float* d_out);
 /* Forward + loss + backward over one frame: the target is a BGRX8 image
  * (device pointer, e.g. the full raycast of the same view). Loss per pixel:
  * mean squared colour error over R, G, B plus lambda * binary cross-entropy
  * of the confidence against "every colour channel within tau". loss (host,
- * may be NULL) receives the two mean terms. Synchronises when loss != NULL. */
+ * may be NULL) receives the two mean terms. Synchronises when loss != NULL.
+ * All convolutions run on the tensor cores: the forward pass as in
+ * svo_net_infer (keeping the hidden activations), the data and weight
+ * gradients as implicit GEMMs with each FP32 gradient split into two bf16
+ * parts; FP32 sums. */
 svo_status svo_net_backward(svo_net* net, const float* d_features, const uint32_t* d_target_bgrx, int w, int h,
                             float tau, float lambda, float* loss);
 /* One Adam step with the last gradient (asynchronous). */

@@ -31,7 +31,7 @@ CXX_FLAGS = ["-std=c++17", "-O3", "-ffp-contract=off", "-fno-fast-math", "-fPIC"
 
 SOURCES_CU = ["svo_device.cu"]
 SOURCES_CPP = ["svo_host.cpp"]
-HEADERS = ["svo_trace.cuh", "svo_kernels.cuh", "svo_net.cuh"]
+HEADERS = ["svo_trace.cuh", "svo_kernels.cuh", "svo_net.cuh", "svo_net_train.cuh"]
 
 
 def _nvcc() -> str:

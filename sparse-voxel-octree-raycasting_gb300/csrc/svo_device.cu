@@ -20,6 +20,7 @@
 #include "../../include/svo_gb300.h"
 #include "svo_kernels.cuh"
 #include "svo_net.cuh"
+#include "svo_net_train.cuh"
 #include "svo_build.cuh"
 
 using namespace svo;
@@ -129,6 +130,7 @@ struct svo_net {
     float* grads = nullptr;
     float* wr = nullptr;         // bf16-rounded weights, FP32 (CUDA-core path)
     uint16_t* packed = nullptr;  // tensor-core operand image
+    uint16_t* packed_bwd = nullptr;  // backward-data operand image (layers 1-3)
     float* bias = nullptr;       // 52 biases
     int step = 0;
     size_t cap = 0;           // pixels the training buffers hold
@@ -686,8 +688,8 @@ svo_status net_reserve(svo_net* net, size_t n) {
         SVO_CUDA(ctx, cudaMalloc(&net->g1, 16 * n * 4));
         net->cap = n;
     }
-    const size_t blocks = (n + kNetChunk - 1) / kNetChunk;
-    const size_t need = blocks * (9 * 16 * 16 + 16);
+    // weight-gradient partial sums: one row per CTA of the backward kernels
+    const size_t need = (size_t)std::max(ctx->sm_count, 1) * (9 * 16 * 16 + 16);
     if (need > net->partial_cap) {
         cudaFree(net->partial);
         net->partial = nullptr;
@@ -709,6 +711,8 @@ svo_status net_reserve(svo_net* net, size_t n) {
 svo_status net_prepare(svo_net* net) {
     k_net_prepare<<<(kNetMmaTotal * 256 + 255) / 256, 256, 0, net->ctx->stream>>>(net->params, net->wr, net->packed,
                                                                                    net->bias);
+    SVO_LAUNCHED(net->ctx);
+    k_net_prepare_bwd<<<(kNetBwdBlocks * 256 + 255) / 256, 256, 0, net->ctx->stream>>>(net->params, net->packed_bwd);
     SVO_LAUNCHED(net->ctx);
     return SVO_OK;
 }
@@ -737,17 +741,38 @@ svo_status net_forward_fp32(svo_net* net, const float* feat, int W, int H, float
     return SVO_OK;
 }
 
-template <int CIN, int COUT, bool kFirst>
-svo_status net_weight_grad(svo_net* net, const float* a, const float* g, int W, int H, int layer) {
+// Tensor-core backward of one layer (svo_net_train.cuh), over 62x30-position
+// tiles, one CTA per SM: the weight and bias gradient (per-CTA partial sums,
+// then reduced in CTA order) and, for layers above the first, the gradient
+// of the layer below's pre-activation (the ReLU mask of `a` applied).
+template <int CIN, int KIN, bool kFirst>
+svo_status net_backward_layer(svo_net* net, const float* a, const float* g, float* g_in, int W, int H, int layer) {
     svo_context* ctx = net->ctx;
-    const size_t n = (size_t)W * H;
-    const int blocks = (int)((n + kNetChunk - 1) / kNetChunk);
-    constexpr int vals = 9 * CIN * COUT + COUT;
-    k_net_conv_bwd_weight<CIN, COUT, kFirst><<<blocks, 160, 0, ctx->stream>>>(a, g, net->partial, W, H);
-    SVO_LAUNCHED(ctx);
-    k_net_reduce<<<(vals + 255) / 256, 256, 0, ctx->stream>>>(net->partial, blocks, vals,
-                                                               net->grads + net_w_off(layer));
-    SVO_LAUNCHED(ctx);
+    const int tiles_x = (W + kBwdOutW - 1) / kBwdOutW;
+    const int tiles = tiles_x * ((H + kBwdOutH - 1) / kBwdOutH);
+    const int grid = std::max(1, std::min(tiles, ctx->sm_count));
+    {
+        NetBwdWeightArgs A{a, g, net->partial, W, H, tiles_x, tiles, ctx->d_fault};
+        const void* fn = (const void*)k_net_bwd_weight_tc<CIN, KIN, kFirst>;
+        constexpr int smem = BwdWeightLayout<CIN>::kSmem;
+        SVO_CUDA(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        void* args[] = {&A};
+        SVO_CUDA(ctx, cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kBwdThreads), args, smem, ctx->stream));
+        ++ctx->launches;
+        constexpr int vals = 9 * CIN * KIN + KIN;
+        k_net_reduce<<<(vals + 255) / 256, 256, 0, ctx->stream>>>(net->partial, grid, vals,
+                                                                   net->grads + net_w_off(layer));
+        SVO_LAUNCHED(ctx);
+    }
+    if (g_in) {
+        NetBwdDataArgs D{g, net->packed_bwd + (size_t)(layer - 1) * 9 * 256, a, g_in, W, H, tiles_x, tiles,
+                         ctx->d_fault};
+        const void* fn = (const void*)k_net_bwd_data_tc<KIN>;
+        SVO_CUDA(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kBwdDataSmem));
+        void* args[] = {&D};
+        SVO_CUDA(ctx, cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kBwdThreads), args, kBwdDataSmem, ctx->stream));
+        ++ctx->launches;
+    }
     return SVO_OK;
 }
 
@@ -1673,6 +1698,7 @@ svo_status svo_net_create(svo_context* ctx, svo_net** out) {
     A((void**)&net->grads, kNetParams * 4);
     A((void**)&net->wr, kNetParams * 4);
     A((void**)&net->packed, kNetMmaTotal * 512);
+    A((void**)&net->packed_bwd, kNetBwdBlocks * 512);
     A((void**)&net->bias, 64 * 4);
     if (st != SVO_OK) {
         svo_net_destroy(net);
@@ -1687,7 +1713,7 @@ svo_status svo_net_destroy(svo_net* net) {
     if (!net) return SVO_OK;
     cudaSetDevice(net->ctx->device);
     cudaStreamSynchronize(net->ctx->stream);
-    void* ptrs[] = {net->params, net->m, net->v, net->grads, net->wr, net->packed, net->bias, net->act,
+    void* ptrs[] = {net->params, net->m, net->v, net->grads, net->wr, net->packed, net->packed_bwd, net->bias, net->act,
                     net->out, net->dout, net->g0, net->g1, net->partial, net->loss_partial};
     for (void* q : ptrs)
         if (q) cudaFree(q);
@@ -1784,39 +1810,27 @@ svo_status svo_net_backward(svo_net* net, const float* d_features, const uint32_
     const size_t n = (size_t)w * h;
     svo_status st = net_reserve(net, n);
     if (st != SVO_OK) return st;
-    st = net_forward_fp32(net, d_features, w, h, net->out);
-    if (st != SVO_OK) return st;
+    {  // the forward pass on the tensor cores, keeping the hidden activations
+        NetInferArgs A{};
+        A.feat = d_features;
+        A.out = net->out;
+        A.act = net->act;
+        A.w = w;
+        A.h = h;
+        st = launch_net_infer(ctx, net, false, A);
+        if (st != SVO_OK) return st;
+    }
     const int lb = (int)((n + 255) / 256);
     k_net_loss<<<lb, 256, 0, s>>>(net->out, d_target_bgrx, net->dout, net->loss_partial, (int)n, tau, lambda);
     SVO_LAUNCHED(ctx);
     float* a0 = net->act;
     float* a1 = net->act + 16 * n;
     float* a2 = net->act + 32 * n;
-    const dim3 grid((w + 31) / 32, (h + 7) / 8);
-    const int rg = std::min<size_t>((16 * n + 255) / 256, (size_t)ctx->sm_count * 16);
-    // layer 3
-    st = net_weight_grad<16, 4, false>(net, a2, net->dout, w, h, 3);
-    if (st != SVO_OK) return st;
-    k_net_conv_bwd_data<16, 4><<<grid, 256, 0, s>>>(net->dout, net->wr + net_w_off(3), net->g0, w, h);
-    SVO_LAUNCHED(ctx);
-    k_net_relu_grad<<<rg, 256, 0, s>>>(net->g0, a2, 16 * n);
-    SVO_LAUNCHED(ctx);
-    // layer 2
-    st = net_weight_grad<16, 16, false>(net, a1, net->g0, w, h, 2);
-    if (st != SVO_OK) return st;
-    k_net_conv_bwd_data<16, 16><<<grid, 256, 0, s>>>(net->g0, net->wr + net_w_off(2), net->g1, w, h);
-    SVO_LAUNCHED(ctx);
-    k_net_relu_grad<<<rg, 256, 0, s>>>(net->g1, a1, 16 * n);
-    SVO_LAUNCHED(ctx);
-    // layer 1
-    st = net_weight_grad<16, 16, false>(net, a0, net->g1, w, h, 1);
-    if (st != SVO_OK) return st;
-    k_net_conv_bwd_data<16, 16><<<grid, 256, 0, s>>>(net->g1, net->wr + net_w_off(1), net->g0, w, h);
-    SVO_LAUNCHED(ctx);
-    k_net_relu_grad<<<rg, 256, 0, s>>>(net->g0, a0, 16 * n);
-    SVO_LAUNCHED(ctx);
-    // layer 0
-    st = net_weight_grad<8, 16, true>(net, d_features, net->g0, w, h, 0);
+    // layer 3 (4 outputs) .. layer 0 (the features as input, no data gradient)
+    st = net_backward_layer<16, 4, false>(net, a2, net->dout, net->g0, w, h, 3);
+    if (st == SVO_OK) st = net_backward_layer<16, 16, false>(net, a1, net->g0, net->g1, w, h, 2);
+    if (st == SVO_OK) st = net_backward_layer<16, 16, false>(net, a0, net->g1, net->g0, w, h, 1);
+    if (st == SVO_OK) st = net_backward_layer<8, 16, true>(net, d_features, net->g0, nullptr, w, h, 0);
     if (st != SVO_OK) return st;
     if (loss) {
         std::vector<float> part(2 * (size_t)lb);

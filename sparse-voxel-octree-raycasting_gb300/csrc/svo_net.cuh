@@ -21,8 +21,11 @@
 //                     cores: tcgen05.mma (kind::f16, bf16 x bf16 -> fp32 in
 //                     tensor memory) as an implicit GEMM, activations staged
 //                     in shared memory between layers
-//   k_net_conv_*      FP32 CUDA-core forward / backward of one layer, the
-//                     loss, a deterministic reduction and Adam (training)
+//   k_net_conv_fwd    FP32 CUDA-core forward of one layer (the reference the
+//                     tensor-core forward is checked against)
+//   k_net_loss, k_net_reduce, k_net_adam
+//                     the training loss, a deterministic reduction and Adam;
+//                     the backward convolutions are in svo_net_train.cuh
 #pragma once
 #include <cstdint>
 #include <cstring>
@@ -553,6 +556,7 @@ struct NetInferArgs {
     TargetBuffers B;
     const float* feat;  // [8][h][w] when not from planes
     float* out;         // [4][h][w] when not from planes
+    float* act;         // training: [3][16][h][w] hidden activations (bf16 values), or null
     int w, h;
     int tiles_x, tiles;
     float logit_threshold;  // pipeline: traced when logit < threshold
@@ -749,6 +753,20 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_infer(NetInferArgs A) {
                         make_uint4(h[0], h[1], h[2], h[3]);
                     *reinterpret_cast<uint4*>(smem + out_off + kNetPlaneBytes + (kNetGuard + p) * 16) =
                         make_uint4(h[4], h[5], h[6], h[7]);
+                    if (!kPipeline && A.act) {
+                        // training: the tile's own positions keep this layer's activations
+                        // (the bf16 values the next layer reads) for the backward pass
+                        const int col = p & (kNetTW - 1), row = p >> 6;
+                        if (inside && col >= 4 && col < 4 + kNetOutW && row >= 4 && row < 4 + kNetOutH) {
+                            const size_t n = (size_t)W * H;
+                            float* dst = A.act + (size_t)l * 16 * n + (size_t)gy * W + gx;
+#pragma unroll
+                            for (int c = 0; c < 8; ++c) {
+                                dst[(2 * c) * n] = __uint_as_float(h[c] << 16);
+                                dst[(2 * c + 1) * n] = __uint_as_float(h[c] & 0xFFFF0000u);
+                            }
+                        }
+                    }
                 }
             } else {
                 for (int j = warp >> 2; j < nb; j += kNetWarps / 4) {
@@ -893,7 +911,7 @@ __global__ void __launch_bounds__(kReqBlock) k_request_write(TargetBuffers B, co
     }
 }
 
-// ----------------------------------------------- FP32 training path --
+// ------------------------------------------------ FP32 reference path --
 // One layer forward: one thread per pixel, weights (already bf16-rounded) in
 // shared memory. kFirst rounds the input features to bf16 on load; hidden
 // layers store bf16(ReLU(.)); the last layer stores FP32 plus the residual
@@ -977,87 +995,6 @@ __global__ void __launch_bounds__(256) k_net_loss(const float* __restrict__ out,
         }
         partial[2 * blockIdx.x] = a;
         partial[2 * blockIdx.x + 1] = c;
-    }
-}
-
-// g <- g * (a > 0): the gradient w.r.t. a hidden layer's pre-activation.
-__global__ void k_net_relu_grad(float* __restrict__ g, const float* __restrict__ a, size_t n) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-        if (!(a[i] > 0.0f)) g[i] = 0.0f;
-}
-
-// Gradient w.r.t. a layer's input: g_in[ci][q] = sum_t sum_co
-// W[t][ci][co] * g[co][q - off_t] (zero outside the frame).
-template <int CIN, int COUT>
-__global__ void __launch_bounds__(256) k_net_conv_bwd_data(const float* __restrict__ g, const float* __restrict__ wr,
-                                                           float* __restrict__ g_in, int W, int H) {
-    __shared__ float ws[9 * CIN * COUT];
-    for (int i = threadIdx.x; i < 9 * CIN * COUT; i += blockDim.x) ws[i] = wr[i];
-    __syncthreads();
-    const int x = blockIdx.x * 32 + (threadIdx.x & 31), y = blockIdx.y * 8 + (threadIdx.x >> 5);
-    if (x >= W || y >= H) return;
-    const size_t n = (size_t)W * H;
-    float acc[CIN];
-#pragma unroll
-    for (int c = 0; c < CIN; ++c) acc[c] = 0.0f;
-    for (int t = 0; t < 9; ++t) {
-        const int sx = x - (t % 3 - 1), sy = y - (t / 3 - 1);
-        if (sx < 0 || sx >= W || sy < 0 || sy >= H) continue;
-        const size_t o = (size_t)sy * W + sx;
-        for (int co = 0; co < COUT; ++co) {
-            const float gv = __ldg(g + co * n + o);
-#pragma unroll
-            for (int ci = 0; ci < CIN; ++ci) acc[ci] = __fmaf_rn(ws[(t * CIN + ci) * COUT + co], gv, acc[ci]);
-        }
-    }
-    const size_t o = (size_t)y * W + x;
-#pragma unroll
-    for (int ci = 0; ci < CIN; ++ci) g_in[ci * n + o] = acc[ci];
-}
-
-// Weight and bias gradient partial sums over a chunk of kNetChunk pixels per
-// block: thread (t, ci) accumulates COUT sums a[ci][p + off_t] * g[co][p];
-// threads past 9*CIN sum g for the biases. Partials [block][9*CIN*COUT + COUT].
-constexpr int kNetChunk = 512;
-
-template <int CIN, int COUT, bool kFirst>
-__global__ void __launch_bounds__(160) k_net_conv_bwd_weight(const float* __restrict__ a, const float* __restrict__ g,
-                                                             float* __restrict__ partial, int W, int H) {
-    __shared__ float gs[COUT][kNetChunk];
-    const size_t n = (size_t)W * H;
-    const size_t p0 = (size_t)blockIdx.x * kNetChunk;
-    for (int i = threadIdx.x; i < COUT * kNetChunk; i += blockDim.x) {
-        const int co = i / kNetChunk, k = i % kNetChunk;
-        gs[co][k] = p0 + k < n ? g[co * n + p0 + k] : 0.0f;
-    }
-    __syncthreads();
-    constexpr int kVals = 9 * CIN * COUT + COUT;
-    float* dst = partial + (size_t)blockIdx.x * kVals;
-    const int j = threadIdx.x;
-    if (j < 9 * CIN) {
-        const int t = j / CIN, ci = j % CIN;
-        const int dx = t % 3 - 1, dy = t / 3 - 1;
-        float acc[COUT];
-#pragma unroll
-        for (int c = 0; c < COUT; ++c) acc[c] = 0.0f;
-        for (int k = 0; k < kNetChunk; ++k) {
-            const size_t p = p0 + k;
-            if (p >= n) break;
-            const int x = (int)(p % (size_t)W), y = (int)(p / (size_t)W);
-            const int sx = x + dx, sy = y + dy;
-            if (sx < 0 || sx >= W || sy < 0 || sy >= H) continue;
-            float av = __ldg(a + ci * n + (size_t)sy * W + sx);
-            if (kFirst) av = bf16_round(av);
-#pragma unroll
-            for (int c = 0; c < COUT; ++c) acc[c] = __fmaf_rn(av, gs[c][k], acc[c]);
-        }
-#pragma unroll
-        for (int c = 0; c < COUT; ++c) dst[(t * CIN + ci) * COUT + c] = acc[c];
-    } else if (j < 9 * CIN + COUT) {
-        const int co = j - 9 * CIN;
-        float s = 0.0f;
-        for (int k = 0; k < kNetChunk; ++k) s += gs[co][k];
-        dst[9 * CIN * COUT + co] = s;
     }
 }
 

@@ -1,0 +1,388 @@
+// svo_net_train.cuh -- the reconstruction net's backward pass on the tensor
+// cores (training; no reference counterpart).
+//
+// The forward pass of a training step is k_net_infer (tcgen05, bf16 x bf16 ->
+// fp32) writing its hidden activations out; the two kernels here do the
+// backward convolutions as implicit GEMMs on the same operand layouts (the
+// no-swizzle K-major canonical layout k_net_probe checks):
+//
+//   k_net_bwd_data_tc    dL/dinput of a layer, times the ReLU mask of the
+//                        layer below: D[position, ci] = sum over taps t and
+//                        output channels co of g[co][position - off_t] *
+//                        W[t][ci][co] -- the gradient planes read through the
+//                        same shifted-descriptor trick as the forward pass
+//   k_net_bwd_weight_tc  dL/dW[t][ci][co] = sum over positions p of
+//                        a[ci][p + off_t] * g[co][p]: a GEMM whose K dimension
+//                        is the positions; the rows (t, ci) are gathered per
+//                        64-position chunk into shared memory (im2col), the
+//                        chunks double-buffered against the MMAs
+//
+// The gradients are FP32. A bf16 operand keeps 8 bits, too few for them, so
+// every gradient enters the MMAs as two bf16 parts, g = hi + lo (hi the
+// nearest bf16, lo the nearest bf16 of the rest): two MMAs per product, about
+// 16 significant bits. The activations are bf16 values already (the forward
+// pass rounds them, the features included), so they enter exactly. Sums are
+// FP32 in tensor memory. Every mbarrier wait is bounded (a fault flag, then
+// the CTA leaves); tensor memory is always released.
+#pragma once
+#include <cstdint>
+
+#include "svo_net.cuh"
+
+namespace svo {
+
+constexpr int kBwdOutW = kNetTW - 2, kBwdOutH = kNetTH - 2;  // 62 x 30 positions per tile (halo 1)
+constexpr int kBwdThreads = 512;
+constexpr int kBwdBlocks = 15;  // 128-position blocks of window rows 1..30
+
+// Packed backward-data weights of layers 1-3, one 512-byte block per tap in
+// the layout of k_net_prepare's blocks with the roles of the channels
+// swapped: B[n = ci][k = co] = W[t][ci][co] (co past the layer's outputs: 0).
+constexpr int kNetBwdBlocks = 27;
+
+__global__ void k_net_prepare_bwd(const float* __restrict__ params, uint16_t* __restrict__ packed) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kNetBwdBlocks * 256) return;
+    const int blk = i >> 8, e = i & 255;
+    const int l = 1 + blk / 9, t = blk % 9;
+    const int ng = e >> 7, kc = (e >> 6) & 1, r = (e >> 3) & 7, k = e & 7;
+    const int ci = ng * 8 + r, co = kc * 8 + k;
+    float v = 0.0f;
+    if (co < net_cout(l)) v = params[net_w_off(l) + (t * net_cin(l) + ci) * net_cout(l) + co];
+    packed[i] = (uint16_t)bf16_bits(v);
+}
+
+// hi/lo bf16 parts of an FP32 value.
+__device__ __forceinline__ void split_bf16(float v, uint32_t& hi, uint32_t& lo) {
+    hi = bf16_bits(v);
+    lo = bf16_bits(v - __uint_as_float(hi << 16));
+}
+
+// ------------------------------------------------------ backward data --
+struct NetBwdDataArgs {
+    const float* g;        // [kin][h][w]: gradient w.r.t. the layer's output (pre-activation)
+    const uint16_t* wpk;   // the layer's 9 packed backward-data blocks
+    const float* act;      // [16][h][w]: the layer's input activation (ReLU mask)
+    float* g_in;           // [16][h][w]: gradient w.r.t. the previous layer's pre-activation
+    int w, h, tiles_x, tiles;
+    uint32_t* fault;
+};
+
+// Shared memory: the gradient's hi parts (two planes of 8 channels) and lo
+// parts (two planes), each plane laid out as k_net_infer's activation planes,
+// then the 9 weight blocks.
+constexpr int kBwdDataSmemW = 4 * kNetPlaneBytes;
+constexpr int kBwdDataSmem = kBwdDataSmemW + 9 * 512;
+
+template <int KIN>
+__global__ void __launch_bounds__(kBwdThreads, 1) k_net_bwd_data_tc(NetBwdDataArgs A) {
+    __shared__ uint64_t mbar[kNetIssuers];
+    __shared__ uint32_t tmem_base_s;
+    uint8_t* smem = reinterpret_cast<uint8_t*>(svo_dsmem);
+    const uint32_t sbase = smem_addr(smem);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int W = A.w, H = A.h;
+    const size_t n = (size_t)W * H;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base_s)),
+                     "r"(kNetTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid < kNetIssuers) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[tid])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    {
+        const uint4* src = reinterpret_cast<const uint4*>(A.wpk);
+        uint4* dst = reinterpret_cast<uint4*>(smem + kBwdDataSmemW);
+        for (int i = tid; i < 9 * 32; i += kBwdThreads) dst[i] = src[i];
+        uint4* z = reinterpret_cast<uint4*>(smem);
+        for (int i = tid; i < kBwdDataSmemW / 16; i += kBwdThreads) z[i] = make_uint4(0, 0, 0, 0);
+    }
+    __syncthreads();
+    const uint32_t tmem = tmem_base_s;
+    const uint32_t bar = smem_addr(&mbar[warp >> 2]);
+    uint32_t phase = 0, fault = 0;
+
+    for (int item = blockIdx.x; item < A.tiles; item += gridDim.x) {
+        const int ox = (item % A.tiles_x) * kBwdOutW, oy = (item / A.tiles_x) * kBwdOutH;
+        const int wx = ox - 1, wy = oy - 1;  // image position of window position 0
+        // stage the gradient window as hi and lo bf16 planes
+        for (int k = 0; k < kNetPos / kBwdThreads; ++k) {
+            const int p = tid + k * kBwdThreads;
+            const int gx = wx + (p & (kNetTW - 1)), gy = wy + (p >> 6);
+            const bool inside = gx >= 0 && gx < W && gy >= 0 && gy < H;
+            uint32_t hi[16], lo[16];
+#pragma unroll
+            for (int c = 0; c < 16; ++c) {
+                const float v = (inside && c < KIN) ? __ldg(A.g + c * n + (size_t)gy * W + gx) : 0.0f;
+                split_bf16(v, hi[c], lo[c]);
+            }
+#pragma unroll
+            for (int h2 = 0; h2 < 2; ++h2) {
+                const int c0 = 8 * h2;
+                *reinterpret_cast<uint4*>(smem + h2 * kNetPlaneBytes + (kNetGuard + p) * 16) =
+                    make_uint4(hi[c0] | hi[c0 + 1] << 16, hi[c0 + 2] | hi[c0 + 3] << 16, hi[c0 + 4] | hi[c0 + 5] << 16,
+                               hi[c0 + 6] | hi[c0 + 7] << 16);
+                *reinterpret_cast<uint4*>(smem + (2 + h2) * kNetPlaneBytes + (kNetGuard + p) * 16) =
+                    make_uint4(lo[c0] | lo[c0 + 1] << 16, lo[c0 + 2] | lo[c0 + 3] << 16, lo[c0 + 4] | lo[c0 + 5] << 16,
+                               lo[c0 + 6] | lo[c0 + 7] << 16);
+            }
+        }
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (lane == 0 && warp < kNetIssuers) {
+            // blocks j = warp (mod 4): 9 taps x (hi, lo), output rows 1..30
+            for (int j = warp; j < kBwdBlocks; j += kNetIssuers) {
+#pragma unroll
+                for (int t = 0; t < 9; ++t) {
+                    const int off = (t / 3 - 1) * kNetTW + (t % 3 - 1);  // position offset of tap t
+                    const uint32_t pos = (uint32_t)(kNetGuard + kNetTW + 128 * j - off);
+                    const uint64_t bd = tc_desc(sbase + kBwdDataSmemW + (uint32_t)t * 512u, 128u, 256u);
+                    tc_mma(tmem + 16u * j, tc_desc(sbase + pos * 16u, kNetPlaneBytes, 128u), bd, t > 0 ? 1u : 0u);
+                    tc_mma(tmem + 16u * j, tc_desc(sbase + 2u * kNetPlaneBytes + pos * 16u, kNetPlaneBytes, 128u), bd,
+                           1u);
+                }
+            }
+            tc_commit(smem_addr(&mbar[warp]));
+        }
+        const bool ready = mbar_wait_phase(bar, phase);
+        phase ^= 1u;
+        tc_fence_after();
+        if (ready) {
+            const int g = warp & 3;
+            for (int j = warp >> 2; j < kBwdBlocks; j += kNetWarps / 4) {
+                float v[16];
+                tc_ld16(tmem + ((uint32_t)(32 * g) << 16) + 16u * j, v);
+                const int p = kNetTW + 128 * j + 32 * g + lane;
+                const int col = p & (kNetTW - 1);
+                const int gx = wx + col, gy = wy + (p >> 6);
+                if (col >= 1 && col <= kBwdOutW && gx < W && gy < H) {
+                    const size_t o = (size_t)gy * W + gx;
+#pragma unroll
+                    for (int c = 0; c < 16; ++c) A.g_in[c * n + o] = __ldg(A.act + c * n + o) > 0.0f ? v[c] : 0.0f;
+                }
+            }
+        }
+        tc_fence_before();
+        const bool aborted = __syncthreads_or(ready ? 0 : 1) != 0;
+        tc_fence_after();
+        if (aborted) {
+            fault |= kFaultNet;
+            break;
+        }
+    }
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kNetTmemCols) : "memory");
+    }
+    if (fault && tid == 0) atomicOr(A.fault, fault);
+}
+
+// ---------------------------------------------------- backward weights --
+struct NetBwdWeightArgs {
+    const float* a;    // [cin][h][w]: the layer's input (the features for layer 0)
+    const float* g;    // [kin][h][w]: gradient w.r.t. the layer's output (pre-activation)
+    float* partial;    // [gridDim.x][9 * cin * kin + kin]
+    int w, h, tiles_x, tiles;
+    uint32_t* fault;
+};
+
+// Rows of the im2col operand: (tap, input channel) pairs, t * cin + ci; the
+// first 128 in one operand, the rest (tap 8 when cin = 16) in a second one
+// whose other rows stay zero.
+template <int CIN>
+struct BwdWeightLayout {
+    static constexpr int kRows = 9 * CIN;
+    static constexpr int kA1 = kRows > 128;                      // a second 128-row operand
+    static constexpr int kWinPlane = (kNetPos + 2 * kNetGuard) * 2;  // bytes of one bf16 channel plane
+    static constexpr int kWin = CIN * kWinPlane;
+    static constexpr int kK = 64;                                // positions per chunk (one window row)
+    static constexpr int kABytes = 128 * kK * 2;                 // 16 KB
+    static constexpr int kBBytes = 16 * kK * 2;                  // 2 KB
+    static constexpr int kBuf = (1 + kA1) * kABytes + 2 * kBBytes;
+    static constexpr int kSmem = kWin + 2 * kBuf;
+};
+
+template <int CIN, int KIN, bool kFirst>
+__global__ void __launch_bounds__(kBwdThreads, 1) k_net_bwd_weight_tc(NetBwdWeightArgs A) {
+    using L = BwdWeightLayout<CIN>;
+    constexpr int kTmemCols = 32;  // D0 in columns 0-15, D1 in 16-31
+    __shared__ uint64_t mbar[2];
+    __shared__ uint32_t tmem_base_s;
+    __shared__ uint32_t abort_s;
+    uint8_t* smem = reinterpret_cast<uint8_t*>(svo_dsmem);
+    const uint32_t sbase = smem_addr(smem);
+    const uint16_t* win = reinterpret_cast<const uint16_t*>(smem);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int W = A.w, H = A.h;
+    const size_t n = (size_t)W * H;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base_s)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (tid < 2) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[tid])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (tid == 0) abort_s = 0;
+    {  // zero everything: window guards and the operand rows staging never writes
+        uint4* z = reinterpret_cast<uint4*>(smem);
+        for (int i = tid; i < L::kSmem / 16; i += kBwdThreads) z[i] = make_uint4(0, 0, 0, 0);
+    }
+    __syncthreads();
+    const uint32_t tmem = tmem_base_s;
+    float bias_acc = 0.0f;  // thread i sums g of output channel i / 32
+    uint32_t chunks = 0, fault = 0;
+    bool ok = true;
+
+    for (int item = blockIdx.x; item < A.tiles && ok; item += gridDim.x) {
+        const int ox = (item % A.tiles_x) * kBwdOutW, oy = (item / A.tiles_x) * kBwdOutH;
+        const int wx = ox - 1, wy = oy - 1;
+        // the input window, bf16 channel planes with a guard of kNetGuard positions
+        for (int i = tid; i < CIN * kNetPos; i += kBwdThreads) {
+            const int ci = i / kNetPos, p = i % kNetPos;
+            const int gx = wx + (p & (kNetTW - 1)), gy = wy + (p >> 6);
+            float v = 0.0f;
+            if (gx >= 0 && gx < W && gy >= 0 && gy < H) v = __ldg(A.a + ci * n + (size_t)gy * W + gx);
+            if (kFirst) v = bf16_round(v);
+            reinterpret_cast<uint16_t*>(smem)[ci * (L::kWinPlane / 2) + kNetGuard + p] = (uint16_t)bf16_bits(v);
+        }
+        __syncthreads();
+        for (int c = 0; c < kBwdOutH && ok; ++c, ++chunks) {
+            const uint32_t buf = chunks & 1u;
+            if (chunks >= 2) {  // the MMAs of chunk (chunks - 2) read this buffer
+                const bool r = mbar_wait_phase(smem_addr(&mbar[buf]), ((chunks - 2) >> 1) & 1u);
+                if (!r) atomicOr(&abort_s, 1u);
+                __syncthreads();
+                if (abort_s) {
+                    ok = false;
+                    fault |= kFaultNet;
+                    break;
+                }
+            }
+            uint8_t* bufp = smem + L::kWin + buf * L::kBuf;
+            const int row = c + 1;  // window row of this chunk's positions
+            // im2col rows (t, ci): 8 positions of channel ci shifted by tap t per item
+            for (int it = tid; it < L::kRows * (L::kK / 8); it += kBwdThreads) {
+                const int r = it >> 3, kc = it & 7;
+                const int t = r / CIN, ci = r % CIN;
+                const int off = (t / 3 - 1) * kNetTW + (t % 3 - 1);
+                const int p0 = row * kNetTW + kc * 8 + off;
+                const uint16_t* s = win + ci * (L::kWinPlane / 2) + kNetGuard + p0;
+                uint4 v;
+                v.x = (uint32_t)s[0] | (uint32_t)s[1] << 16;
+                v.y = (uint32_t)s[2] | (uint32_t)s[3] << 16;
+                v.z = (uint32_t)s[4] | (uint32_t)s[5] << 16;
+                v.w = (uint32_t)s[6] | (uint32_t)s[7] << 16;
+                const int op = r >> 7, rr = r & 127;  // operand and its row
+                *reinterpret_cast<uint4*>(bufp + op * L::kABytes + kc * 2048 + rr * 16) = v;
+            }
+            // gradient rows (co): hi and lo parts of 64 positions, zero outside the tile
+            {
+                const int co = tid >> 5, k = 2 * lane;
+                uint16_t* bh = reinterpret_cast<uint16_t*>(bufp + (1 + L::kA1) * L::kABytes);
+                uint16_t* bl = bh + L::kBBytes / 2;
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                    const int kk = k + e;
+                    const int gx = wx + kk, gy = wy + row;
+                    float v = 0.0f;
+                    if (co < KIN && kk >= 1 && kk <= kBwdOutW && gx < W && gy < H)
+                        v = __ldg(A.g + co * n + (size_t)gy * W + gx);
+                    bias_acc += v;
+                    uint32_t hi, lo;
+                    split_bf16(v, hi, lo);
+                    const int idx = (co >> 3) * (8 * L::kK) + (kk >> 3) * 64 + (co & 7) * 8 + (kk & 7);
+                    bh[idx] = (uint16_t)hi;
+                    bl[idx] = (uint16_t)lo;
+                }
+            }
+            fence_async_smem();
+            tc_fence_before();
+            __syncthreads();
+            tc_fence_after();
+            if (tid == 0) {
+                const uint32_t a0 = sbase + (uint32_t)(L::kWin + buf * L::kBuf);
+                const uint32_t bhi = a0 + (uint32_t)((1 + L::kA1) * L::kABytes), blo = bhi + (uint32_t)L::kBBytes;
+#pragma unroll
+                for (int s = 0; s < L::kK / 16; ++s) {
+                    const uint32_t acc = (chunks > 0 || s > 0) ? 1u : 0u;
+                    const uint64_t bdh = tc_desc(bhi + (uint32_t)s * 256u, 128u, 1024u);
+                    const uint64_t bdl = tc_desc(blo + (uint32_t)s * 256u, 128u, 1024u);
+                    const uint64_t ad0 = tc_desc(a0 + (uint32_t)s * 4096u, 2048u, 128u);
+                    tc_mma(tmem, ad0, bdh, acc);
+                    tc_mma(tmem, ad0, bdl, 1u);
+                    if (L::kA1) {
+                        const uint64_t ad1 = tc_desc(a0 + (uint32_t)L::kABytes + (uint32_t)s * 4096u, 2048u, 128u);
+                        tc_mma(tmem + 16u, ad1, bdh, acc);
+                        tc_mma(tmem + 16u, ad1, bdl, 1u);
+                    }
+                }
+                tc_commit(smem_addr(&mbar[buf]));
+            }
+        }
+        __syncthreads();  // every thread has read the window before the next tile restages it
+    }
+    // wait for the last chunk on each buffer
+    if (ok && chunks > 0) {
+        bool r = true;
+        for (uint32_t b = 0; b < 2 && b < chunks; ++b) {
+            const uint32_t last = (chunks - 1u) - ((chunks - 1u - b) & 1u);  // last chunk staged in buffer b
+            r = r && mbar_wait_phase(smem_addr(&mbar[b]), (last >> 1) & 1u);
+        }
+        if (!r) atomicOr(&abort_s, 1u);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    constexpr int kVals = 9 * CIN * KIN + KIN;
+    float* dst = A.partial + (size_t)blockIdx.x * kVals;
+    if (ok && !abort_s) {
+        if (warp < 4) {
+            float v[16];
+            if (chunks > 0) {
+                tc_ld16(tmem + ((uint32_t)(32 * warp) << 16), v);
+            } else {
+#pragma unroll
+                for (int c = 0; c < 16; ++c) v[c] = 0.0f;
+            }
+            const int r = 32 * warp + lane;
+            if (r < (L::kA1 ? 128 : L::kRows))
+#pragma unroll
+                for (int c = 0; c < KIN; ++c) dst[r * KIN + c] = v[c];
+            if (L::kA1) {
+                if (chunks > 0) {
+                    tc_ld16(tmem + ((uint32_t)(32 * warp) << 16) + 16u, v);
+                }
+                if (r < L::kRows - 128)
+#pragma unroll
+                    for (int c = 0; c < KIN; ++c) dst[(128 + r) * KIN + c] = v[c];
+            }
+        }
+        // biases: warp co sums its lanes' partial sums in a fixed order
+        float s = bias_acc;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0 && warp < KIN) dst[9 * CIN * KIN + warp] = s;
+    } else {
+        fault |= kFaultNet;
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+    }
+    if (fault && tid == 0) atomicOr(A.fault, fault);
+}
+
+}  // namespace svo

@@ -609,11 +609,15 @@ class Net:
     def infer(self, d_features: int, w: int, h: int, d_out: int) -> None:
         _check(self._lib.svo_net_infer(self._h, _P(d_features), w, h, _P(d_out)), self.ctx)
 
-    def backward(self, d_features: int, d_target_bgrx: int, w: int, h: int, tau: float, lam: float):
+    def backward(self, d_features: int, d_target_bgrx: int, w: int, h: int, tau: float, lam: float,
+                 read_loss: bool = True):
+        """Gradients of the loss into the net (forward + backward on the tensor
+        cores); returns the two loss terms, or None with read_loss=False (no
+        host synchronisation)."""
         loss = np.zeros(2, np.float32)
-        _check(self._lib.svo_net_backward(self._h, _P(d_features), _P(d_target_bgrx), w, h, tau, lam, _ptr(loss)),
-               self.ctx)
-        return float(loss[0]), float(loss[1])
+        _check(self._lib.svo_net_backward(self._h, _P(d_features), _P(d_target_bgrx), w, h, tau, lam,
+                                          _ptr(loss) if read_loss else None), self.ctx)
+        return (float(loss[0]), float(loss[1])) if read_loss else None
 
     def adam(self, lr: float, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8) -> None:
         _check(self._lib.svo_net_adam(self._h, lr, beta1, beta2, eps), self.ctx)

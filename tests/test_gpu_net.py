@@ -1,7 +1,10 @@
-"""GPU tests of the reconstruction net: the FP32 CUDA-core forward and its
-gradients against the CPU restatement (oracle/net_oracle.py), the Adam step,
-the tensor-core inference kernel against the FP32 forward, and learned warp
-frames (all pixels requested -> exactly the full raycast; the feature tap)."""
+"""GPU tests of the reconstruction net: the FP32 CUDA-core forward against the
+CPU restatement (oracle/net_oracle.py); the training step's gradients -- the
+tensor-core forward keeping its activations, then the tensor-core backward
+convolutions (data and weight gradients) -- against the restatement's; the
+Adam step; the tensor-core inference kernel against the FP32 forward; and
+learned warp frames (all pixels requested -> exactly the full raycast; the
+feature tap)."""
 import numpy as np
 import pytest
 
@@ -50,8 +53,10 @@ def test_forward_matches_oracle(svo, gpu_ctx, net, W, H):
     assert np.abs(got - ref).mean() < 1e-4 * scale
 
 
-def test_gradients_match_oracle(svo, gpu_ctx, net):
-    W, H = 45, 31
+@pytest.mark.parametrize("W,H", [(45, 31), (130, 70), (200, 124), (5, 3)])
+def test_gradients_match_oracle(svo, gpu_ctx, net, W, H):
+    # one 62x30 tile of the backward kernels, several ragged tiles, more
+    # tiles than a handful of CTAs, and a frame smaller than one 3x3 window
     params, feat, tgt = _rand_case(5, W, H)
     net.set_params(params)
     df, dt = _dev(feat), _dev(tgt.view(np.int32))
