@@ -539,6 +539,8 @@ def measure_config1(svo, torch, device, seed, no_cpu: bool, steps: int = 20):
                                        and np.array_equal(xyzw.view(np.uint32), oxyzw.view(np.uint32)))
         out["boundary_ray_fraction"] = float(st[3]) / float(st[0])
         out["boundary_rays"] = int(st[3])
+        out["hit_boundary_ray_fraction"] = float(st[6]) / float(st[0])
+        out["mismatching_rays"] = int(np.count_nonzero(col != ocol))
     tgt.close()
     ctx.close()
     return out
@@ -944,6 +946,9 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                                           1.0, 1.0, threads)
         bytes_per_ray = (4.0 * (float(st[1]) + float(st[2])) + 20.0 * float(st[0])) / float(st[0])
         boundary = {"fraction": float(st[3]) / float(st[0]), "rays": int(st[3]), "of": int(st[0]),
+                    "hit_fraction": float(st[6]) / float(st[0]),
+                    "definition": "fraction: a step landed a coordinate within 1 ulp of a leaf face; hit_fraction: "
+                                  "the hit point lies within 1 ulp of a face of its cell (other than the entry face)",
                     "frame": "full raycast of the last timed orbit frame"}
         if args.guided:
             # the same count for the guided walks of that frame, from the start

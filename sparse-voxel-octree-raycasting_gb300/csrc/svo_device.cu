@@ -589,7 +589,7 @@ svo_status enqueue_learned_body(svo_context* ctx, svo_target* t, const svo_net* 
     A.logit_threshold = logit_threshold;
     svo_status st = launch_net_infer(ctx, net, true, A);
     if (st != SVO_OK) return st;
-    {
+    if (!t->B.guide) {  // guided frames' requests are appended by the net kernel itself
         const size_t packets = (size_t)t->B.packets_x * t->B.packets_y;
         const unsigned nb = (unsigned)((packets + kReqBlock - 1) / kReqBlock);
         k_request_scan<<<nb, kReqBlock, 0, s>>>(t->B, t->req_offs, t->req_offs + packets);

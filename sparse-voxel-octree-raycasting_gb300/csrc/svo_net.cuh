@@ -797,11 +797,26 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_infer(NetInferArgs A) {
                             req = !sP.have_cache ||
                                   (!(z >= A.logit_threshold) && !(list && __ldg(A.B.guide + ofs) >= 0.0f));
                         }
-                        // Ray requests: bit (x&7) + 8*(y&3) of the pixel's 8x4 packet. The
-                        // warp's lanes are consecutive pixels of one row, so the first lane
-                        // of each run of one packet ORs the run's bits in one atomic.
                         const uint32_t bal = __ballot_sync(0xffffffffu, req);
-                        if (bal && (lane == 0 || (gx & 7) == 0)) {
+                        if (list) {
+                            // Guided frames request few rays (the unguided pixels the net is
+                            // not confident about): the warp appends them to the hole list
+                            // itself, one atomic per warp, instead of the packet masks and
+                            // their two compaction kernels. The list's order varies; every
+                            // pixel's ray does not depend on it.
+                            if (bal) {
+                                uint32_t base = 0;
+                                if (lane == 0) base = atomicAdd(A.B.counters + 1, (uint32_t)__popc(bal));
+                                base = __shfl_sync(0xffffffffu, base, 0);
+                                const uint32_t at = base + (uint32_t)__popc(bal & ((1u << lane) - 1u));
+                                if (req && at < (uint32_t)W * (uint32_t)H)
+                                    A.B.ids[2u * (uint32_t)A.B.tiles_x * (uint32_t)A.B.tiles_y + at] =
+                                        (uint32_t)gx | ((uint32_t)gy << 16);
+                            }
+                        } else if (bal && (lane == 0 || (gx & 7) == 0)) {
+                            // Ray requests: bit (x&7) + 8*(y&3) of the pixel's 8x4 packet. The
+                            // warp's lanes are consecutive pixels of one row, so the first lane
+                            // of each run of one packet ORs the run's bits in one atomic.
                             const int len = min(8 - (gx & 7), 32 - lane);
                             const uint32_t run = (bal >> lane) & ((1u << len) - 1u);
                             if (run)
