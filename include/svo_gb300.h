@@ -305,6 +305,15 @@ svo_status svo_read_requested(svo_target* t, uint32_t* count);
 svo_status svo_target_set_guided(svo_target* t, int enable);
 /* The start distances of the last guided frame, res_x*res_y floats in raypos
  * units (16 per world unit; 0 = from the camera, -1 = unguided). */
+/* Certified reprojection in guided learned frames (no reference counterpart;
+ * on by default): a guided pixel whose own ray provably meets the face a
+ * cached hit point of its 3x3 neighbourhood lies on -- the hit codes the
+ * learned frames keep in w of the coordinate planes (level | ray signs << 5,
+ * -1 without a hit) name the face -- takes that point's colour and needs no
+ * walk (start distance -2 in svo_read_guide), unless a cached point lies more
+ * than 2 cells in front of the face, a hole is next to it or it is in the
+ * refresh tile. enable = 0 walks every guided pixel. */
+svo_status svo_target_set_certified(svo_target* t, int enable);
 svo_status svo_read_guide(svo_target* t, float* host);
 /* Training tap: when d_features is not NULL, every later frame of the target
  * (plain or learned) writes the net's input features after reprojection to

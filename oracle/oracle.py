@@ -69,6 +69,7 @@ def oracle() -> ctypes.CDLL:
         lib.orc_guided_create.argtypes = [i, i, i]
         lib.orc_guided_free.argtypes = [_P]
         lib.orc_guided_frame.argtypes = [_P, _P, sz, u32, _P, _P, i, i]
+        lib.orc_guided_set_certify.argtypes = [_P, i]
         for name in ("orc_guided_colour", "orc_guided_coords", "orc_guided_guide"):
             getattr(lib, name).restype = _P
             getattr(lib, name).argtypes = [_P]
@@ -212,12 +213,13 @@ class Guided:
     reprojection of the last frame's plane re-based by whole periods, start
     distances, rays from the camera and walks. Test infrastructure only."""
 
-    def __init__(self, depth: int, res_x: int, res_y: int):
+    def __init__(self, depth: int, res_x: int, res_y: int, certify: bool = False):
         self.n = res_x * res_y
         self._lib = oracle()
         self._h = self._lib.orc_guided_create(depth, res_x, res_y)
         if not self._h:
             raise ValueError("guided frames: resolution must be at least 16x16")
+        self._lib.orc_guided_set_certify(self._h, 1 if certify else 0)
 
     def frame(self, words, root, pos, m, frame: int, threads: int = 0) -> None:
         words = np.ascontiguousarray(words, np.uint32)

@@ -202,6 +202,8 @@ struct Ray {
     uint32_t child_fetches, colour_fetches, steps;
     bool boundary;     // a non-stepping coordinate landed within 1 ulp of an integer
     bool hit_boundary; // the hit point lies within 1 ulp of a face of its hit cell (other than the entry face)
+    int level;         // level of the hit cell (its edge is 2^level raypos units), -1 without a hit
+    uint32_t signs;    // the ray's direction signs, bit a set when component a < 0
 };
 
 struct Tracer {
@@ -414,6 +416,8 @@ struct Tracer {
             }
             r.voxel = key;
         }
+        r.level = hit ? rek : -1;
+        r.signs = sign_xyz;
         return r;
     }
 };
@@ -747,6 +751,110 @@ int orc_raycast_guided_steps(int depth, const uint32_t* words, size_t n_words, u
     return 0;
 }
 
+// ------------------------------------------------ certified reprojection --
+// The product's learned frames certify a reprojected colour without a walk
+// when the pixel's own ray provably meets a face a cached hit point lies on.
+// Every cached point carries its hit code in w: the level L of its hit cell
+// (edge s = 2^L raypos units) and the signs of the ray that found it. The hit
+// point lies on the cell's entry face: exactly one of its coordinates (raypos
+// units) is a multiple of s, and the old ray crossed that plane in the
+// direction its sign bit gives. The pixel's ray (the ray kernels' direction,
+// not normalised) meets the plane at parameter t; the candidate passes when
+// the ray crosses the plane the same way, t > 0, the other two coordinates of
+// the meeting point lie inside the cell's face with a margin of s/64, the
+// level of detail at the meeting distance is L a thirty-second either side,
+// and that distance is at most 2 cells behind the nearest reprojected point of
+// the 3x3 neighbourhood (nothing cached lies in front). Of the passing
+// candidates of the 3x3 neighbourhood the nearest (smallest t, the first in
+// row order on a tie) is taken: colour byte, meeting point, code. Every
+// operation is one IEEE binary32 operation, as on the GPU.
+constexpr float kGuideCertified = -2.0f;
+
+inline float hit_code(const Ray& r) { return r.level < 0 ? -1.0f : (float)(r.level | (int)(r.signs << 5)); }
+
+inline int lod_at(float s, int res_x) {
+    float sw = (float)(2 * res_x);
+    int lod = 1;
+    while (s > sw && lod < 24) {
+        sw *= 2.0f;
+        ++lod;
+    }
+    return lod;
+}
+
+struct Certified {
+    uint32_t colour;
+    float xyzw[4];
+};
+
+bool certify(const View& v, int res_x, int res_y, int x, int y, const uint32_t* col, const float* xyz, float near_s,
+             Certified& out) {
+    float d1[3];
+    d1[0] = (float)((double)(x - res_x / 2) + 0.5) * 1.0f / (float)res_y;
+    d1[1] = (float)((double)(y - res_y / 2) + 0.5) * 1.0f / (float)res_y;
+    d1[2] = 1.0f;
+    const float d[3] = {dot3(d1, v.mx), dot3(d1, v.my), dot3(d1, v.mz)};
+    const float cam[3] = {v.pos[0] * 16.0f, v.pos[1] * 16.0f, v.pos[2] * 16.0f};
+    const float dlen = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    const uint32_t signs = (d[0] < 0.0f ? 1u : 0u) | (d[1] < 0.0f ? 2u : 0u) | (d[2] < 0.0f ? 4u : 0u);
+    float best = INFINITY;
+    bool found = false;
+    for (int j = -1; j <= 1; ++j)
+        for (int i = -1; i <= 1; ++i) {
+            const int xi = x + i, yj = y + j;
+            if (xi < 0 || xi >= res_x || yj < 0 || yj >= res_y) continue;
+            const size_t o = (size_t)yj * res_x + xi;
+            if (col[o] == kEmpty) continue;
+            const float code = xyz[o * 4 + 3];
+            if (!(code >= 0.0f)) continue;
+            const int ic = (int)code;
+            const int L = ic & 31;
+            const uint32_t sb = (uint32_t)ic >> 5;
+            uint32_t sbits = (uint32_t)(127 + L) << 23, ibits = (uint32_t)(127 - L) << 23;
+            float cs, inv;
+            std::memcpy(&cs, &sbits, 4);
+            std::memcpy(&inv, &ibits, 4);
+            float p[3], f[3];
+            int axis = -1, on = 0;
+            for (int a = 0; a < 3; ++a) {
+                p[a] = xyz[o * 4 + a] * 16.0f;
+                f[a] = std::floor(p[a] * inv);
+                if (f[a] * cs == p[a]) {
+                    axis = a;
+                    ++on;
+                }
+            }
+            if (on != 1) continue;
+            const float da = d[axis];
+            if (((sb >> axis) & 1u) ? !(da < 0.0f) : !(da > 0.0f)) continue;
+            const float t = (p[axis] - cam[axis]) / da;
+            if (!(t > 0.0f)) continue;
+            float q[3];
+            bool inside = true;
+            for (int b = 0; b < 3; ++b) {
+                if (b == axis) {
+                    q[b] = p[b];
+                    continue;
+                }
+                q[b] = cam[b] + t * d[b];
+                const float r = (q[b] - f[b] * cs) * inv;
+                inside = inside && r > 0.015625f && r < 0.984375f;
+            }
+            if (!inside) continue;
+            const float dist = t * dlen;
+            if (lod_at(dist * 0.96875f, res_x) != L || lod_at(dist * 1.03125f, res_x) != L) continue;
+            if (!(dist - near_s <= 2.0f * cs)) continue;
+            if (t < best) {
+                best = t;
+                found = true;
+                out.colour = 0xff000000u | (col[o] & 255u);
+                for (int a = 0; a < 3; ++a) out.xyzw[a] = q[a] * 0.0625f;
+                out.xyzw[3] = (float)(L | (int)(signs << 5));
+            }
+        }
+    return found;
+}
+
 // Guided learned frames with every unguided pixel traced: the product's
 // svo_warp_frame_learned on a guided target with a confidence threshold no
 // pixel reaches (the net then decides nothing; the reference has no such
@@ -764,6 +872,7 @@ struct Guided {
     std::vector<float> guide;
     float cache_pos[3] = {0, 0, 0};
     int cache = -1;  // plane holding the last frame, -1 before the first frame
+    bool certify = false;
 };
 
 void* orc_guided_create(int depth, int res_x, int res_y) {
@@ -782,6 +891,7 @@ void* orc_guided_create(int depth, int res_x, int res_y) {
     return g;
 }
 void orc_guided_free(void* h) { delete static_cast<Guided*>(h); }
+void orc_guided_set_certify(void* h, int enable) { static_cast<Guided*>(h)->certify = enable != 0; }
 const uint32_t* orc_guided_colour(void* h) {
     Guided* g = static_cast<Guided*>(h);
     return g->col[g->cache < 0 ? 0 : g->cache].data();
@@ -841,13 +951,19 @@ int orc_guided_frame(void* h, const uint32_t* words, size_t n_words, uint32_t ro
             const float q[3] = {sx[(size_t)src * 4 + 0] + shift[0], sx[(size_t)src * 4 + 1] + shift[1],
                                 sx[(size_t)src * 4 + 2] + shift[2]};
             float p[3] = {q[0] - v.pos[0], q[1] - v.pos[1], q[2] - v.pos[2]};
+            (void)p;
             col[t] = (hi & ~255u) + (sc[src] & 255u);
             xyz[t * 4 + 0] = q[0];
             xyz[t * 4 + 1] = q[1];
             xyz[t * 4 + 2] = q[2];
-            xyz[t * 4 + 3] = dot3(p, v.vz);
+            xyz[t * 4 + 3] = sx[(size_t)src * 4 + 3];  // the hit code travels with the point
         }
     }
+    const int ax = (res_x / 8) * (frame & 7), ay = (res_y / 4) * ((frame >> 3) & 3);
+    const int xe = std::min(res_x, ax + (res_x / 8 + 15) / 16 * 16);
+    const int ye = std::min(res_y, ay + (res_y / 4 + 15) / 16 * 16);
+    std::vector<uint32_t> cert_col(N, 0u);
+    std::vector<float> cert_xyz(N * 4, 0.0f);
     // start distances: the 3x3 minimum of the reprojected points' camera
     // distances, less 4 cells of the level of detail there; half that minimum
     // for a pixel with at least 3 holes (pixels of the frame without a point)
@@ -886,21 +1002,35 @@ int orc_guided_frame(void* h, const uint32_t* words, size_t n_words, uint32_t ro
                 ++lod;
             }
             gd = holes >= 3 ? s * 0.5f : std::fmax(s - 4.0f * (float)(1 << lod), 0.0f);
+            const bool rect = x >= ax && x < xe && y >= ay && y < ye;
+            if (g.certify && holes == 0 && !rect) {
+                Certified c;
+                if (certify(v, res_x, res_y, x, y, col.data(), xyz.data(), s, c)) {
+                    gd = kGuideCertified;
+                    cert_col[t] = c.colour;
+                    for (int a = 0; a < 4; ++a) cert_xyz[t * 4 + a] = c.xyzw[a];
+                }
+            }
         }
         g.guide[t] = gd;
     }
     // rays: the refresh tile (raycast.h:363-366) and the unguided pixels (all of
-    // them without a cache) from the camera, every other pixel walked
-    const int ax = (res_x / 8) * (frame & 7), ay = (res_y / 4) * ((frame >> 3) & 3);
-    const int xe = std::min(res_x, ax + (res_x / 8 + 15) / 16 * 16);
-    const int ye = std::min(res_y, ay + (res_y / 4 + 15) / 16 * 16);
+    // them without a cache) from the camera, every other pixel walked, except
+    // the certified ones, which take the certified colour and point
 #pragma omp parallel for schedule(dynamic, 4)
     for (int y = 0; y < res_y; ++y)
         for (int x = 0; x < res_x; ++x) {
             const size_t t = (size_t)y * res_x + x;
             const bool rect = x >= ax && x < xe && y >= ay && y < ye;
+            if (!rect && have_cache && g.guide[t] == kGuideCertified) {
+                col[t] = cert_col[t];
+                for (int a = 0; a < 4; ++a) xyz[t * 4 + a] = cert_xyz[t * 4 + a];
+                continue;
+            }
             const float s0 = (rect || !have_cache || g.guide[t] < 0.0f) ? 0.0f : g.guide[t];
-            store_ray_plane(col.data(), xyz.data(), t, tr.trace(v, x, y, res_x, res_y, 1.0f, 1.0f, s0));
+            const Ray r = tr.trace(v, x, y, res_x, res_y, 1.0f, 1.0f, s0);
+            store_ray_plane(col.data(), xyz.data(), t, r);
+            xyz[t * 4 + 3] = hit_code(r);
         }
     g.cache = cur;
     for (int i = 0; i < 3; ++i) g.cache_pos[i] = v.pos[i];

@@ -105,6 +105,7 @@ struct svo_target {
     uint32_t* req_offs = nullptr;  // learned frames: request offsets per 8x4 packet
     // guided learned frames (walks from the cached depth); buffers in B
     bool guided = false;
+    bool certify = true;  // certified reprojection in guided learned frames
     float* d_guide = nullptr;
     // camera position each physical plane's points were written under (the
     // rebase of learned frames across wraps of the periodic volume)
@@ -481,6 +482,7 @@ FrameParams make_params(const svo_target* t, const svo_view& v, int frame, const
         p.prev_vz[i] = t->prev_view.m[8 + i];
     }
     p.serial = (uint32_t)(t->frames + 1);
+    p.certify = (learned && t->guided && t->certify) ? 1 : 0;
     if (learned) {
         const float period = (float)(1u << (t->ctx->depth + 1)) / 16.0f;  // world units
         p.rebase = 1;
@@ -1307,9 +1309,12 @@ svo_status svo_target_create(svo_context* ctx, int res_x, int res_y, svo_target*
     A((void**)&t->req_offs, (packets + (packets + kReqBlock - 1) / kReqBlock) * 4);  // offsets + block totals
     const size_t net_tiles = (size_t)((res_x + kNetOutW - 1) / kNetOutW) * ((res_y + kNetOutH - 1) / kNetOutH);
     A((void**)&t->d_guide, N * 4);
-    // walk packets of any shape pw x (32/pw), pw in 4..32: at most N/32 + res_x/4 + res_y + 1
-    t->B.walk_cap = (uint32_t)(N / 32 + res_x / 4 + res_y + 64);
-    A((void**)&t->B.walk_list, (size_t)t->B.walk_cap * 4);
+    // guided frames' pixel lists (walks, certified pixels) and certified results
+    t->B.walk_cap = (uint32_t)N;
+    A((void**)&t->B.walk_list, N * 4);
+    A((void**)&t->B.cert_list, N * 4);
+    A((void**)&t->B.cert_col, N * 4);
+    A((void**)&t->B.cert_xyz, N * 16);
     A((void**)&t->B.net_flags, net_tiles * 4);
     A((void**)&t->B.net_list, net_tiles * 4);
     A((void**)&t->B.counters, 64);
@@ -1351,7 +1356,8 @@ svo_status svo_target_destroy(svo_target* t) {
     for (auto& g : t->graphs) g.reset();
     void* ptrs[] = {t->B.col[0], t->B.col[1], t->B.col[2], t->B.xyz[0], t->B.xyz[1], t->B.xyz[2], t->B.disp, t->B.bgrx, t->B.keys, t->B.ids,
                     t->B.tile_mask, t->B.counters, t->d_params, t->full_col, t->full_xyzw, t->full_vox,
-                    t->B.req_mask, t->req_offs, t->d_guide, t->B.net_flags, t->B.net_list, t->B.walk_list};
+                    t->B.req_mask, t->req_offs, t->d_guide, t->B.net_flags, t->B.net_list, t->B.walk_list,
+                    t->B.cert_list, t->B.cert_col, t->B.cert_xyz};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (auto& e : t->ev)
@@ -1904,6 +1910,12 @@ svo_status svo_target_set_guided(svo_target* t, int enable) {
     if (!t) return SVO_ERR_INVALID_ARGUMENT;
     t->guided = enable != 0;
     t->B.guide = t->guided ? t->d_guide : nullptr;
+    return SVO_OK;
+}
+
+svo_status svo_target_set_certified(svo_target* t, int enable) {
+    if (!t) return SVO_ERR_INVALID_ARGUMENT;
+    t->certify = enable != 0;
     return SVO_OK;
 }
 

@@ -51,6 +51,7 @@ struct FrameParams {
     int rebase;
     float src_shift[2][3];
     uint32_t serial;  // frame serial of the target (stamps the net tile flags)
+    int certify;      // guided frames: certified reprojection (k_guide)
 };
 
 // Buffers of one render target.
@@ -69,15 +70,21 @@ struct TargetBuffers {
     // tile, the serial of the last frame that needed the net there, and the
     // list of those tiles (count in counters[3]). guide == nullptr: no walks.
     float* guide;
-    // The walk packets (pw x ph) holding at least one walk, listed by k_guide:
-    // those expected to hold a long walk from the front (counters[4] of them),
-    // the others from the back (counters[5]); walk_cap entries.
+    // Pixel lists k_guide writes (entries x | y << 16, walk_cap = res_x*res_y
+    // each): the walks expected to be long from the front of walk_list
+    // (counters[4] of them), the others from its back (counters[5]); the
+    // certified pixels in cert_list (counters[6]), whose colour word and
+    // point k_guide leaves in cert_col / cert_xyz for the tracer to commit.
     uint32_t* walk_list;
     uint32_t walk_cap;
+    uint32_t* cert_list;
+    uint32_t* cert_col;
+    float4* cert_xyz;
     uint32_t* net_flags;
     uint32_t* net_list;
     uint32_t* counters;   // [0] trace work counter, [1] hole entries, [2] coarse-pass work counter,
-                          // [3] net tiles listed, [4] long walk packets listed, [5] other walk packets listed
+                          // [3] net tiles listed, [4] long walks listed, [5] other walks listed,
+                          // [6] certified pixels listed
     int res_x, res_y;
     int tiles_x, tiles_y;  // whole 16x16 tiles (res/16)
 };
@@ -113,7 +120,7 @@ __device__ __forceinline__ float4* plane_xyz(const TargetBuffers& B, int i) {
 __global__ void k_set_params(FrameParams p, FrameParams* dst, uint32_t* counters) {
     *dst = p;
 #pragma unroll
-    for (int i = 0; i < 6; ++i) counters[i] = 0;
+    for (int i = 0; i < 7; ++i) counters[i] = 0;
 }
 
 __global__ void k_reset_counter(uint32_t* counter) { *counter = 0; }
@@ -259,7 +266,9 @@ __global__ void __launch_bounds__(256) k_resolve_gather(const FrameParams* __res
                 const float ax = __fsub_rn(q.x, P->ray.px), ay = __fsub_rn(q.y, P->ray.py),
                             az = __fsub_rn(q.z, P->ray.pz);
                 outc = (hi & ~255u) + (plane_col(B, phys)[src] & 255u);
-                plane_xyz(B, cur)[t] = make_float4(q.x, q.y, q.z, dot3(ax, ay, az, P->vz));
+                // learned frames carry the point's hit code along; plain frames store
+                // the view depth (kernel.cl:585)
+                plane_xyz(B, cur)[t] = make_float4(q.x, q.y, q.z, P->rebase ? q.w : dot3(ax, ay, az, P->vz));
             }
         }
         plane_col(B, cur)[t] = outc;
@@ -420,15 +429,15 @@ __global__ void __launch_bounds__(BLOCK) k_trace_full(Octree o_in, const FullBat
     if (fault) atomicOr(fault_out, fault);
 }
 
-// kBgrx (learned frames): also writes the traced pixels' colourised output,
-// and with a guide buffer walks every guided pixel after the requested rays
-// and the refresh tile: the walk packets k_guide listed (those holding a
-// walk), each guided pixel's ray starting at its guide distance (pixels of
-// the refresh tile and unguided pixels are skipped). Requested pixels are
-// unguided, so every pixel is written at most once and the walks read
-// nothing the launch writes. The packets k_guide expects to be long (a depth
-// edge inside: some pixel walks from the near side) come first in the list,
-// so the launch does not end on a long packet.
+// kBgrx (learned frames): also writes the traced pixels' colourised output
+// and, in w, the hit code instead of the distance; with a guide buffer it
+// walks the pixels k_guide listed after the requested rays and the refresh
+// tile, 32 list entries per packet, each ray starting at the pixel's guide
+// distance -- the walks k_guide expects to be long (a depth edge nearby: the
+// start comes from the near side) first, so the launch does not end on a long
+// walk -- and finally commits the certified pixels' colour words and points.
+// Requested pixels are unguided and neither walked nor certified, so every
+// pixel is written at most once and the walks read nothing the launch writes.
 template <int DEPTH, int BLOCK, bool kBgrx>
 __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FrameParams* __restrict__ P,
                                                     TargetBuffers B, uint32_t* fault_out) {
@@ -447,10 +456,11 @@ __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FramePa
     const uint32_t rpx = (uint32_t)max(0, (xe - ax + pw - 1) / pw), rpy = (uint32_t)max(0, (ye - ay + ph - 1) / ph);
     const uint32_t fixed = hole_packets + rpx * rpy;
     const float* __restrict__ guide = kBgrx ? B.guide : nullptr;
-    const uint32_t wpx = (uint32_t)((res_x + pw - 1) / pw);
     const uint32_t n_long = guide ? min(B.counters[4], B.walk_cap) : 0u;
-    const uint32_t n_walk = guide ? min(n_long + B.counters[5], B.walk_cap) : 0u;
-    const uint32_t total = fixed + n_walk;
+    const uint32_t n_short = guide ? min(B.counters[5], B.walk_cap - n_long) : 0u;
+    const uint32_t n_cert = guide ? min(B.counters[6], B.walk_cap) : 0u;
+    const uint32_t p_long = (n_long + 31u) / 32u, p_short = (n_short + 31u) / 32u, p_cert = (n_cert + 31u) / 32u;
+    const uint32_t total = fixed + p_long + p_short + p_cert;
     const RayCam cam = P->ray;
     float4* __restrict__ xyz = plane_xyz(B, P->cur);
     uint32_t* __restrict__ col = plane_col(B, P->cur);
@@ -463,11 +473,36 @@ __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FramePa
         bool valid;
         float s0 = 0.0f;
         if (kBgrx && p >= fixed) {
-            const uint32_t k = p - fixed;
-            const uint32_t q = __ldg(B.walk_list + (k < n_long ? k : B.walk_cap - 1u - (k - n_long)));
-            x = (int)(q % wpx) * pw + (lane & (pw - 1));
-            y = (int)(q / wpx) * ph + (lane >> ps);
-            valid = x < res_x && y < res_y && !(x >= ax && x < xe && y >= ay && y < ye);
+            uint32_t k = p - fixed;
+            uint32_t e;
+            if (k < p_long) {
+                e = k * 32u + (uint32_t)lane;
+                valid = e < n_long;
+            } else if ((k -= p_long) < p_short) {
+                e = k * 32u + (uint32_t)lane;
+                valid = e < n_short;
+                e = B.walk_cap - 1u - e;
+            } else {  // certified pixels: commit the colour word and point k_guide left
+                e = (k - p_short) * 32u + (uint32_t)lane;
+                if (e < n_cert) {
+                    const uint32_t xy = __ldg(B.cert_list + e);
+                    const size_t ofs = (size_t)(xy >> 16) * res_x + (xy & 0xffffu);
+                    if ((xy & 0xffffu) < (uint32_t)res_x && (xy >> 16) < (uint32_t)res_y) {
+                        col[ofs] = __ldg(B.cert_col + ofs);
+                        xyz[ofs] = __ldg(B.cert_xyz + ofs);
+                    } else {
+                        fault |= kFaultHoleEntry;
+                    }
+                }
+                continue;
+            }
+            const uint32_t xy = valid ? __ldg(B.walk_list + e) : 0u;
+            x = (int)(xy & 0xffffu);
+            y = (int)(xy >> 16);
+            if (valid && (x >= res_x || y >= res_y)) {
+                fault |= kFaultHoleEntry;
+                valid = false;
+            }
             if (valid) {
                 s0 = __ldg(guide + (size_t)y * res_x + x);
                 valid = s0 >= 0.0f;
@@ -494,7 +529,7 @@ __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FramePa
             const RayResult r = trace_ray<DEPTH, false, kBgrx>(o, cam, x, y, res_x, res_y, stk, BLOCK, fault, s0);
             const size_t ofs = (size_t)y * res_x + x;
             col[ofs] = r.colour;
-            xyz[ofs] = make_float4(r.hx, r.hy, r.hz, r.dist);
+            xyz[ofs] = make_float4(r.hx, r.hy, r.hz, kBgrx ? r.code : r.dist);
             if (kBgrx) B.bgrx[ofs] = colorize(r.colour);
         }
     }

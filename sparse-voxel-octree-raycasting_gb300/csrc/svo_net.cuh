@@ -426,54 +426,168 @@ constexpr int kGuideHoleCount = 3;          // holes in the 3x3 that make a hole
 constexpr float kGuideLong = 64.0f;         // cells between the start and the pixel's own point: a long walk
 constexpr int kGuideBW = 32, kGuideBH = 8;  // pixels per block (whole ray packets of every packet shape)
 
+// Certified reprojection: a guided pixel needs no walk when its own ray
+// provably meets a face a cached hit point of its 3x3 neighbourhood lies on.
+// Every cached point carries its hit code in w (level L of the hit cell, edge
+// s = 2^L raypos units, and the signs of the ray that found it); the point
+// lies on the cell's entry face, the one plane of its three coordinates that
+// is a multiple of s, which the old ray crossed in the direction of its sign.
+// The pixel's ray (the ray kernels' direction, not normalised) meets that
+// plane at parameter t; the candidate passes when the ray crosses the plane
+// the same way, t > 0, the other two coordinates of the meeting point lie
+// inside the face with a margin of s/64, the level of detail at the meeting
+// distance is L a thirty-second either side of it, and that distance is at
+// most kCertifyGap cells behind the 3x3 minimum distance (nothing cached lies
+// in front). The nearest passing candidate (smallest t; the first in row order
+// on a tie) gives the pixel's colour word (0xff000000 | colour byte), point
+// and code. Only pixels outside the refresh tile with no hole in their 3x3
+// are certified. An exact face test alone certified 40% of the orbit's
+// pixels, 3.4% of them wrongly (a surface the cache missed in front of the
+// face); with the gap test 24-26% on both camera paths, 0.3-0.4% wrongly
+// (oracle experiments at 960x512). Every operation is one IEEE binary32
+// operation; the CPU oracle repeats them.
+constexpr float kGuideCertified = -2.0f;  // guide value of a certified pixel
+constexpr float kCertifyGap = 2.0f;       // cells
+
+__device__ __forceinline__ int lod_at(float s, int res_x) {
+    float sw = (float)(2 * res_x);
+    int lod = 1;
+    while (s > sw && lod < 24) {  // the walk's lodswitch doublings
+        sw *= 2.0f;
+        ++lod;
+    }
+    return lod;
+}
+
+struct CertCand {
+    float4 q;    // cached point (world units) and hit code
+    uint32_t c;  // colour word, kEmptyPixel for none
+};
+
+__device__ __forceinline__ bool certify_pixel(const RayCam& cam, int res_x, int res_y, int x, int y,
+                                              const CertCand* cand, int stride, float near_s, uint32_t& out_col,
+                                              float4& out_q) {
+    const float d1x = __fdiv_rn(__fmul_rn(__fadd_rn((float)(x - (res_x >> 1)), 0.5f), cam.fovx), (float)res_y);
+    const float d1y = __fdiv_rn(__fmul_rn(__fadd_rn((float)(y - (res_y >> 1)), 0.5f), cam.fovy), (float)res_y);
+    const float d[3] = {__fadd_rn(__fadd_rn(__fmul_rn(d1x, cam.mxx), __fmul_rn(d1y, cam.mxy)), cam.mxz),
+                        __fadd_rn(__fadd_rn(__fmul_rn(d1x, cam.myx), __fmul_rn(d1y, cam.myy)), cam.myz),
+                        __fadd_rn(__fadd_rn(__fmul_rn(d1x, cam.mzx), __fmul_rn(d1y, cam.mzy)), cam.mzz)};
+    const float c16[3] = {__fmul_rn(cam.px, 16.0f), __fmul_rn(cam.py, 16.0f), __fmul_rn(cam.pz, 16.0f)};
+    const float dlen =
+        __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(d[0], d[0]), __fmul_rn(d[1], d[1])), __fmul_rn(d[2], d[2])));
+    const uint32_t signs = (d[0] < 0.0f ? 1u : 0u) | (d[1] < 0.0f ? 2u : 0u) | (d[2] < 0.0f ? 4u : 0u);
+    float best = INFINITY;
+    bool found = false;
+#pragma unroll 1
+    for (int k = 0; k < 9; ++k) {
+        const CertCand cc = cand[(k / 3) * stride + (k % 3)];
+        if (cc.c == kEmptyPixel || !(cc.q.w >= 0.0f)) continue;
+        const int ic = (int)cc.q.w;
+        const int L = ic & 31;
+        const uint32_t sb = (uint32_t)ic >> 5;
+        const float cs = __int_as_float((127 + L) << 23), inv = __int_as_float((127 - L) << 23);
+        const float p[3] = {__fmul_rn(cc.q.x, 16.0f), __fmul_rn(cc.q.y, 16.0f), __fmul_rn(cc.q.z, 16.0f)};
+        float f[3];
+        int axis = -1, on = 0;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            f[a] = floorf(__fmul_rn(p[a], inv));
+            if (__fmul_rn(f[a], cs) == p[a]) {
+                axis = a;
+                ++on;
+            }
+        }
+        if (on != 1) continue;
+        const float da = axis == 0 ? d[0] : (axis == 1 ? d[1] : d[2]);
+        const float pa = axis == 0 ? p[0] : (axis == 1 ? p[1] : p[2]);
+        const float ca = axis == 0 ? c16[0] : (axis == 1 ? c16[1] : c16[2]);
+        if (((sb >> axis) & 1u) ? !(da < 0.0f) : !(da > 0.0f)) continue;
+        const float t = __fdiv_rn(__fsub_rn(pa, ca), da);
+        if (!(t > 0.0f)) continue;
+        float q[3];
+        bool inside = true;
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            if (b == axis) {
+                q[b] = p[b];
+                continue;
+            }
+            q[b] = __fadd_rn(c16[b], __fmul_rn(t, d[b]));
+            const float r = __fmul_rn(__fsub_rn(q[b], __fmul_rn(f[b], cs)), inv);
+            inside = inside && r > 0.015625f && r < 0.984375f;
+        }
+        if (!inside) continue;
+        const float dist = __fmul_rn(t, dlen);
+        if (lod_at(__fmul_rn(dist, 0.96875f), res_x) != L || lod_at(__fmul_rn(dist, 1.03125f), res_x) != L) continue;
+        if (!(__fsub_rn(dist, near_s) <= __fmul_rn(kCertifyGap, cs))) continue;
+        if (t < best) {
+            best = t;
+            found = true;
+            out_col = 0xff000000u | (cc.c & 255u);
+            out_q = make_float4(__fmul_rn(q[0], 0.0625f), __fmul_rn(q[1], 0.0625f), __fmul_rn(q[2], 0.0625f),
+                                (float)(L | (int)(signs << 5)));
+        }
+    }
+    return found;
+}
+
 // Also lists the net tiles (kNetOutW x kNetOutH) holding an unguided pixel:
 // the first block to find one in a tile stamps the tile with this frame's
 // serial and appends it (a block of 32 x 8 pixels touches at most 2 x 2
-// tiles). And it lists the walk packets (pw x ph, eight per block) that hold
-// a walk -- a guided pixel outside the refresh tile -- for the tracer: from
-// the front those holding a long walk (a pixel whose own reprojected point,
-// else the farthest around it, lies more than kGuideLong cells beyond its
-// start: a depth edge, where the start comes from the near side), which the
-// tracer walks first, from the back the others. Packets without a walk are
-// not listed, so the tracer never pulls them.
+// tiles). And it lists, per pixel, what the tracer does with it: a walk (a
+// guided pixel outside the refresh tile that is not certified) -- at the
+// front of the walk list when it is expected to be long (its own reprojected
+// point, else the farthest around it, lies more than kGuideLong cells beyond
+// its start: a depth edge, where the start comes from the near side), at the
+// back otherwise -- or a commit of a certified pixel (its colour word and
+// point wait in cert_col / cert_xyz: the block cannot write them into the
+// plane, which other blocks read as their halo). Each warp appends the
+// pixels of one ray packet (pw x ph) of the block, so consecutive list
+// entries stay spatial neighbours.
 __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams* __restrict__ P, TargetBuffers B) {
-    __shared__ float dist[kGuideBH + 2][kGuideBW + 2];
-    __shared__ uint8_t hole[kGuideBH + 2][kGuideBW + 2];  // a pixel of the frame without a point
+    constexpr int kHW = kGuideBW + 2, kHH = kGuideBH + 2;
+    __shared__ float dist[kHH][kHW];
+    __shared__ uint8_t hole[kHH][kHW];  // a pixel of the frame without a point
+    __shared__ CertCand cand[kHH][kHW];
+    __shared__ uint8_t kind[kGuideBH][kGuideBW];  // 0 none, 1 long walk, 2 walk, 3 certified
     __shared__ uint32_t touched;
-    __shared__ uint32_t long_packets;  // bit k: packet k of this block holds a long walk
-    __shared__ uint32_t walk_packets;  // bit k: packet k of this block holds a walk
     const int res_x = B.res_x, res_y = B.res_y;
     const int x0 = blockIdx.x * kGuideBW, y0 = blockIdx.y * kGuideBH;
     const float cx = P->ray.px, cy = P->ray.py, cz = P->ray.pz;
     const uint32_t* __restrict__ col = plane_col(B, P->cur);
     const float4* __restrict__ xyz = plane_xyz(B, P->cur);
-    if (threadIdx.x == 0) {
-        touched = 0;
-        long_packets = 0;
-        walk_packets = 0;
-    }
-    for (int i = threadIdx.x; i < (kGuideBW + 2) * (kGuideBH + 2); i += kGuideBW * kGuideBH) {
-        const int wx = i % (kGuideBW + 2), wy = i / (kGuideBW + 2);
+    const bool certify = P->certify != 0;
+    if (threadIdx.x == 0) touched = 0;
+    for (int i = threadIdx.x; i < kHW * kHH; i += kGuideBW * kGuideBH) {
+        const int wx = i % kHW, wy = i / kHW;
         const int gx = x0 + wx - 1, gy = y0 + wy - 1;
         float d = INFINITY;
         uint8_t h = 0;
+        CertCand cc;
+        cc.c = kEmptyPixel;
+        cc.q = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
         if (gx >= 0 && gx < res_x && gy >= 0 && gy < res_y) {
             const size_t o = (size_t)gy * res_x + gx;
             const uint32_t c = __ldg(col + o);  // both loads in flight together
             const float4 q = __ldg(xyz + o);
             // exact IEEE operations, so the CPU oracle finds the same start distances
             const float ax = __fsub_rn(q.x, cx), ay = __fsub_rn(q.y, cy), az = __fsub_rn(q.z, cz);
-            if (c != kEmptyPixel)
+            if (c != kEmptyPixel) {
                 d = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(ax, ax), __fmul_rn(ay, ay)), __fmul_rn(az, az)));
-            else
+                cc.c = c;
+                cc.q = q;
+            } else {
                 h = 1;
+            }
         }
         dist[wy][wx] = d;
         hole[wy][wx] = h;
+        cand[wy][wx] = cc;
     }
     __syncthreads();
     const int tx = threadIdx.x % kGuideBW, ty = threadIdx.x / kGuideBW;
     const int x = x0 + tx, y = y0 + ty;
+    uint8_t k_of = 0;
     if (x < res_x && y < res_y) {
         float m = INFINITY, far = 0.0f;
         int holes = 0;
@@ -487,57 +601,57 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
                 holes += hole[ty + j][tx + i];
             }
         const float own = dist[ty + 1][tx + 1];
+        const size_t ofs = (size_t)y * res_x + x;
         float g = -1.0f;
         if (m < INFINITY) {
             const float s = __fmul_rn(m, 16.0f);  // raypos units
-            float sw = (float)(2 * res_x);
-            int lod = 1;
-            while (s > sw && lod < 24) {  // the walk's lodswitch doublings
-                sw *= 2.0f;
-                ++lod;
-            }
+            const int lod = lod_at(s, res_x);
             const float cell = (float)(1 << lod);
             g = holes >= kGuideHoleCount ? __fmul_rn(s, kGuideNearHole)
                                          : fmaxf(__fsub_rn(s, __fmul_rn(kGuideMargin, cell)), 0.0f);
-            const float ahead = (own < INFINITY ? own : far) * 16.0f - g;
-            const int ps = P->pw_shift, pw = 1 << ps, ph = 32 >> ps;
-            const uint32_t bit = 1u << ((tx >> ps) + (ty / ph) * (kGuideBW / pw));
             const bool in_tile = x >= P->add_x && x < P->x_end && y >= P->add_y && y < P->y_end;
-            if (!in_tile) {  // the refresh tile traces its pixels from the camera
-                atomicOr(&walk_packets, bit);
-                if (ahead > kGuideLong * cell) atomicOr(&long_packets, bit);
+            uint32_t cc = 0;
+            float4 cq;
+            if (certify && holes == 0 && !in_tile &&
+                certify_pixel(P->ray, res_x, res_y, x, y, &cand[ty][tx], kHW, s, cc, cq)) {
+                g = kGuideCertified;
+                B.cert_col[ofs] = cc;
+                B.cert_xyz[ofs] = cq;
+                B.bgrx[ofs] = colorize(cc);
+                k_of = 3;
+            } else if (!in_tile) {  // the refresh tile traces its pixels from the camera
+                const float ahead = (own < INFINITY ? own : far) * 16.0f - g;
+                k_of = ahead > kGuideLong * cell ? 1 : 2;
             }
         } else {
             const int ntx = x / kNetOutW - x0 / kNetOutW, nty = y / kNetOutH - y0 / kNetOutH;
             atomicOr(&touched, 1u << (ntx + 2 * nty));
         }
-        B.guide[(size_t)y * res_x + x] = g;
+        B.guide[ofs] = g;
     }
+    kind[ty][tx] = k_of;
     __syncthreads();
-    if (threadIdx.x < 32) {  // the block's eight walk packets, appended by lanes 0-7 of warp 0
-        const int k = (int)threadIdx.x;
+    {  // warp w appends the pixels of packet w of the block, in packet order
+        const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
         const int ps = P->pw_shift, pw = 1 << ps, ph = 32 >> ps;
         const int per_row = kGuideBW / pw;
-        const int px = x0 / pw + k % per_row, py = y0 / ph + k / per_row;
-        const int wpx = (res_x + pw - 1) / pw, wpy = (res_y + ph - 1) / ph;
-        const bool walk = k < 8 && px < wpx && py < wpy && ((walk_packets >> k) & 1u);
-        const bool lng = walk && ((long_packets >> k) & 1u);
-        const uint32_t bl = __ballot_sync(0xffffffffu, lng), bs = __ballot_sync(0xffffffffu, walk && !lng);
-        uint32_t base_l = 0, base_s = 0;
-        if (k == 0) {
-            if (bl) base_l = atomicAdd(B.counters + 4, (uint32_t)__popc(bl));
-            if (bs) base_s = atomicAdd(B.counters + 5, (uint32_t)__popc(bs));
-        }
-        base_l = __shfl_sync(0xffffffffu, base_l, 0);
-        base_s = __shfl_sync(0xffffffffu, base_s, 0);
-        const uint32_t below = (1u << k) - 1u;
-        const uint32_t id = (uint32_t)py * (uint32_t)wpx + (uint32_t)px;
-        if (lng) {
-            const uint32_t at = base_l + (uint32_t)__popc(bl & below);
-            if (at < B.walk_cap) B.walk_list[at] = id;
-        } else if (walk) {
-            const uint32_t at = base_s + (uint32_t)__popc(bs & below);
-            if (at < B.walk_cap) B.walk_list[B.walk_cap - 1u - at] = id;
+        const int bx = (w % per_row) * pw + (lane & (pw - 1)), by = (w / per_row) * ph + (lane >> ps);
+        const int k = kind[by][bx];
+        const uint32_t xy = (uint32_t)(x0 + bx) | ((uint32_t)(y0 + by) << 16);
+        const uint32_t below = (1u << lane) - 1u;
+#pragma unroll
+        for (int kk = 1; kk <= 3; ++kk) {
+            const uint32_t bal = __ballot_sync(0xffffffffu, k == kk);
+            if (!bal) continue;
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(B.counters + (kk == 1 ? 4 : (kk == 2 ? 5 : 6)), (uint32_t)__popc(bal));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            const uint32_t at = base + (uint32_t)__popc(bal & below);
+            if (k == kk && at < B.walk_cap) {
+                if (kk == 1) B.walk_list[at] = xy;
+                else if (kk == 2) B.walk_list[B.walk_cap - 1u - at] = xy;
+                else B.cert_list[at] = xy;
+            }
         }
     }
     if (threadIdx.x < 4 && ((touched >> threadIdx.x) & 1u)) {
@@ -790,12 +904,14 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_infer(NetInferArgs A) {
                             const uint32_t ri = (uint32_t)__float2int_rn(fminf(fmaxf(r, 0.0f), 1.0f) * 255.0f);
                             const uint32_t gi = (uint32_t)__float2int_rn(fminf(fmaxf(gg, 0.0f), 1.0f) * 255.0f);
                             const uint32_t bi = (uint32_t)__float2int_rn(fminf(fmaxf(b, 0.0f), 1.0f) * 255.0f);
-                            A.B.bgrx[ofs] = bi + (gi << 8) + (ri << 16);
-                            // guided pixels are walked, never requested; with no cache
-                            // (the first frames) every pixel is traced: pixels the net
-                            // fills are not cached, so they would stay unguided
-                            req = !sP.have_cache ||
-                                  (!(z >= A.logit_threshold) && !(list && __ldg(A.B.guide + ofs) >= 0.0f));
+                            // In guided frames the net decides the unguided pixels only
+                            // (guide -1): the others are walked or certified and k_guide
+                            // has written the certified pixels' colour already. With no
+                            // cache (the first frames) every pixel is traced: pixels the
+                            // net fills are not cached, so they would stay unguided.
+                            const bool mine = !list || __ldg(A.B.guide + ofs) == -1.0f;
+                            if (mine) A.B.bgrx[ofs] = bi + (gi << 8) + (ri << 16);
+                            req = !sP.have_cache || (!(z >= A.logit_threshold) && mine);
                         }
                         const uint32_t bal = __ballot_sync(0xffffffffu, req);
                         if (list) {

@@ -61,6 +61,7 @@ struct RayResult {
     float hx, hy, hz;  // raypos/16 (kernel.cl:920)
     float dist;        // distance/16
     uint64_t voxel;    // packed hit cell (bit 63 = hit)
+    float code;        // hit code: level | signs << 5 (a float holding an integer), -1 without a hit
 };
 
 // Node word fetch: the staged prefix from shared memory, the rest through the
@@ -437,6 +438,7 @@ __device__ __forceinline__ RayResult trace_ray(const Octree& o, const RayCam& c,
     r.hz = __fmul_rn(rpz, 0.0625f);
     r.dist = __fmul_rn(w.distance, 0.0625f);
     r.voxel = 0;
+    r.code = w.hit ? (float)(rek | (int)(sxyz << 5)) : -1.0f;
     if (kVoxel && w.hit) {
         const uint32_t cells = (uint32_t)kScaleMax >> rek;
         uint32_t cx = (uint32_t)w.hcx, cy = (uint32_t)w.hcy, cz = (uint32_t)w.hcz;

@@ -51,7 +51,7 @@ EXPORTS = [
     "svo_net_forward", "svo_net_infer", "svo_net_backward", "svo_net_adam", "svo_target_set_cache_mode",
     "svo_target_set_coarse_refresh", "svo_octree_build", "svo_octree_info", "svo_octree_download",
     "svo_context_autotune", "svo_target_set_guided", "svo_read_guide", "svo_context_autotune_learned",
-    "svo_measure_read_bandwidth",
+    "svo_measure_read_bandwidth", "svo_target_set_certified",
 ]
 
 NET_PARAMS = 6388
@@ -125,6 +125,7 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "svo_context_destroy": (i, [_P]),
         "svo_last_error": (ctypes.c_char_p, [_P]),
         "svo_context_stream": (_P, [_P]),
+        "svo_target_set_certified": (i, [_P, i]),
         "svo_synchronize": (i, [_P]),
         "svo_measure_read_bandwidth": (i, [_P, _P, ctypes.c_size_t, i, ctypes.POINTER(ctypes.c_double)]),
         "svo_launch_count": (ctypes.c_uint64, [_P]),
@@ -546,8 +547,14 @@ class Target:
         walked from just in front of it; only the others go to the net."""
         _check(self._lib.svo_target_set_guided(self._h, 1 if enable else 0), self.ctx)
 
+    def set_certified(self, enable: bool = True) -> None:
+        """Certified reprojection in guided learned frames (on by default):
+        pixels whose ray provably meets a cached point's face skip the walk."""
+        _check(self._lib.svo_target_set_certified(self._h, 1 if enable else 0), self.ctx)
+
     def guide(self) -> np.ndarray:
-        """Start distances of the last guided frame (raypos units; -1 unguided)."""
+        """Start distances of the last guided frame (raypos units; -1 unguided,
+        -2 certified)."""
         out = np.empty(self.n, np.float32)
         _check(self._lib.svo_read_guide(self._h, _ptr(out)), self.ctx)
         return out

@@ -122,7 +122,7 @@ def test_guided_frames_fullsize_match_oracle(svo, orc, big, gpu_ctx):
         t = gpu_ctx.target(W, H)
         t.set_guided(True)
         t.use_graph(True)
-        og = orc.Guided(DEPTH, W, H)
+        og = orc.Guided(DEPTH, W, H, certify=True)
         for f in range(6):
             v = svo.camera_path(kind, DEPTH, 28 + f, W, H)
             gpu_ctx.warp_frame_learned(t, v, f, net, 0.999999)

@@ -74,3 +74,37 @@ def test_oracle_guided_frames_across_camera_wraps(svo, orc, scene):
             assert (g.colour() == full).mean() > 0.98, f
         prev = p
     assert wraps >= 2
+
+
+def test_oracle_certified_frames(svo, orc, scene):
+    # Certified reprojection in the oracle's guided frames: a pixel whose ray
+    # meets the face a cached hit lies on takes that point's colour without a
+    # walk. Such pixels are marked -2; their displayed colour is nearly always
+    # the full raycast's, and the frame stays as close to it as without them.
+    depth, W, H = 10, 240, 128
+    octree = scene(depth, 2024, True)
+    on = orc.Guided(depth, W, H, certify=True)
+    off = orc.Guided(depth, W, H)
+    share, wrong = [], []
+    for f in range(12):
+        v = svo.camera_path(1, depth, f, W, H)
+        on.frame(octree.words, octree.root, v.pos_array, v.m_array, f)
+        off.frame(octree.words, octree.root, v.pos_array, v.m_array, f)
+        full, _, _, _ = orc.raycast_full(depth, octree.words, octree.root, v.pos_array, v.m_array, W, H)
+        gd = on.guide()
+        c = gd == -2.0
+        if f < 2:
+            assert not c.any()
+            continue
+        share.append(c.mean())
+        a, b = orc.colorize(on.colour()), orc.colorize(full)
+        wrong.append((a[c] != b[c]).mean() if c.any() else 0.0)
+        # certified pixels carry their hit code: level in the low 5 bits
+        codes = on.coords()[c, 3]
+        assert np.all(codes >= 1) and np.all(codes == np.floor(codes))
+        # walked pixels are the same with and without certification (same cache)
+        if f == 2:
+            w = gd >= 0
+            assert np.array_equal(on.colour()[w], off.colour()[w])
+    assert np.mean(share) > 0.1, np.mean(share)
+    assert np.mean(wrong) < 0.02, np.mean(wrong)
