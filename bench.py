@@ -777,14 +777,14 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
         # 56x24 net tiles holding an unguided pixel (the tiles k_guide lists)
         tw, th = -(-W // 56), -(-H // 24)
         pad = np.zeros((th * 24, tw * 56), bool)
-        pad[:H, :W] = (g < 0).reshape(H, W)
+        pad[:H, :W] = (g == -1.0).reshape(H, W)
         return int(pad.reshape(th, 24, tw, 56).any(axis=(1, 3)).sum())
 
     def quality(render, t, kind, frames, traced_of, walked=False, sample=4):
         """Frames 0..frames-1 of camera path `kind`, each against the full
         raycast of its camera; the ray fractions on every `sample`-th frame."""
         err = ErrorSum(torch, ext)
-        traced, walk, tiles = [], [], []
+        traced, walk, cert, tiles = [], [], [], []
         for f in range(frames):
             v = view(f, kind)
             render(f, v)
@@ -795,11 +795,13 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                 if walked:
                     g = t.guide()
                     walk.append(float((g >= 0).mean()))
+                    cert.append(float((g == -2.0).mean()))
                     tiles.append(net_tiles(g))
         ctx.synchronize()
         out = {**err.result(), "window": f"frames 0-{frames - 1}", "traced_fraction": float(np.mean(traced))}
         if walked:
             out["walked_fraction"] = float(np.mean(walk))
+            out["certified_fraction"] = float(np.mean(cert))
             out["net_tiles"] = float(np.mean(tiles))
         return out
 

@@ -764,23 +764,15 @@ int orc_raycast_guided_steps(int depth, const uint32_t* words, size_t n_words, u
 // the meeting point lie inside the cell's face with a margin of s/64, the
 // level of detail at the meeting distance is L a thirty-second either side,
 // and that distance is at most 2 cells behind the nearest reprojected point of
-// the 3x3 neighbourhood (nothing cached lies in front). Of the passing
-// candidates of the 3x3 neighbourhood the nearest (smallest t, the first in
-// row order on a tie) is taken: colour byte, meeting point, code. Every
-// operation is one IEEE binary32 operation, as on the GPU.
+// the 3x3 neighbourhood (nothing cached lies in front). The candidates are
+// the pixel's own cached point and its four neighbours'; the nearest passing
+// one (smallest t, the first in row order on a tie) is taken: colour byte,
+// meeting point, code. t = (plane - camera) * (1 / d), the reciprocal taken
+// once per pixel and axis. Every operation is one IEEE binary32 operation, as
+// on the GPU.
 constexpr float kGuideCertified = -2.0f;
 
 inline float hit_code(const Ray& r) { return r.level < 0 ? -1.0f : (float)(r.level | (int)(r.signs << 5)); }
-
-inline int lod_at(float s, int res_x) {
-    float sw = (float)(2 * res_x);
-    int lod = 1;
-    while (s > sw && lod < 24) {
-        sw *= 2.0f;
-        ++lod;
-    }
-    return lod;
-}
 
 struct Certified {
     uint32_t colour;
@@ -794,64 +786,72 @@ bool certify(const View& v, int res_x, int res_y, int x, int y, const uint32_t* 
     d1[1] = (float)((double)(y - res_y / 2) + 0.5) * 1.0f / (float)res_y;
     d1[2] = 1.0f;
     const float d[3] = {dot3(d1, v.mx), dot3(d1, v.my), dot3(d1, v.mz)};
+    const float rd[3] = {1.0f / d[0], 1.0f / d[1], 1.0f / d[2]};
     const float cam[3] = {v.pos[0] * 16.0f, v.pos[1] * 16.0f, v.pos[2] * 16.0f};
     const float dlen = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
     const uint32_t signs = (d[0] < 0.0f ? 1u : 0u) | (d[1] < 0.0f ? 2u : 0u) | (d[2] < 0.0f ? 4u : 0u);
+    const float sw1 = (float)(2 * res_x);
+    auto pow2 = [](int e) {
+        const uint32_t bits = (uint32_t)(127 + e) << 23;
+        float f;
+        std::memcpy(&f, &bits, 4);
+        return f;
+    };
     float best = INFINITY;
     bool found = false;
-    for (int j = -1; j <= 1; ++j)
-        for (int i = -1; i <= 1; ++i) {
-            const int xi = x + i, yj = y + j;
-            if (xi < 0 || xi >= res_x || yj < 0 || yj >= res_y) continue;
-            const size_t o = (size_t)yj * res_x + xi;
-            if (col[o] == kEmpty) continue;
-            const float code = xyz[o * 4 + 3];
-            if (!(code >= 0.0f)) continue;
-            const int ic = (int)code;
-            const int L = ic & 31;
-            const uint32_t sb = (uint32_t)ic >> 5;
-            uint32_t sbits = (uint32_t)(127 + L) << 23, ibits = (uint32_t)(127 - L) << 23;
-            float cs, inv;
-            std::memcpy(&cs, &sbits, 4);
-            std::memcpy(&inv, &ibits, 4);
-            float p[3], f[3];
-            int axis = -1, on = 0;
-            for (int a = 0; a < 3; ++a) {
-                p[a] = xyz[o * 4 + a] * 16.0f;
-                f[a] = std::floor(p[a] * inv);
-                if (f[a] * cs == p[a]) {
-                    axis = a;
-                    ++on;
-                }
-            }
-            if (on != 1) continue;
-            const float da = d[axis];
-            if (((sb >> axis) & 1u) ? !(da < 0.0f) : !(da > 0.0f)) continue;
-            const float t = (p[axis] - cam[axis]) / da;
-            if (!(t > 0.0f)) continue;
-            float q[3];
-            bool inside = true;
-            for (int b = 0; b < 3; ++b) {
-                if (b == axis) {
-                    q[b] = p[b];
-                    continue;
-                }
-                q[b] = cam[b] + t * d[b];
-                const float r = (q[b] - f[b] * cs) * inv;
-                inside = inside && r > 0.015625f && r < 0.984375f;
-            }
-            if (!inside) continue;
-            const float dist = t * dlen;
-            if (lod_at(dist * 0.96875f, res_x) != L || lod_at(dist * 1.03125f, res_x) != L) continue;
-            if (!(dist - near_s <= 2.0f * cs)) continue;
-            if (t < best) {
-                best = t;
-                found = true;
-                out.colour = 0xff000000u | (col[o] & 255u);
-                for (int a = 0; a < 3; ++a) out.xyzw[a] = q[a] * 0.0625f;
-                out.xyzw[3] = (float)(L | (int)(signs << 5));
+    // the pixel's own point and its four neighbours', in row order
+    static const int kOff[5][2] = {{0, -1}, {-1, 0}, {0, 0}, {1, 0}, {0, 1}};
+    for (int k = 0; k < 5; ++k) {
+        const int xi = x + kOff[k][0], yj = y + kOff[k][1];
+        if (xi < 0 || xi >= res_x || yj < 0 || yj >= res_y) continue;
+        const size_t o = (size_t)yj * res_x + xi;
+        if (col[o] == kEmpty) continue;
+        const float code = xyz[o * 4 + 3];
+        if (!(code >= 0.0f)) continue;
+        const int ic = (int)code;
+        const int L = ic & 31;
+        if (L > 23) continue;
+        const uint32_t sb = (uint32_t)ic >> 5;
+        const float cs = pow2(L), inv = pow2(-L);
+        float p[3], f[3];
+        int axis = -1, on = 0;
+        for (int a = 0; a < 3; ++a) {
+            p[a] = xyz[o * 4 + a] * 16.0f;
+            f[a] = std::floor(p[a] * inv);
+            if (f[a] * cs == p[a]) {
+                axis = a;
+                ++on;
             }
         }
+        if (on != 1) continue;
+        const float da = d[axis];
+        if (((sb >> axis) & 1u) ? !(da < 0.0f) : !(da > 0.0f)) continue;
+        const float t = (p[axis] - cam[axis]) * rd[axis];
+        if (!(t > 0.0f) || !(t < best)) continue;
+        const float dist = t * dlen;
+        if (!(dist - near_s <= 2.0f * cs)) continue;
+        // the walk's level of detail at dist, a thirty-second either side, is L
+        const float lo = dist * 0.96875f, hi = dist * 1.03125f;
+        if (!(hi <= sw1 * pow2(L - 1))) continue;
+        if (L > 1 && !(lo > sw1 * pow2(L - 2))) continue;
+        float q[3];
+        bool inside = true;
+        for (int b2 = 0; b2 < 3; ++b2) {
+            if (b2 == axis) {
+                q[b2] = p[b2];
+                continue;
+            }
+            q[b2] = cam[b2] + t * d[b2];
+            const float r = (q[b2] - f[b2] * cs) * inv;
+            inside = inside && r > 0.015625f && r < 0.984375f;
+        }
+        if (!inside) continue;
+        best = t;
+        found = true;
+        out.colour = 0xff000000u | (col[o] & 255u);
+        for (int a = 0; a < 3; ++a) out.xyzw[a] = q[a] * 0.0625f;
+        out.xyzw[3] = (float)(L | (int)(signs << 5));
+    }
     return found;
 }
 

@@ -427,7 +427,7 @@ constexpr float kGuideLong = 64.0f;         // cells between the start and the p
 constexpr int kGuideBW = 32, kGuideBH = 8;  // pixels per block (whole ray packets of every packet shape)
 
 // Certified reprojection: a guided pixel needs no walk when its own ray
-// provably meets a face a cached hit point of its 3x3 neighbourhood lies on.
+// provably meets a face a cached hit point of its neighbourhood lies on.
 // Every cached point carries its hit code in w (level L of the hit cell, edge
 // s = 2^L raypos units, and the signs of the ray that found it); the point
 // lies on the cell's entry face, the one plane of its three coordinates that
@@ -438,10 +438,12 @@ constexpr int kGuideBW = 32, kGuideBH = 8;  // pixels per block (whole ray packe
 // inside the face with a margin of s/64, the level of detail at the meeting
 // distance is L a thirty-second either side of it, and that distance is at
 // most kCertifyGap cells behind the 3x3 minimum distance (nothing cached lies
-// in front). The nearest passing candidate (smallest t; the first in row order
+// in front). The candidates are the cached points of the pixel and of its
+// four neighbours. The nearest passing candidate (smallest t; the first in row order
 // on a tie) gives the pixel's colour word (0xff000000 | colour byte), point
 // and code. Only pixels outside the refresh tile with no hole in their 3x3
-// are certified. An exact face test alone certified 40% of the orbit's
+// are certified. The meeting parameter is t = (plane - camera) * (1 / d),
+// the reciprocal taken once per pixel and axis. An exact face test alone certified 40% of the orbit's
 // pixels, 3.4% of them wrongly (a surface the cache missed in front of the
 // face); with the gap test 24-26% on both camera paths, 0.3-0.4% wrongly
 // (oracle experiments at 960x512). Every operation is one IEEE binary32
@@ -459,34 +461,43 @@ __device__ __forceinline__ int lod_at(float s, int res_x) {
     return lod;
 }
 
-struct CertCand {
-    float4 q;    // cached point (world units) and hit code
-    uint32_t c;  // colour word, kEmptyPixel for none
+// Candidate data of the halo, one array per field (conflict-free reads).
+struct CertHalo {
+    float x[kGuideBH + 2][kGuideBW + 2], y[kGuideBH + 2][kGuideBW + 2], z[kGuideBH + 2][kGuideBW + 2];
+    float code[kGuideBH + 2][kGuideBW + 2];  // hit code, -1: none
+    uint32_t col[kGuideBH + 2][kGuideBW + 2];
 };
 
+// The candidates are the pixel's own cached point and its four neighbours'
+// (the four diagonal neighbours added 3% of the certified pixels for 80% more
+// work in an oracle experiment); hx, hy = the pixel's halo position.
 __device__ __forceinline__ bool certify_pixel(const RayCam& cam, int res_x, int res_y, int x, int y,
-                                              const CertCand* cand, int stride, float near_s, uint32_t& out_col,
+                                              const CertHalo& h, int hx, int hy, float near_s, uint32_t& out_col,
                                               float4& out_q) {
     const float d1x = __fdiv_rn(__fmul_rn(__fadd_rn((float)(x - (res_x >> 1)), 0.5f), cam.fovx), (float)res_y);
     const float d1y = __fdiv_rn(__fmul_rn(__fadd_rn((float)(y - (res_y >> 1)), 0.5f), cam.fovy), (float)res_y);
     const float d[3] = {__fadd_rn(__fadd_rn(__fmul_rn(d1x, cam.mxx), __fmul_rn(d1y, cam.mxy)), cam.mxz),
                         __fadd_rn(__fadd_rn(__fmul_rn(d1x, cam.myx), __fmul_rn(d1y, cam.myy)), cam.myz),
                         __fadd_rn(__fadd_rn(__fmul_rn(d1x, cam.mzx), __fmul_rn(d1y, cam.mzy)), cam.mzz)};
+    const float rd[3] = {__fdiv_rn(1.0f, d[0]), __fdiv_rn(1.0f, d[1]), __fdiv_rn(1.0f, d[2])};
     const float c16[3] = {__fmul_rn(cam.px, 16.0f), __fmul_rn(cam.py, 16.0f), __fmul_rn(cam.pz, 16.0f)};
     const float dlen =
         __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(d[0], d[0]), __fmul_rn(d[1], d[1])), __fmul_rn(d[2], d[2])));
     const uint32_t signs = (d[0] < 0.0f ? 1u : 0u) | (d[1] < 0.0f ? 2u : 0u) | (d[2] < 0.0f ? 4u : 0u);
+    const float sw1 = (float)(2 * res_x);  // the level-of-detail distance of level 1
     float best = INFINITY;
     bool found = false;
 #pragma unroll 1
-    for (int k = 0; k < 9; ++k) {
-        const CertCand cc = cand[(k / 3) * stride + (k % 3)];
-        if (cc.c == kEmptyPixel || !(cc.q.w >= 0.0f)) continue;
-        const int ic = (int)cc.q.w;
+    for (int k = 0; k < 5; ++k) {  // up, left, own, right, down (row order)
+        const int cy = hy + (k == 0 ? -1 : (k == 4 ? 1 : 0)), cx = hx + (k == 1 ? -1 : (k == 3 ? 1 : 0));
+        const float code = h.code[cy][cx];
+        if (!(code >= 0.0f)) continue;  // no point, or no hit
+        const int ic = (int)code;
         const int L = ic & 31;
+        if (L > 23) continue;
         const uint32_t sb = (uint32_t)ic >> 5;
         const float cs = __int_as_float((127 + L) << 23), inv = __int_as_float((127 - L) << 23);
-        const float p[3] = {__fmul_rn(cc.q.x, 16.0f), __fmul_rn(cc.q.y, 16.0f), __fmul_rn(cc.q.z, 16.0f)};
+        const float p[3] = {__fmul_rn(h.x[cy][cx], 16.0f), __fmul_rn(h.y[cy][cx], 16.0f), __fmul_rn(h.z[cy][cx], 16.0f)};
         float f[3];
         int axis = -1, on = 0;
 #pragma unroll
@@ -499,11 +510,20 @@ __device__ __forceinline__ bool certify_pixel(const RayCam& cam, int res_x, int 
         }
         if (on != 1) continue;
         const float da = axis == 0 ? d[0] : (axis == 1 ? d[1] : d[2]);
+        if (((sb >> axis) & 1u) ? !(da < 0.0f) : !(da > 0.0f)) continue;
         const float pa = axis == 0 ? p[0] : (axis == 1 ? p[1] : p[2]);
         const float ca = axis == 0 ? c16[0] : (axis == 1 ? c16[1] : c16[2]);
-        if (((sb >> axis) & 1u) ? !(da < 0.0f) : !(da > 0.0f)) continue;
-        const float t = __fdiv_rn(__fsub_rn(pa, ca), da);
-        if (!(t > 0.0f)) continue;
+        const float ra = axis == 0 ? rd[0] : (axis == 1 ? rd[1] : rd[2]);
+        const float t = __fmul_rn(__fsub_rn(pa, ca), ra);
+        if (!(t > 0.0f) || !(t < best)) continue;
+        const float dist = __fmul_rn(t, dlen);
+        if (!(__fsub_rn(dist, near_s) <= __fmul_rn(kCertifyGap, cs))) continue;
+        // level of detail L a thirty-second either side: the walk's lodswitch
+        // doublings put dist*(1-1/32) above and dist*(1+1/32) at most at the
+        // switch distances of levels L-1 and L (exact powers of two of sw1)
+        const float lo = __fmul_rn(dist, 0.96875f), hi = __fmul_rn(dist, 1.03125f);
+        if (!(hi <= __fmul_rn(sw1, __int_as_float((126 + L) << 23)))) continue;
+        if (L > 1 && !(lo > __fmul_rn(sw1, __int_as_float((125 + L) << 23)))) continue;
         float q[3];
         bool inside = true;
 #pragma unroll
@@ -517,16 +537,11 @@ __device__ __forceinline__ bool certify_pixel(const RayCam& cam, int res_x, int 
             inside = inside && r > 0.015625f && r < 0.984375f;
         }
         if (!inside) continue;
-        const float dist = __fmul_rn(t, dlen);
-        if (lod_at(__fmul_rn(dist, 0.96875f), res_x) != L || lod_at(__fmul_rn(dist, 1.03125f), res_x) != L) continue;
-        if (!(__fsub_rn(dist, near_s) <= __fmul_rn(kCertifyGap, cs))) continue;
-        if (t < best) {
-            best = t;
-            found = true;
-            out_col = 0xff000000u | (cc.c & 255u);
-            out_q = make_float4(__fmul_rn(q[0], 0.0625f), __fmul_rn(q[1], 0.0625f), __fmul_rn(q[2], 0.0625f),
-                                (float)(L | (int)(signs << 5)));
-        }
+        best = t;
+        found = true;
+        out_col = 0xff000000u | (h.col[cy][cx] & 255u);
+        out_q = make_float4(__fmul_rn(q[0], 0.0625f), __fmul_rn(q[1], 0.0625f), __fmul_rn(q[2], 0.0625f),
+                            (float)(L | (int)(signs << 5)));
     }
     return found;
 }
@@ -548,7 +563,7 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
     constexpr int kHW = kGuideBW + 2, kHH = kGuideBH + 2;
     __shared__ float dist[kHH][kHW];
     __shared__ uint8_t hole[kHH][kHW];  // a pixel of the frame without a point
-    __shared__ CertCand cand[kHH][kHW];
+    __shared__ CertHalo cand;
     __shared__ uint8_t kind[kGuideBH][kGuideBW];  // 0 none, 1 long walk, 2 walk, 3 certified
     __shared__ uint32_t touched;
     const int res_x = B.res_x, res_y = B.res_y;
@@ -563,9 +578,8 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
         const int gx = x0 + wx - 1, gy = y0 + wy - 1;
         float d = INFINITY;
         uint8_t h = 0;
-        CertCand cc;
-        cc.c = kEmptyPixel;
-        cc.q = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+        uint32_t cc = kEmptyPixel;
+        float4 cq = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
         if (gx >= 0 && gx < res_x && gy >= 0 && gy < res_y) {
             const size_t o = (size_t)gy * res_x + gx;
             const uint32_t c = __ldg(col + o);  // both loads in flight together
@@ -574,15 +588,19 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
             const float ax = __fsub_rn(q.x, cx), ay = __fsub_rn(q.y, cy), az = __fsub_rn(q.z, cz);
             if (c != kEmptyPixel) {
                 d = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(ax, ax), __fmul_rn(ay, ay)), __fmul_rn(az, az)));
-                cc.c = c;
-                cc.q = q;
+                cc = c;
+                cq = q;
             } else {
                 h = 1;
             }
         }
         dist[wy][wx] = d;
         hole[wy][wx] = h;
-        cand[wy][wx] = cc;
+        cand.x[wy][wx] = cq.x;
+        cand.y[wy][wx] = cq.y;
+        cand.z[wy][wx] = cq.z;
+        cand.code[wy][wx] = cc == kEmptyPixel ? -1.0f : cq.w;
+        cand.col[wy][wx] = cc;
     }
     __syncthreads();
     const int tx = threadIdx.x % kGuideBW, ty = threadIdx.x / kGuideBW;
@@ -613,7 +631,7 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
             uint32_t cc = 0;
             float4 cq;
             if (certify && holes == 0 && !in_tile &&
-                certify_pixel(P->ray, res_x, res_y, x, y, &cand[ty][tx], kHW, s, cc, cq)) {
+                certify_pixel(P->ray, res_x, res_y, x, y, cand, tx + 1, ty + 1, s, cc, cq)) {
                 g = kGuideCertified;
                 B.cert_col[ofs] = cc;
                 B.cert_xyz[ofs] = cq;
