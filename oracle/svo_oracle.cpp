@@ -767,9 +767,10 @@ int orc_raycast_guided_steps(int depth, const uint32_t* words, size_t n_words, u
 // the 3x3 neighbourhood (nothing cached lies in front). The candidates are
 // the pixel's own cached point and its four neighbours'; the nearest passing
 // one (smallest t, the first in row order on a tie) is taken: colour byte,
-// meeting point, code. t = (plane - camera) * (1 / d), the reciprocal taken
-// once per pixel and axis. Every operation is one IEEE binary32 operation, as
-// on the GPU.
+// meeting point, code. The tests compare cross-multiplied quantities (with n
+// = |plane - camera| and A = |d along the face's axis|: t = n/A, the meeting
+// distance n*|d|/A compared squared); one division is left, for the winner's
+// point. Every operation is one IEEE binary32 operation, as on the GPU.
 constexpr float kGuideCertified = -2.0f;
 
 inline float hit_code(const Ray& r) { return r.level < 0 ? -1.0f : (float)(r.level | (int)(r.signs << 5)); }
@@ -786,10 +787,8 @@ bool certify(const View& v, int res_x, int res_y, int x, int y, const uint32_t* 
     d1[1] = (float)((double)(y - res_y / 2) + 0.5) * 1.0f / (float)res_y;
     d1[2] = 1.0f;
     const float d[3] = {dot3(d1, v.mx), dot3(d1, v.my), dot3(d1, v.mz)};
-    const float rd[3] = {1.0f / d[0], 1.0f / d[1], 1.0f / d[2]};
     const float cam[3] = {v.pos[0] * 16.0f, v.pos[1] * 16.0f, v.pos[2] * 16.0f};
-    const float dlen = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-    const uint32_t signs = (d[0] < 0.0f ? 1u : 0u) | (d[1] < 0.0f ? 2u : 0u) | (d[2] < 0.0f ? 4u : 0u);
+    const float dl2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
     const float sw1 = (float)(2 * res_x);
     auto pow2 = [](int e) {
         const uint32_t bits = (uint32_t)(127 + e) << 23;
@@ -797,8 +796,9 @@ bool certify(const View& v, int res_x, int res_y, int x, int y, const uint32_t* 
         std::memcpy(&f, &bits, 4);
         return f;
     };
-    float best = INFINITY;
-    bool found = false;
+    float bn = 1.0f, ba = 0.0f, bp = 0.0f;  // best t = bn / ba
+    int bk = -1, baxis = 0;
+    size_t bo = 0;
     // the pixel's own point and its four neighbours', in row order
     static const int kOff[5][2] = {{0, -1}, {-1, 0}, {0, 0}, {1, 0}, {0, 1}};
     for (int k = 0; k < 5; ++k) {
@@ -825,34 +825,45 @@ bool certify(const View& v, int res_x, int res_y, int x, int y, const uint32_t* 
         }
         if (on != 1) continue;
         const float da = d[axis];
-        if (((sb >> axis) & 1u) ? !(da < 0.0f) : !(da > 0.0f)) continue;
-        const float t = (p[axis] - cam[axis]) * rd[axis];
-        if (!(t > 0.0f) || !(t < best)) continue;
-        const float dist = t * dlen;
-        if (!(dist - near_s <= 2.0f * cs)) continue;
-        // the walk's level of detail at dist, a thirty-second either side, is L
-        const float lo = dist * 0.96875f, hi = dist * 1.03125f;
-        if (!(hi <= sw1 * pow2(L - 1))) continue;
-        if (L > 1 && !(lo > sw1 * pow2(L - 2))) continue;
-        float q[3];
+        const bool neg = ((sb >> axis) & 1u) != 0;
+        if (neg ? !(da < 0.0f) : !(da > 0.0f)) continue;
+        const float num = p[axis] - cam[axis];
+        const float n = neg ? -num : num, A = neg ? -da : da;  // t = n / A
+        if (!(n > 0.0f)) continue;
+        if (!(n * ba < bn * A)) continue;
+        // the meeting distance n*|d|/A: gap and level-of-detail tests squared
+        const float nd2 = (n * n) * dl2;
+        const float gap = (near_s + 2.0f * cs) * A;
+        if (!(nd2 <= gap * gap)) continue;
+        const float swl = (sw1 * pow2(L - 1)) * A;
+        if (!(nd2 * 1.0634765625f <= swl * swl)) continue;  // (1 + 1/32)^2
+        if (L > 1) {
+            const float swm = (sw1 * pow2(L - 2)) * A;
+            if (!(nd2 * 0.9384765625f > swm * swm)) continue;  // (1 - 1/32)^2
+        }
         bool inside = true;
         for (int b2 = 0; b2 < 3; ++b2) {
-            if (b2 == axis) {
-                q[b2] = p[b2];
-                continue;
-            }
-            q[b2] = cam[b2] + t * d[b2];
-            const float r = (q[b2] - f[b2] * cs) * inv;
-            inside = inside && r > 0.015625f && r < 0.984375f;
+            if (b2 == axis) continue;
+            const float u = (cam[b2] - f[b2] * cs) * A + n * d[b2];
+            const float sa = cs * A;
+            inside = inside && u > sa * 0.015625f && u < sa * 0.984375f;
         }
         if (!inside) continue;
-        best = t;
-        found = true;
-        out.colour = 0xff000000u | (col[o] & 255u);
-        for (int a = 0; a < 3; ++a) out.xyzw[a] = q[a] * 0.0625f;
-        out.xyzw[3] = (float)(L | (int)(signs << 5));
+        bn = n;
+        ba = A;
+        bk = k;
+        baxis = axis;
+        bp = p[axis];
+        bo = o;
     }
-    return found;
+    if (bk < 0) return false;
+    const int L = (int)xyz[bo * 4 + 3] & 31;
+    const float t = bn / ba;
+    const uint32_t signs = (d[0] < 0.0f ? 1u : 0u) | (d[1] < 0.0f ? 2u : 0u) | (d[2] < 0.0f ? 4u : 0u);
+    out.colour = 0xff000000u | (col[bo] & 255u);
+    for (int b2 = 0; b2 < 3; ++b2) out.xyzw[b2] = (b2 == baxis ? bp : cam[b2] + t * d[b2]) * 0.0625f;
+    out.xyzw[3] = (float)(L | (int)(signs << 5));
+    return true;
 }
 
 // Guided learned frames with every unguided pixel traced: the product's

@@ -438,12 +438,11 @@ constexpr int kGuideBW = 32, kGuideBH = 8;  // pixels per block (whole ray packe
 // inside the face with a margin of s/64, the level of detail at the meeting
 // distance is L a thirty-second either side of it, and that distance is at
 // most kCertifyGap cells behind the 3x3 minimum distance (nothing cached lies
-// in front). The candidates are the cached points of the pixel and of its
+// in front) -- each test cross-multiplied, see certify_pixel. The candidates are the cached points of the pixel and of its
 // four neighbours. The nearest passing candidate (smallest t; the first in row order
 // on a tie) gives the pixel's colour word (0xff000000 | colour byte), point
 // and code. Only pixels outside the refresh tile with no hole in their 3x3
-// are certified. The meeting parameter is t = (plane - camera) * (1 / d),
-// the reciprocal taken once per pixel and axis. An exact face test alone certified 40% of the orbit's
+// are certified. An exact face test alone certified 40% of the orbit's
 // pixels, 3.4% of them wrongly (a surface the cache missed in front of the
 // face); with the gap test 24-26% on both camera paths, 0.3-0.4% wrongly
 // (oracle experiments at 960x512). Every operation is one IEEE binary32
@@ -470,23 +469,23 @@ struct CertHalo {
 
 // The candidates are the pixel's own cached point and its four neighbours'
 // (the four diagonal neighbours added 3% of the certified pixels for 80% more
-// work in an oracle experiment); hx, hy = the pixel's halo position.
-__device__ __forceinline__ bool certify_pixel(const RayCam& cam, int res_x, int res_y, int x, int y,
-                                              const CertHalo& h, int hx, int hy, float near_s, uint32_t& out_col,
-                                              float4& out_q) {
-    const float d1x = __fdiv_rn(__fmul_rn(__fadd_rn((float)(x - (res_x >> 1)), 0.5f), cam.fovx), (float)res_y);
-    const float d1y = __fdiv_rn(__fmul_rn(__fadd_rn((float)(y - (res_y >> 1)), 0.5f), cam.fovy), (float)res_y);
+// work in an oracle experiment); hx, hy = the pixel's halo position. The tests
+// compare cross-multiplied quantities instead of dividing: with n = |plane -
+// camera| and A = |d along the face's axis| the meeting parameter is t = n/A,
+// the meeting distance n*|d|/A (compared squared), and one division is left,
+// for the winner's point. d1x, d1y: the ray kernels' per-column and per-row
+// direction terms.
+__device__ __forceinline__ bool certify_pixel(const RayCam& cam, int res_x, float d1x, float d1y, const CertHalo& h,
+                                              int hx, int hy, float near_s, uint32_t& out_col, float4& out_q) {
     const float d[3] = {__fadd_rn(__fadd_rn(__fmul_rn(d1x, cam.mxx), __fmul_rn(d1y, cam.mxy)), cam.mxz),
                         __fadd_rn(__fadd_rn(__fmul_rn(d1x, cam.myx), __fmul_rn(d1y, cam.myy)), cam.myz),
                         __fadd_rn(__fadd_rn(__fmul_rn(d1x, cam.mzx), __fmul_rn(d1y, cam.mzy)), cam.mzz)};
-    const float rd[3] = {__fdiv_rn(1.0f, d[0]), __fdiv_rn(1.0f, d[1]), __fdiv_rn(1.0f, d[2])};
     const float c16[3] = {__fmul_rn(cam.px, 16.0f), __fmul_rn(cam.py, 16.0f), __fmul_rn(cam.pz, 16.0f)};
-    const float dlen =
-        __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(d[0], d[0]), __fmul_rn(d[1], d[1])), __fmul_rn(d[2], d[2])));
-    const uint32_t signs = (d[0] < 0.0f ? 1u : 0u) | (d[1] < 0.0f ? 2u : 0u) | (d[2] < 0.0f ? 4u : 0u);
+    const float dl2 = __fadd_rn(__fadd_rn(__fmul_rn(d[0], d[0]), __fmul_rn(d[1], d[1])), __fmul_rn(d[2], d[2]));
     const float sw1 = (float)(2 * res_x);  // the level-of-detail distance of level 1
-    float best = INFINITY;
-    bool found = false;
+    float bn = 1.0f, ba = 0.0f;            // best t = bn / ba (none yet: infinite)
+    int bk = -1, baxis = 0;
+    float bp = 0.0f;
 #pragma unroll 1
     for (int k = 0; k < 5; ++k) {  // up, left, own, right, down (row order)
         const int cy = hy + (k == 0 ? -1 : (k == 4 ? 1 : 0)), cx = hx + (k == 1 ? -1 : (k == 3 ? 1 : 0));
@@ -510,40 +509,53 @@ __device__ __forceinline__ bool certify_pixel(const RayCam& cam, int res_x, int 
         }
         if (on != 1) continue;
         const float da = axis == 0 ? d[0] : (axis == 1 ? d[1] : d[2]);
-        if (((sb >> axis) & 1u) ? !(da < 0.0f) : !(da > 0.0f)) continue;
+        const bool neg = ((sb >> axis) & 1u) != 0;
+        if (neg ? !(da < 0.0f) : !(da > 0.0f)) continue;
         const float pa = axis == 0 ? p[0] : (axis == 1 ? p[1] : p[2]);
         const float ca = axis == 0 ? c16[0] : (axis == 1 ? c16[1] : c16[2]);
-        const float ra = axis == 0 ? rd[0] : (axis == 1 ? rd[1] : rd[2]);
-        const float t = __fmul_rn(__fsub_rn(pa, ca), ra);
-        if (!(t > 0.0f) || !(t < best)) continue;
-        const float dist = __fmul_rn(t, dlen);
-        if (!(__fsub_rn(dist, near_s) <= __fmul_rn(kCertifyGap, cs))) continue;
-        // level of detail L a thirty-second either side: the walk's lodswitch
-        // doublings put dist*(1-1/32) above and dist*(1+1/32) at most at the
-        // switch distances of levels L-1 and L (exact powers of two of sw1)
-        const float lo = __fmul_rn(dist, 0.96875f), hi = __fmul_rn(dist, 1.03125f);
-        if (!(hi <= __fmul_rn(sw1, __int_as_float((126 + L) << 23)))) continue;
-        if (L > 1 && !(lo > __fmul_rn(sw1, __int_as_float((125 + L) << 23)))) continue;
-        float q[3];
+        const float num = __fsub_rn(pa, ca);
+        const float n = neg ? -num : num, A = neg ? -da : da;  // t = n / A
+        if (!(n > 0.0f)) continue;
+        if (!(__fmul_rn(n, ba) < __fmul_rn(bn, A))) continue;  // not nearer than the best so far
+        // meeting distance n*|d|/A: gap and level-of-detail tests squared
+        const float nd2 = __fmul_rn(__fmul_rn(n, n), dl2);
+        const float gap = __fmul_rn(__fadd_rn(near_s, __fmul_rn(kCertifyGap, cs)), A);
+        if (!(nd2 <= __fmul_rn(gap, gap))) continue;
+        const float swl = __fmul_rn(__fmul_rn(sw1, __int_as_float((126 + L) << 23)), A);
+        if (!(__fmul_rn(nd2, 1.0634765625f) <= __fmul_rn(swl, swl))) continue;  // (1 + 1/32)^2
+        if (L > 1) {
+            const float swm = __fmul_rn(__fmul_rn(sw1, __int_as_float((125 + L) << 23)), A);
+            if (!(__fmul_rn(nd2, 0.9384765625f) > __fmul_rn(swm, swm))) continue;  // (1 - 1/32)^2
+        }
+        // the meeting point inside the face, s/64 from its edges: with
+        // u = (camera - cell corner) * A + n * d, A * s/64 < u < A * s * 63/64
         bool inside = true;
 #pragma unroll
         for (int b = 0; b < 3; ++b) {
-            if (b == axis) {
-                q[b] = p[b];
-                continue;
-            }
-            q[b] = __fadd_rn(c16[b], __fmul_rn(t, d[b]));
-            const float r = __fmul_rn(__fsub_rn(q[b], __fmul_rn(f[b], cs)), inv);
-            inside = inside && r > 0.015625f && r < 0.984375f;
+            if (b == axis) continue;
+            const float u = __fadd_rn(__fmul_rn(__fsub_rn(c16[b], __fmul_rn(f[b], cs)), A), __fmul_rn(n, d[b]));
+            const float sa = __fmul_rn(cs, A);
+            inside = inside && u > __fmul_rn(sa, 0.015625f) && u < __fmul_rn(sa, 0.984375f);
         }
         if (!inside) continue;
-        best = t;
-        found = true;
-        out_col = 0xff000000u | (h.col[cy][cx] & 255u);
-        out_q = make_float4(__fmul_rn(q[0], 0.0625f), __fmul_rn(q[1], 0.0625f), __fmul_rn(q[2], 0.0625f),
-                            (float)(L | (int)(signs << 5)));
+        bn = n;
+        ba = A;
+        bk = k;
+        baxis = axis;
+        bp = pa;
     }
-    return found;
+    if (bk < 0) return false;
+    const int cy = hy + (bk == 0 ? -1 : (bk == 4 ? 1 : 0)), cx = hx + (bk == 1 ? -1 : (bk == 3 ? 1 : 0));
+    const int L = (int)h.code[cy][cx] & 31;
+    const float t = __fdiv_rn(bn, ba);
+    float q[3];
+#pragma unroll
+    for (int b = 0; b < 3; ++b) q[b] = b == baxis ? bp : __fadd_rn(c16[b], __fmul_rn(t, d[b]));
+    const uint32_t signs = (d[0] < 0.0f ? 1u : 0u) | (d[1] < 0.0f ? 2u : 0u) | (d[2] < 0.0f ? 4u : 0u);
+    out_col = 0xff000000u | (h.col[cy][cx] & 255u);
+    out_q = make_float4(__fmul_rn(q[0], 0.0625f), __fmul_rn(q[1], 0.0625f), __fmul_rn(q[2], 0.0625f),
+                        (float)(L | (int)(signs << 5)));
+    return true;
 }
 
 // Also lists the net tiles (kNetOutW x kNetOutH) holding an unguided pixel:
@@ -564,6 +576,7 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
     __shared__ float dist[kHH][kHW];
     __shared__ uint8_t hole[kHH][kHW];  // a pixel of the frame without a point
     __shared__ CertHalo cand;
+    __shared__ float d1col[kGuideBW], d1row[kGuideBH];  // the ray kernels' direction terms
     __shared__ uint8_t kind[kGuideBH][kGuideBW];  // 0 none, 1 long walk, 2 walk, 3 certified
     __shared__ uint32_t touched;
     const int res_x = B.res_x, res_y = B.res_y;
@@ -573,6 +586,15 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
     const float4* __restrict__ xyz = plane_xyz(B, P->cur);
     const bool certify = P->certify != 0;
     if (threadIdx.x == 0) touched = 0;
+    if (threadIdx.x < kGuideBW + kGuideBH) {  // as trace_ray computes them
+        const bool c = threadIdx.x < kGuideBW;
+        const int v = c ? x0 + (int)threadIdx.x : y0 + (int)threadIdx.x - kGuideBW;
+        const int half = c ? (res_x >> 1) : (res_y >> 1);
+        const float t = __fdiv_rn(__fmul_rn(__fadd_rn((float)(v - half), 0.5f), c ? P->ray.fovx : P->ray.fovy),
+                                  (float)res_y);
+        if (c) d1col[threadIdx.x] = t;
+        else d1row[threadIdx.x - kGuideBW] = t;
+    }
     for (int i = threadIdx.x; i < kHW * kHH; i += kGuideBW * kGuideBH) {
         const int wx = i % kHW, wy = i / kHW;
         const int gx = x0 + wx - 1, gy = y0 + wy - 1;
@@ -631,7 +653,7 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
             uint32_t cc = 0;
             float4 cq;
             if (certify && holes == 0 && !in_tile &&
-                certify_pixel(P->ray, res_x, res_y, x, y, cand, tx + 1, ty + 1, s, cc, cq)) {
+                certify_pixel(P->ray, res_x, d1col[tx], d1row[ty], cand, tx + 1, ty + 1, s, cc, cq)) {
                 g = kGuideCertified;
                 B.cert_col[ofs] = cc;
                 B.cert_xyz[ofs] = cq;

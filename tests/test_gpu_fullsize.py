@@ -132,7 +132,7 @@ def test_guided_frames_fullsize_match_oracle(svo, orc, big, gpu_ctx):
             assert np.array_equal(g.view(np.uint32), og.guide().view(np.uint32)), (kind, f)
             assert np.array_equal(t.colour(2), og.colour()), (kind, f, int((t.colour(2) != og.colour()).sum()))
             assert np.array_equal(t.coords(0).view(np.uint32), og.coords().view(np.uint32)), (kind, f)
-        assert (g >= 0).mean() > 0.8
+        assert ((g >= 0) | (g == -2.0)).mean() > 0.8  # walked or certified
         t.close()
     net.close()
 
