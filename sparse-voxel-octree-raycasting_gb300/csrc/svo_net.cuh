@@ -460,12 +460,58 @@ __device__ __forceinline__ int lod_at(float s, int res_x) {
     return lod;
 }
 
-// Candidate data of the halo, one array per field (conflict-free reads).
+// Candidate data of the halo, one array per field (conflict-free reads): the
+// parts of the face test that do not depend on the pixel's ray, computed once
+// per cached point as the halo is loaded.
 struct CertHalo {
-    float x[kGuideBH + 2][kGuideBW + 2], y[kGuideBH + 2][kGuideBW + 2], z[kGuideBH + 2][kGuideBW + 2];
-    float code[kGuideBH + 2][kGuideBW + 2];  // hit code, -1: none
+    uint8_t face[kGuideBH + 2][kGuideBW + 2];  // bit 7: a candidate; bits 0-1 axis; bit 2 the old ray's sign
+    uint8_t level[kGuideBH + 2][kGuideBW + 2];
+    float plane[kGuideBH + 2][kGuideBW + 2];   // the face's coordinate on its axis (raypos units)
+    float lo1[kGuideBH + 2][kGuideBW + 2];     // the cell's low corner on the other two axes, in axis order
+    float lo2[kGuideBH + 2][kGuideBW + 2];
     uint32_t col[kGuideBH + 2][kGuideBW + 2];
 };
+
+// The entry face of a cached point with hit code `code` (see certify_pixel):
+// the one coordinate (raypos units) that is a multiple of the hit cell's
+// edge. Writes the halo entry (face byte 0: no candidate).
+__device__ __forceinline__ void cert_face(CertHalo& h, int wy, int wx, uint32_t c, float4 q) {
+    uint8_t face = 0, lv = 0;
+    float pl = 0.0f, l1 = 0.0f, l2 = 0.0f;
+    if (c != kEmptyPixel && q.w >= 0.0f) {
+        const int ic = (int)q.w;
+        const int L = ic & 31;
+        const uint32_t sb = (uint32_t)ic >> 5;
+        if (L <= 23) {
+            const float cs = __int_as_float((127 + L) << 23), inv = __int_as_float((127 - L) << 23);
+            const float p[3] = {__fmul_rn(q.x, 16.0f), __fmul_rn(q.y, 16.0f), __fmul_rn(q.z, 16.0f)};
+            float f[3];
+            int axis = -1, on = 0;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                f[a] = floorf(__fmul_rn(p[a], inv));
+                if (__fmul_rn(f[a], cs) == p[a]) {
+                    axis = a;
+                    ++on;
+                }
+            }
+            if (on == 1) {
+                face = (uint8_t)(0x80u | (uint32_t)axis | (((sb >> axis) & 1u) << 2));
+                lv = (uint8_t)L;
+                pl = axis == 0 ? p[0] : (axis == 1 ? p[1] : p[2]);
+                const int b1 = axis == 0 ? 1 : 0, b2 = axis == 2 ? 1 : 2;
+                l1 = __fmul_rn(b1 == 0 ? f[0] : f[1], cs);
+                l2 = __fmul_rn(b2 == 1 ? f[1] : f[2], cs);
+            }
+        }
+    }
+    h.face[wy][wx] = face;
+    h.level[wy][wx] = lv;
+    h.plane[wy][wx] = pl;
+    h.lo1[wy][wx] = l1;
+    h.lo2[wy][wx] = l2;
+    h.col[wy][wx] = c;
+}
 
 // The candidates are the pixel's own cached point and its four neighbours'
 // (the four diagonal neighbours added 3% of the certified pixels for 80% more
@@ -484,39 +530,23 @@ __device__ __forceinline__ bool certify_pixel(const RayCam& cam, int res_x, floa
     const float dl2 = __fadd_rn(__fadd_rn(__fmul_rn(d[0], d[0]), __fmul_rn(d[1], d[1])), __fmul_rn(d[2], d[2]));
     const float sw1 = (float)(2 * res_x);  // the level-of-detail distance of level 1
     float bn = 1.0f, ba = 0.0f;            // best t = bn / ba (none yet: infinite)
-    int bk = -1, baxis = 0;
-    float bp = 0.0f;
+    int bk = -1;
 #pragma unroll 1
     for (int k = 0; k < 5; ++k) {  // up, left, own, right, down (row order)
         const int cy = hy + (k == 0 ? -1 : (k == 4 ? 1 : 0)), cx = hx + (k == 1 ? -1 : (k == 3 ? 1 : 0));
-        const float code = h.code[cy][cx];
-        if (!(code >= 0.0f)) continue;  // no point, or no hit
-        const int ic = (int)code;
-        const int L = ic & 31;
-        if (L > 23) continue;
-        const uint32_t sb = (uint32_t)ic >> 5;
-        const float cs = __int_as_float((127 + L) << 23), inv = __int_as_float((127 - L) << 23);
-        const float p[3] = {__fmul_rn(h.x[cy][cx], 16.0f), __fmul_rn(h.y[cy][cx], 16.0f), __fmul_rn(h.z[cy][cx], 16.0f)};
-        float f[3];
-        int axis = -1, on = 0;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            f[a] = floorf(__fmul_rn(p[a], inv));
-            if (__fmul_rn(f[a], cs) == p[a]) {
-                axis = a;
-                ++on;
-            }
-        }
-        if (on != 1) continue;
+        const uint32_t face = h.face[cy][cx];
+        if (!(face & 0x80u)) continue;
+        const int axis = (int)(face & 3u);
+        const bool neg = (face & 4u) != 0;
         const float da = axis == 0 ? d[0] : (axis == 1 ? d[1] : d[2]);
-        const bool neg = ((sb >> axis) & 1u) != 0;
         if (neg ? !(da < 0.0f) : !(da > 0.0f)) continue;
-        const float pa = axis == 0 ? p[0] : (axis == 1 ? p[1] : p[2]);
         const float ca = axis == 0 ? c16[0] : (axis == 1 ? c16[1] : c16[2]);
-        const float num = __fsub_rn(pa, ca);
+        const float num = __fsub_rn(h.plane[cy][cx], ca);
         const float n = neg ? -num : num, A = neg ? -da : da;  // t = n / A
         if (!(n > 0.0f)) continue;
         if (!(__fmul_rn(n, ba) < __fmul_rn(bn, A))) continue;  // not nearer than the best so far
+        const int L = h.level[cy][cx];
+        const float cs = __int_as_float((127 + L) << 23);
         // meeting distance n*|d|/A: gap and level-of-detail tests squared
         const float nd2 = __fmul_rn(__fmul_rn(n, n), dl2);
         const float gap = __fmul_rn(__fadd_rn(near_s, __fmul_rn(kCertifyGap, cs)), A);
@@ -529,28 +559,27 @@ __device__ __forceinline__ bool certify_pixel(const RayCam& cam, int res_x, floa
         }
         // the meeting point inside the face, s/64 from its edges: with
         // u = (camera - cell corner) * A + n * d, A * s/64 < u < A * s * 63/64
-        bool inside = true;
-#pragma unroll
-        for (int b = 0; b < 3; ++b) {
-            if (b == axis) continue;
-            const float u = __fadd_rn(__fmul_rn(__fsub_rn(c16[b], __fmul_rn(f[b], cs)), A), __fmul_rn(n, d[b]));
-            const float sa = __fmul_rn(cs, A);
-            inside = inside && u > __fmul_rn(sa, 0.015625f) && u < __fmul_rn(sa, 0.984375f);
-        }
-        if (!inside) continue;
+        const int b1 = axis == 0 ? 1 : 0, b2 = axis == 2 ? 1 : 2;
+        const float sa = __fmul_rn(cs, A);
+        const float smin = __fmul_rn(sa, 0.015625f), smax = __fmul_rn(sa, 0.984375f);
+        const float u1 = __fadd_rn(__fmul_rn(__fsub_rn(b1 == 0 ? c16[0] : c16[1], h.lo1[cy][cx]), A),
+                                   __fmul_rn(n, b1 == 0 ? d[0] : d[1]));
+        if (!(u1 > smin && u1 < smax)) continue;
+        const float u2 = __fadd_rn(__fmul_rn(__fsub_rn(b2 == 1 ? c16[1] : c16[2], h.lo2[cy][cx]), A),
+                                   __fmul_rn(n, b2 == 1 ? d[1] : d[2]));
+        if (!(u2 > smin && u2 < smax)) continue;
         bn = n;
         ba = A;
         bk = k;
-        baxis = axis;
-        bp = pa;
     }
     if (bk < 0) return false;
     const int cy = hy + (bk == 0 ? -1 : (bk == 4 ? 1 : 0)), cx = hx + (bk == 1 ? -1 : (bk == 3 ? 1 : 0));
-    const int L = (int)h.code[cy][cx] & 31;
+    const int L = h.level[cy][cx];
+    const int baxis = (int)(h.face[cy][cx] & 3u);
     const float t = __fdiv_rn(bn, ba);
     float q[3];
 #pragma unroll
-    for (int b = 0; b < 3; ++b) q[b] = b == baxis ? bp : __fadd_rn(c16[b], __fmul_rn(t, d[b]));
+    for (int b = 0; b < 3; ++b) q[b] = b == baxis ? h.plane[cy][cx] : __fadd_rn(c16[b], __fmul_rn(t, d[b]));
     const uint32_t signs = (d[0] < 0.0f ? 1u : 0u) | (d[1] < 0.0f ? 2u : 0u) | (d[2] < 0.0f ? 4u : 0u);
     out_col = 0xff000000u | (h.col[cy][cx] & 255u);
     out_q = make_float4(__fmul_rn(q[0], 0.0625f), __fmul_rn(q[1], 0.0625f), __fmul_rn(q[2], 0.0625f),
@@ -619,11 +648,7 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
         }
         dist[wy][wx] = d;
         hole[wy][wx] = h;
-        cand.x[wy][wx] = cq.x;
-        cand.y[wy][wx] = cq.y;
-        cand.z[wy][wx] = cq.z;
-        cand.code[wy][wx] = cc == kEmptyPixel ? -1.0f : cq.w;
-        cand.col[wy][wx] = cc;
+        if (certify) cert_face(cand, wy, wx, cc, cq);
     }
     __syncthreads();
     const int tx = threadIdx.x % kGuideBW, ty = threadIdx.x / kGuideBW;
