@@ -82,6 +82,8 @@ def parse_args(argv=None):
     ap.add_argument("--autotune", type=int, default=1, help="pick the trace configuration by measurement first")
     ap.add_argument("--guided", type=int, default=1,
                     help="learned frames walk pixels with a cached surface nearby from just in front of it")
+    ap.add_argument("--certify", type=int, default=1,
+                    help="guided learned frames certify reprojected pixels whose ray meets a cached face")
     ap.add_argument("--orbit-window", type=int, default=256, help="orbit frames in the quality window")
     ap.add_argument("--fast-window", type=int, default=512, help="fast-motion frames in the quality window")
     ap.add_argument("--extras", type=int, default=1,
@@ -390,6 +392,7 @@ def measure_large(svo, torch, args, device, frames=16, views=8):
         t = cx.target(W, H)
         t.use_graph(True)
         t.set_guided(bool(args.guided))
+        t.set_certified(bool(args.certify))
         net = svo.Net(cx)
         net.load_file(args.weights)
         ctxs.append(cx)
@@ -623,6 +626,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     thr = args.threshold
     tgt_l, full = ctx.target(W, H), ctx.target(W, H)
     tgt_l.set_guided(bool(args.guided))
+    tgt_l.set_certified(bool(args.certify))
     if args.graph:
         tgt_l.use_graph(True)
     ext = torch.cuda.ExternalStream(ctx.stream, device=device)
@@ -640,6 +644,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     if args.autotune:
         tt = ctx.target(W, H)
         tt.set_guided(bool(args.guided))
+        tt.set_certified(bool(args.certify))
         tt.use_graph(bool(args.graph))
         tune_l = ctx.autotune_learned(tt, [view(f) for f in range(16)], net, thr)
         tt.close()
@@ -655,6 +660,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
             t.use_graph(True)
         if guided is not None:
             t.set_guided(guided)
+        t.set_certified(bool(args.certify))
         return t
 
     def plain(t):
@@ -871,6 +877,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
             c.upload_device(d_words.data_ptr(), octree.words.size, octree.root, octree.depth)
             t = c.target(W, H)
             t.set_guided(bool(args.guided))
+            t.set_certified(bool(args.certify))
             n = svo.Net(c)
             n.load_file(args.weights)
             if args.graph:
@@ -957,6 +964,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
             # distances the GPU used (read back after the frame)
             tg = ctx.target(W, H)
             tg.set_guided(True)
+            tg.set_certified(bool(args.certify))
             for f in range(args.warmup + args.steps):
                 ctx.warp_frame_learned(tg, view(f), f, net, thr)
             g = tg.guide()
