@@ -82,7 +82,7 @@ def parse_args(argv=None):
     ap.add_argument("--autotune", type=int, default=1, help="pick the trace configuration by measurement first")
     ap.add_argument("--guided", type=int, default=1,
                     help="learned frames walk pixels with a cached surface nearby from just in front of it")
-    ap.add_argument("--certify", type=int, default=1,
+    ap.add_argument("--certify", type=int, default=0,
                     help="guided learned frames certify reprojected pixels whose ray meets a cached face")
     ap.add_argument("--orbit-window", type=int, default=256, help="orbit frames in the quality window")
     ap.add_argument("--fast-window", type=int, default=512, help="fast-motion frames in the quality window")

@@ -306,7 +306,8 @@ svo_status svo_target_set_guided(svo_target* t, int enable);
 /* The start distances of the last guided frame, res_x*res_y floats in raypos
  * units (16 per world unit; 0 = from the camera, -1 = unguided). */
 /* Certified reprojection in guided learned frames (no reference counterpart;
- * on by default): a guided pixel whose own ray provably meets the face a
+ * off by default -- on a GB300 at 1920x1024 it saves 6% of the trace and
+ * costs as much in the start-distance kernel): a guided pixel whose own ray provably meets the face a
  * cached hit point of its 3x3 neighbourhood lies on -- the hit codes the
  * learned frames keep in w of the coordinate planes (level | ray signs << 5,
  * -1 without a hit) name the face -- takes that point's colour and needs no

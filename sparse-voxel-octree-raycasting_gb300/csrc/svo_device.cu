@@ -105,7 +105,7 @@ struct svo_target {
     uint32_t* req_offs = nullptr;  // learned frames: request offsets per 8x4 packet
     // guided learned frames (walks from the cached depth); buffers in B
     bool guided = false;
-    bool certify = true;  // certified reprojection in guided learned frames
+    bool certify = false;  // certified reprojection in guided learned frames
     float* d_guide = nullptr;
     // camera position each physical plane's points were written under (the
     // rebase of learned frames across wraps of the periodic volume)

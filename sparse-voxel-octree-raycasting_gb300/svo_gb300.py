@@ -548,7 +548,7 @@ class Target:
         _check(self._lib.svo_target_set_guided(self._h, 1 if enable else 0), self.ctx)
 
     def set_certified(self, enable: bool = True) -> None:
-        """Certified reprojection in guided learned frames (on by default):
+        """Certified reprojection in guided learned frames (off by default):
         pixels whose ray provably meets a cached point's face skip the walk."""
         _check(self._lib.svo_target_set_certified(self._h, 1 if enable else 0), self.ctx)
 

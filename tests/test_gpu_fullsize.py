@@ -121,6 +121,7 @@ def test_guided_frames_fullsize_match_oracle(svo, orc, big, gpu_ctx):
     for kind in (1, 2):
         t = gpu_ctx.target(W, H)
         t.set_guided(True)
+        t.set_certified(True)
         t.use_graph(True)
         og = orc.Guided(DEPTH, W, H, certify=True)
         for f in range(6):

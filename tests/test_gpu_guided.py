@@ -121,6 +121,7 @@ def test_certified_pixels_match_full_raycast(svo, scene, gpu_ctx):
     net.load_file(_weights(svo))
     t, full = gpu_ctx.target(W, H), gpu_ctx.target(W, H)
     t.set_guided(True)
+    t.set_certified(True)
     share, wrong = [], []
     for kind in (1, 2):
         for f in range(16):
