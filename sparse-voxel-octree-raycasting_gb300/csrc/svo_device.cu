@@ -1311,7 +1311,7 @@ svo_status svo_target_create(svo_context* ctx, int res_x, int res_y, svo_target*
     A((void**)&t->d_guide, N * 4);
     // guided frames' pixel lists (walks, certified pixels) and certified results
     t->B.walk_cap = (uint32_t)N;
-    A((void**)&t->B.walk_list, N * 4);
+    A((void**)&t->B.walk_list, N * 4 * kWalkBuckets);
     A((void**)&t->B.cert_list, N * 4);
     A((void**)&t->B.cert_col, N * 4);
     A((void**)&t->B.cert_xyz, N * 16);

@@ -25,6 +25,8 @@
 namespace svo {
 
 constexpr uint64_t kKeyEmpty = ~0ull;
+constexpr int kWalkBuckets = 4;  // guided walks listed by expected length (k_guide)
+static_assert(kWalkBuckets == 4, "k_trace_warp selects among four walk lists");
 constexpr int kMaxBatchViews = 256;
 
 // Everything one warp frame needs, written to device memory by k_set_params
@@ -71,10 +73,11 @@ struct TargetBuffers {
     // list of those tiles (count in counters[3]). guide == nullptr: no walks.
     float* guide;
     // Pixel lists k_guide writes (entries x | y << 16, walk_cap = res_x*res_y
-    // each): the walks expected to be long from the front of walk_list
-    // (counters[4] of them), the others from its back (counters[5]); the
-    // certified pixels in cert_list (counters[6]), whose colour word and
-    // point k_guide leaves in cert_col / cert_xyz for the tracer to commit.
+    // each): the walks in kWalkBuckets lists by expected length, longest
+    // first (walk_list + b * walk_cap, counters[4 + b] entries); the
+    // certified pixels in cert_list (counters[4 + kWalkBuckets]), whose
+    // colour word and point k_guide leaves in cert_col / cert_xyz for the
+    // tracer to commit.
     uint32_t* walk_list;
     uint32_t walk_cap;
     uint32_t* cert_list;
@@ -83,8 +86,8 @@ struct TargetBuffers {
     uint32_t* net_flags;
     uint32_t* net_list;
     uint32_t* counters;   // [0] trace work counter, [1] hole entries, [2] coarse-pass work counter,
-                          // [3] net tiles listed, [4] long walks listed, [5] other walks listed,
-                          // [6] certified pixels listed
+                          // [3] net tiles listed, [4..4+kWalkBuckets) walks listed per bucket,
+                          // [4+kWalkBuckets] certified pixels listed
     int res_x, res_y;
     int tiles_x, tiles_y;  // whole 16x16 tiles (res/16)
 };
@@ -120,7 +123,7 @@ __device__ __forceinline__ float4* plane_xyz(const TargetBuffers& B, int i) {
 __global__ void k_set_params(FrameParams p, FrameParams* dst, uint32_t* counters) {
     *dst = p;
 #pragma unroll
-    for (int i = 0; i < 7; ++i) counters[i] = 0;
+    for (int i = 0; i < 5 + kWalkBuckets; ++i) counters[i] = 0;
 }
 
 __global__ void k_reset_counter(uint32_t* counter) { *counter = 0; }
@@ -456,11 +459,17 @@ __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FramePa
     const uint32_t rpx = (uint32_t)max(0, (xe - ax + pw - 1) / pw), rpy = (uint32_t)max(0, (ye - ay + ph - 1) / ph);
     const uint32_t fixed = hole_packets + rpx * rpy;
     const float* __restrict__ guide = kBgrx ? B.guide : nullptr;
-    const uint32_t n_long = guide ? min(B.counters[4], B.walk_cap) : 0u;
-    const uint32_t n_short = guide ? min(B.counters[5], B.walk_cap - n_long) : 0u;
-    const uint32_t n_cert = guide ? min(B.counters[6], B.walk_cap) : 0u;
-    const uint32_t p_long = (n_long + 31u) / 32u, p_short = (n_short + 31u) / 32u, p_cert = (n_cert + 31u) / 32u;
-    const uint32_t total = fixed + p_long + p_short + p_cert;
+    uint32_t n_walk[kWalkBuckets], p_walk[kWalkBuckets];
+    uint32_t walk_packets = 0;
+#pragma unroll
+    for (int b = 0; b < kWalkBuckets; ++b) {
+        n_walk[b] = guide ? min(B.counters[4 + b], B.walk_cap) : 0u;
+        p_walk[b] = (n_walk[b] + 31u) / 32u;
+        walk_packets += p_walk[b];
+    }
+    const uint32_t n_cert = guide ? min(B.counters[4 + kWalkBuckets], B.walk_cap) : 0u;
+    const uint32_t p_cert = (n_cert + 31u) / 32u;
+    const uint32_t total = fixed + walk_packets + p_cert;
     const RayCam cam = P->ray;
     float4* __restrict__ xyz = plane_xyz(B, P->cur);
     uint32_t* __restrict__ col = plane_col(B, P->cur);
@@ -474,16 +483,30 @@ __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FramePa
         float s0 = 0.0f;
         if (kBgrx && p >= fixed) {
             uint32_t k = p - fixed;
-            uint32_t e;
-            if (k < p_long) {
-                e = k * 32u + (uint32_t)lane;
-                valid = e < n_long;
-            } else if ((k -= p_long) < p_short) {
-                e = k * 32u + (uint32_t)lane;
-                valid = e < n_short;
-                e = B.walk_cap - 1u - e;
+            if (k < walk_packets) {  // the bucket of packet k, longest walks first
+                int b = 0;
+#pragma unroll
+                for (int i = 0; i < kWalkBuckets - 1; ++i)
+                    if (b == i && k >= p_walk[i]) {
+                        k -= p_walk[i];
+                        b = i + 1;
+                    }
+                const uint32_t e = k * 32u + (uint32_t)lane;
+                const uint32_t nb = b == 0 ? n_walk[0] : (b == 1 ? n_walk[1] : (b == 2 ? n_walk[2] : n_walk[3]));
+                valid = e < nb;
+                const uint32_t xy = valid ? __ldg(B.walk_list + (size_t)b * B.walk_cap + e) : 0u;
+                x = (int)(xy & 0xffffu);
+                y = (int)(xy >> 16);
+                if (valid && (x >= res_x || y >= res_y)) {
+                    fault |= kFaultHoleEntry;
+                    valid = false;
+                }
+                if (valid) {
+                    s0 = __ldg(guide + (size_t)y * res_x + x);
+                    valid = s0 >= 0.0f;
+                }
             } else {  // certified pixels: commit the colour word and point k_guide left
-                e = (k - p_short) * 32u + (uint32_t)lane;
+                const uint32_t e = (k - walk_packets) * 32u + (uint32_t)lane;
                 if (e < n_cert) {
                     const uint32_t xy = __ldg(B.cert_list + e);
                     const size_t ofs = (size_t)(xy >> 16) * res_x + (xy & 0xffffu);
@@ -495,17 +518,6 @@ __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FramePa
                     }
                 }
                 continue;
-            }
-            const uint32_t xy = valid ? __ldg(B.walk_list + e) : 0u;
-            x = (int)(xy & 0xffffu);
-            y = (int)(xy >> 16);
-            if (valid && (x >= res_x || y >= res_y)) {
-                fault |= kFaultHoleEntry;
-                valid = false;
-            }
-            if (valid) {
-                s0 = __ldg(guide + (size_t)y * res_x + x);
-                valid = s0 >= 0.0f;
             }
         } else if (p < hole_packets) {
             const uint32_t e = p * 32u + (uint32_t)lane;

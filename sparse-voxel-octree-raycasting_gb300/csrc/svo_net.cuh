@@ -423,7 +423,14 @@ static_assert(kNetPer == kNetLayers, "one slice of the next tile's input per lay
 constexpr float kGuideMargin = 4.0f;        // cells of the start distance's level of detail
 constexpr float kGuideNearHole = 0.5f;      // start distance factor at the edge of a hole region
 constexpr int kGuideHoleCount = 3;          // holes in the 3x3 that make a hole region
-constexpr float kGuideLong = 64.0f;         // cells between the start and the pixel's own point: a long walk
+// Walk buckets by the cells between the start and the pixel's own point: a
+// depth edge (> kGuideLong, the start taken from the near side; such walks
+// cost 4.4x the others in an oracle experiment), then > kGuideMid, >
+// kGuideShort and the rest; the tracer runs the buckets in that order, so
+// walks of similar length share warps.
+constexpr float kGuideLong = 64.0f;
+constexpr float kGuideMid = 16.0f;
+constexpr float kGuideShort = 6.0f;
 constexpr int kGuideBW = 32, kGuideBH = 8;  // pixels per block (whole ray packets of every packet shape)
 
 // Certified reprojection: a guided pixel needs no walk when its own ray
@@ -591,11 +598,8 @@ __device__ __forceinline__ bool certify_pixel(const RayCam& cam, int res_x, floa
 // the first block to find one in a tile stamps the tile with this frame's
 // serial and appends it (a block of 32 x 8 pixels touches at most 2 x 2
 // tiles). And it lists, per pixel, what the tracer does with it: a walk (a
-// guided pixel outside the refresh tile that is not certified) -- at the
-// front of the walk list when it is expected to be long (its own reprojected
-// point, else the farthest around it, lies more than kGuideLong cells beyond
-// its start: a depth edge, where the start comes from the near side), at the
-// back otherwise -- or a commit of a certified pixel (its colour word and
+// guided pixel outside the refresh tile that is not certified), in the walk
+// list of its length bucket -- or a commit of a certified pixel (its colour word and
 // point wait in cert_col / cert_xyz: the block cannot write them into the
 // plane, which other blocks read as their halo). Each warp appends the
 // pixels of one ray packet (pw x ph) of the block, so consecutive list
@@ -606,8 +610,9 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
     __shared__ uint8_t hole[kHH][kHW];  // a pixel of the frame without a point
     __shared__ CertHalo cand;
     __shared__ float d1col[kGuideBW], d1row[kGuideBH];  // the ray kernels' direction terms
-    __shared__ uint8_t kind[kGuideBH][kGuideBW];  // 0 none, 1 long walk, 2 walk, 3 certified
-    __shared__ uint32_t list_cnt[3][kGuideBH];     // per list and warp: count, then list position
+    // 0 none, 1..kWalkBuckets a walk (bucket 1: the longest expected), kWalkBuckets+1 certified
+    __shared__ uint8_t kind[kGuideBH][kGuideBW];
+    __shared__ uint32_t list_cnt[kWalkBuckets + 1][kGuideBH];  // per list and warp: count, then position
     __shared__ uint32_t touched;
     const int res_x = B.res_x, res_y = B.res_y;
     const int x0 = blockIdx.x * kGuideBW, y0 = blockIdx.y * kGuideBH;
@@ -684,10 +689,11 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
                 B.cert_col[ofs] = cc;
                 B.cert_xyz[ofs] = cq;
                 B.bgrx[ofs] = colorize(cc);
-                k_of = 3;
+                k_of = kWalkBuckets + 1;
             } else if (!in_tile) {  // the refresh tile traces its pixels from the camera
-                const float ahead = (own < INFINITY ? own : far) * 16.0f - g;
-                k_of = ahead > kGuideLong * cell ? 1 : 2;
+                // cells between the start and the pixel's own point (else the farthest around)
+                const float ahead = __fdividef((own < INFINITY ? own : far) * 16.0f - g, cell);
+                k_of = ahead > kGuideLong ? 1 : (ahead > kGuideMid ? 2 : (ahead > kGuideShort ? 3 : 4));
             }
         } else {
             const int ntx = x / kNetOutW - x0 / kNetOutW, nty = y / kNetOutH - y0 / kNetOutH;
@@ -706,14 +712,15 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
         const int k = kind[by][bx];
         const uint32_t xy = (uint32_t)(x0 + bx) | ((uint32_t)(y0 + by) << 16);
         const uint32_t below = (1u << lane) - 1u;
-        uint32_t bal[3];
+        uint32_t mine = 0;  // the ballot of this lane's list
 #pragma unroll
-        for (int kk = 0; kk < 3; ++kk) {
-            bal[kk] = __ballot_sync(0xffffffffu, k == kk + 1);
-            if (lane == 0) list_cnt[kk][w] = (uint32_t)__popc(bal[kk]);
+        for (int kk = 0; kk <= kWalkBuckets; ++kk) {
+            const uint32_t bal = __ballot_sync(0xffffffffu, k == kk + 1);
+            if (k == kk + 1) mine = bal;
+            if (lane == 0) list_cnt[kk][w] = (uint32_t)__popc(bal);
         }
         __syncthreads();
-        if (threadIdx.x < 3) {
+        if (threadIdx.x <= kWalkBuckets) {
             const int kk = (int)threadIdx.x;
             uint32_t total = 0;
             for (int i = 0; i < kGuideBH; ++i) total += list_cnt[kk][i];
@@ -726,10 +733,9 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
         }
         __syncthreads();
         if (k > 0) {
-            const uint32_t at = list_cnt[k - 1][w] + (uint32_t)__popc(bal[k - 1] & below);
+            const uint32_t at = list_cnt[k - 1][w] + (uint32_t)__popc(mine & below);
             if (at < B.walk_cap) {
-                if (k == 1) B.walk_list[at] = xy;
-                else if (k == 2) B.walk_list[B.walk_cap - 1u - at] = xy;
+                if (k <= kWalkBuckets) B.walk_list[(size_t)(k - 1) * B.walk_cap + at] = xy;
                 else B.cert_list[at] = xy;
             }
         }
