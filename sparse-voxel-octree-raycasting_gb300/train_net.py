@@ -3,8 +3,9 @@ itself generates, then evaluates it on a held-out camera path.
 
 Every training step renders one learned warp frame (its input features are
 taken through the target's feature tap), the full raycast of the same view
-(the target colour), and runs the net's FP32 forward, loss, backward and one
-Adam step on the GPU (svo_net_backward / svo_net_adam). The camera alternates,
+(the target colour), and runs the net's forward, loss, backward and one Adam
+step on the GPU (svo_net_backward / svo_net_adam: every convolution on the
+tensor cores). The camera alternates,
 in stretches of --segment frames, between the orbit (0.5 deg/frame) and the
 fast-motion path (2 deg/frame yaw plus 0.05 x extent/frame translation).
 
