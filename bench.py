@@ -35,7 +35,7 @@ oracle port of kernel.cl/raycast.h), with all host threads, on scenes and
 cameras from oracle/scene_gen.py: that process never loads the product library.
 
 --profile-case NAME runs one small fixed workload for a profiler capture and
-exits (learned, guided, plain, full, build, config1).
+exits (learned, guided, plain, full, build, config1, train).
 
 Multi-GPU: replicas only (the per-frame pipeline does not shard); each rank
 renders its own camera path on its own GPU, scaling "weak".
@@ -62,7 +62,7 @@ WORKLOAD = ("warped + learned pipeline 1920x1024 (guided walks from the reprojec
             "unguided pixels), depth-11 terrain octree, 256-frame orbit (0.5 deg/frame), confidence threshold 0.5")
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 TRACE_PROFILE = "profiles/k_trace_warp_guided_1920x1024_depth11.md"
-PROFILE_CASES = ("learned", "guided", "plain", "full", "build", "config1")
+PROFILE_CASES = ("learned", "guided", "plain", "full", "build", "config1", "train")
 
 
 def parse_args(argv=None):
@@ -556,11 +556,30 @@ def run_profile_case(case: str) -> None:
     0.5, orbit) without / with guided walks; plain: 8 plain warp frames;
     full: 4 full raycasts; build: 2 GPU octree builds of the benchmark
     terrain's voxels (all 1920x1024, depth-11 benchmark terrain); config1: 4
-    full raycasts of the 512x512 depth-9 solid-terrain configuration."""
+    full raycasts of the 512x512 depth-9 solid-terrain configuration; train:
+    3 training steps of the net at 1920x1024 on seeded features."""
     sys.path.insert(0, PKG)
     import svo_gb300 as svo
 
     W, H, DEPTH, SEED = 1920, 1024, 11, 2024
+    if case == "train":
+        import torch
+
+        ctx = svo.Context(0)
+        net = svo.Net(ctx)
+        net.load_file(os.path.join(PKG, "net_weights.npy"))
+        g = torch.Generator(device="cuda").manual_seed(7)
+        feat = torch.rand((8, H, W), generator=g, device="cuda")
+        tgt = torch.randint(0, 1 << 24, (H * W,), generator=g, device="cuda", dtype=torch.int32)
+        torch.cuda.synchronize()
+        for _ in range(3):
+            net.backward(feat.data_ptr(), tgt.data_ptr(), W, H, 0.015, 0.1, read_loss=False)
+            net.adam(1e-5)
+        ctx.synchronize()
+        print("ok")
+        net.close()
+        ctx.close()
+        return
     if case in ("build", "config1"):
         import torch
 
