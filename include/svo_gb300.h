@@ -374,8 +374,10 @@ svo_status svo_net_adam(svo_net* net, float lr, float beta1, float beta2, float 
  * with SVO_ERR_INVALID_ARGUMENT before any CUDA call.
  * The first call in a CUDA context (normally the device's primary context;
  * a context the host made current through the driver API counts as its own)
- * looks up that array's device address in it; make the first call before any
- * stream capture. Every call shares the array (it keeps the last call's
+ * looks up that array's device address in it. The call is synchronous (it
+ * waits for its rays and reads the fault word back), so it cannot be
+ * captured into a graph: during an active capture of `stream` it returns
+ * SVO_ERR_INVALID_ARGUMENT. Every call shares the array (it keeps the last call's
  * contents; the counter and fault flags are cleared at the start of each
  * call), so calls that overlap on the GPU -- from two host threads or on two
  * streams at once -- race; issue them one after another.

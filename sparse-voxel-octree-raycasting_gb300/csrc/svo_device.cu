@@ -2090,12 +2090,17 @@ extern "C" svo_status svo_raycast_full_noalloc(const uint32_t* d_words, size_t n
         packets_total += (uint64_t)((v.res_x + 7) / 8) * (uint64_t)((v.res_y + 3) / 4);
     }
     if (packets_total > kMaxBatchPackets) return SVO_ERR_INVALID_ARGUMENT;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // The call synchronises and reads the fault word back, which no graph can
+    // hold: refuse it while the stream is being captured.
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &capture) != cudaSuccess || capture != cudaStreamCaptureStatusNone)
+        return SVO_ERR_INVALID_ARGUMENT;
     int device = 0;
     if (cudaGetDevice(&device) != cudaSuccess) return SVO_ERR_CUDA;
     unsigned char* scratch = nullptr;
     svo_status st = scratch_address(device, &scratch);
     if (st != SVO_OK) return st;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
 
     // View table, built on the host stack and copied into the scratch array.
     struct alignas(16) Table {

@@ -87,6 +87,22 @@ def test_noalloc_full_raycast_matches_regular_path(svo):
                                       octree.depth, ctypes.cast(varr, ctypes.c_void_p),
                                       ctypes.cast(oarr, ctypes.c_void_p), n, None)
     assert rc == 7  # SVO_ERR_CAPACITY
+
+    # the call synchronises, so it is refused (before any launch) while its
+    # stream is being captured; the capture itself stays valid
+    side = torch.cuda.Stream(device)
+    x = torch.zeros(16, device=device)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(side):
+        with torch.cuda.graph(graph, stream=side):
+            x.add_(1.0)
+            rc = lib.svo_raycast_full_noalloc(ctypes.c_void_p(d_words.data_ptr()), octree.words.size, octree.root,
+                                              octree.depth, ctypes.cast(varr, ctypes.c_void_p),
+                                              ctypes.cast(oarr, ctypes.c_void_p), 1, ctypes.c_void_p(side.cuda_stream))
+    assert rc == 1  # SVO_ERR_INVALID_ARGUMENT
+    graph.replay()
+    torch.cuda.synchronize()
+    assert float(x[0]) == 1.0
     for t in targets:
         t.close()
     ctx.close()
