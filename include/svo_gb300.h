@@ -294,7 +294,7 @@ svo_status svo_warp_frame_learned(svo_context* ctx, svo_target* t, const svo_vie
 svo_status svo_read_requested(svo_target* t, uint32_t* count);
 /* Guided learned frames (enable = 1): after reprojection, every pixel with a
  * cached surface point in its 3x3 neighbourhood is walked from just in front
- * of the nearest such point (4 cells of the level of detail at that
+ * of the nearest such point (2 cells of the level of detail at that
  * distance) instead of from the camera -- the same walk, started late, so it
  * finds the same voxel unless a surface the cache never saw lies in front of
  * the start. Only the remaining (unguided) pixels go to the net, which runs

@@ -976,7 +976,7 @@ int orc_guided_frame(void* h, const uint32_t* words, size_t n_words, uint32_t ro
     std::vector<uint32_t> cert_col(N, 0u);
     std::vector<float> cert_xyz(N * 4, 0.0f);
     // start distances: the 3x3 minimum of the reprojected points' camera
-    // distances, less 4 cells of the level of detail there; half that minimum
+    // distances, less 2 cells of the level of detail there; half that minimum
     // for a pixel with at least 3 holes (pixels of the frame without a point)
     // in its 3x3
     std::vector<float> dist(N);
@@ -1012,7 +1012,7 @@ int orc_guided_frame(void* h, const uint32_t* words, size_t n_words, uint32_t ro
                 sw *= 2.0f;
                 ++lod;
             }
-            gd = holes >= 3 ? s * 0.5f : std::fmax(s - 4.0f * (float)(1 << lod), 0.0f);
+            gd = holes >= 3 ? s * 0.5f : std::fmax(s - 2.0f * (float)(1 << lod), 0.0f);
             const bool rect = x >= ax && x < xe && y >= ay && y < ye;
             if (g.certify && holes == 0 && !rect) {
                 Certified c;
