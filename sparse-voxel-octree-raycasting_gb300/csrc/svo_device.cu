@@ -447,6 +447,10 @@ void period_shift(const float* a, const float* b, float e, float out[3]) {
     for (int i = 0; i < 3; ++i) out[i] = (float)std::nearbyint(((double)b[i] - (double)a[i]) / e) * e;
 }
 
+// Guided learned frames resolve the projection keys inside k_guide (one launch
+// less), except when the training tap reads the plane between the two.
+bool guided_resolve(const svo_target* t, bool learned) { return learned && t->B.guide && !t->feature_tap; }
+
 FrameParams make_params(const svo_target* t, const svo_view& v, int frame, const PlanePlan& q, bool have_cache,
                         bool learned = false) {
     FrameParams p{};
@@ -483,6 +487,7 @@ FrameParams make_params(const svo_target* t, const svo_view& v, int frame, const
     }
     p.serial = (uint32_t)(t->frames + 1);
     p.certify = (learned && t->guided && t->certify) ? 1 : 0;
+    p.clear_keys = guided_resolve(t, learned) ? 1 : 0;
     if (learned) {
         const float period = (float)(1u << (t->ctx->depth + 1)) / 16.0f;  // world units
         p.rebase = 1;
@@ -571,16 +576,23 @@ svo_status enqueue_learned_body(svo_context* ctx, svo_target* t, const svo_net* 
         SVO_LAUNCHED(ctx);
     }
     record(t, 1);
-    k_resolve_gather<<<dim3((res_x + 15) / 16, (res_y + 15) / 16), 256, 0, s>>>(t->d_params, t->B);
-    SVO_LAUNCHED(ctx);
-    if (t->feature_tap) {
-        k_net_features<<<dim3((res_x + 31) / 32, (res_y + 7) / 8), 256, 0, s>>>(t->d_params, t->B, t->feature_tap);
+    const dim3 guide_grid((res_x + kGuideBW - 1) / kGuideBW, (res_y + kGuideBH - 1) / kGuideBH);
+    if (guided_resolve(t, true)) {
+        // the gather happens inside k_guide; the tracer clears the keys
+        k_guide<true><<<guide_grid, kGuideBW * kGuideBH, 0, s>>>(t->d_params, t->B);
         SVO_LAUNCHED(ctx);
-    }
-    if (t->B.guide) {
-        k_guide<<<dim3((res_x + kGuideBW - 1) / kGuideBW, (res_y + kGuideBH - 1) / kGuideBH), kGuideBW * kGuideBH, 0,
-                  s>>>(t->d_params, t->B);
+    } else {
+        k_resolve_gather<<<dim3((res_x + 15) / 16, (res_y + 15) / 16), 256, 0, s>>>(t->d_params, t->B);
         SVO_LAUNCHED(ctx);
+        if (t->feature_tap) {
+            k_net_features<<<dim3((res_x + 31) / 32, (res_y + 7) / 8), 256, 0, s>>>(t->d_params, t->B,
+                                                                                   t->feature_tap);
+            SVO_LAUNCHED(ctx);
+        }
+        if (t->B.guide) {
+            k_guide<false><<<guide_grid, kGuideBW * kGuideBH, 0, s>>>(t->d_params, t->B);
+            SVO_LAUNCHED(ctx);
+        }
     }
     record(t, 2);
     NetInferArgs A{};

@@ -54,6 +54,12 @@ struct FrameParams {
     float src_shift[2][3];
     uint32_t serial;  // frame serial of the target (stamps the net tile flags)
     int certify;      // guided frames: certified reprojection (k_guide)
+    // Guided frames resolve the projection keys inside k_guide<true>, whose
+    // blocks read their neighbours' keys as a halo and so cannot clear them;
+    // the tracer clears them instead, a 32-key chunk with every packet it
+    // pulls, so the stores spread over the launch (one burst of 16 MB at its
+    // start cost more than the chunks).
+    int clear_keys;
 };
 
 // Buffers of one render target.
@@ -236,6 +242,28 @@ __device__ __forceinline__ void tile_mask_store(const TargetBuffers& B, uint8_t 
     }
 }
 
+// The winning source of target pixel t (its 64-bit key, kKeyEmpty for none):
+// the colour word (depth key bits + the source's colour byte) and the point,
+// re-based by whole periods in learned frames, with the hit code (learned
+// frames) or the view depth (plain frames, kernel.cl:585) in w.
+__device__ __forceinline__ uint32_t resolve_source(const FrameParams* __restrict__ P, const TargetBuffers& B,
+                                                   uint64_t key, float4& q) {
+    const uint32_t src = (uint32_t)key;
+    const uint32_t hi = (uint32_t)(key >> 32);
+    const int phys = (hi & 1u) ? P->src_plane[1] : P->src_plane[0];
+    q = plane_xyz(B, phys)[src];
+    if (P->rebase) {
+        const int r = (int)(hi & 1u);
+        q.x = __fadd_rn(q.x, P->src_shift[r][0]);
+        q.y = __fadd_rn(q.y, P->src_shift[r][1]);
+        q.z = __fadd_rn(q.z, P->src_shift[r][2]);
+    } else {
+        const float ax = __fsub_rn(q.x, P->ray.px), ay = __fsub_rn(q.y, P->ray.py), az = __fsub_rn(q.z, P->ray.pz);
+        q.w = dot3(ax, ay, az, P->vz);
+    }
+    return (hi & ~255u) + (plane_col(B, phys)[src] & 255u);
+}
+
 // Gather + clear + hole count, one 16x16 tile per block: each target pixel
 // takes its winning source (or becomes empty), then the block marks the 2x2
 // blocks whose four pixels are empty (raycast_counthole's test with
@@ -256,22 +284,9 @@ __global__ void __launch_bounds__(256) k_resolve_gather(const FrameParams* __res
             const uint64_t key = B.keys[t];
             if (key != kKeyEmpty) {
                 B.keys[t] = kKeyEmpty;
-                const uint32_t src = (uint32_t)key;
-                const uint32_t hi = (uint32_t)(key >> 32);
-                const int phys = (hi & 1u) ? P->src_plane[1] : P->src_plane[0];
-                float4 q = plane_xyz(B, phys)[src];
-                if (P->rebase) {
-                    const int r = (int)(hi & 1u);
-                    q.x = __fadd_rn(q.x, P->src_shift[r][0]);
-                    q.y = __fadd_rn(q.y, P->src_shift[r][1]);
-                    q.z = __fadd_rn(q.z, P->src_shift[r][2]);
-                }
-                const float ax = __fsub_rn(q.x, P->ray.px), ay = __fsub_rn(q.y, P->ray.py),
-                            az = __fsub_rn(q.z, P->ray.pz);
-                outc = (hi & ~255u) + (plane_col(B, phys)[src] & 255u);
-                // learned frames carry the point's hit code along; plain frames store
-                // the view depth (kernel.cl:585)
-                plane_xyz(B, cur)[t] = make_float4(q.x, q.y, q.z, P->rebase ? q.w : dot3(ax, ay, az, P->vz));
+                float4 q;
+                outc = resolve_source(P, B, key, q);
+                plane_xyz(B, cur)[t] = q;
             }
         }
         plane_col(B, cur)[t] = outc;
@@ -473,11 +488,23 @@ __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FramePa
     const RayCam cam = P->ray;
     float4* __restrict__ xyz = plane_xyz(B, P->cur);
     uint32_t* __restrict__ col = plane_col(B, P->cur);
+    const size_t n_keys = (size_t)res_x * res_y;
+    const uint32_t clear_chunks = (kBgrx && P->clear_keys) ? (uint32_t)((n_keys + 31u) / 32u) : 0u;
+    if (clear_chunks && total == 0) {  // no packet to spread the chunks over
+        for (size_t i = (size_t)blockIdx.x * BLOCK + threadIdx.x; i < n_keys; i += (size_t)gridDim.x * BLOCK)
+            B.keys[i] = kKeyEmpty;
+    }
     for (;;) {
         uint32_t p = 0;
         if (lane == 0) p = atomicAdd(B.counters, 1u);
         p = __shfl_sync(0xffffffffu, p, 0);
         if (p >= total) break;
+        if (kBgrx && clear_chunks) {
+            for (uint32_t c = p; c < clear_chunks; c += total) {
+                const size_t i = (size_t)c * 32u + (uint32_t)lane;
+                if (i < n_keys) B.keys[i] = kKeyEmpty;
+            }
+        }
         int x, y;
         bool valid;
         float s0 = 0.0f;

@@ -613,6 +613,14 @@ __device__ __forceinline__ bool certify_pixel(const RayCam& cam, int res_x, floa
 // plane, which other blocks read as their halo). Each warp appends the
 // pixels of one ray packet (pw x ph) of the block, so consecutive list
 // entries stay spatial neighbours.
+//
+// kResolve: the block also resolves the projection keys (k_resolve_gather's
+// gather, one launch less): every pixel of its halo takes its winning source
+// from the key buffer, and the block writes its own pixels' colour words and
+// points into the current plane. The keys stay set (neighbouring blocks read
+// them as their halo); the tracer clears them (FrameParams::clear_keys). No
+// hole tile masks: learned frames do not use them.
+template <bool kResolve>
 __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams* __restrict__ P, TargetBuffers B) {
     constexpr int kHW = kGuideBW + 2, kHH = kGuideBH + 2;
     __shared__ float dist[kHH][kHW];
@@ -648,8 +656,21 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
         float4 cq = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
         if (gx >= 0 && gx < res_x && gy >= 0 && gy < res_y) {
             const size_t o = (size_t)gy * res_x + gx;
-            const uint32_t c = __ldg(col + o);  // both loads in flight together
-            const float4 q = __ldg(xyz + o);
+            uint32_t c;
+            float4 q;
+            if (kResolve) {
+                const uint64_t key = P->have_cache ? B.keys[o] : kKeyEmpty;
+                c = kEmptyPixel;
+                q = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                if (key != kKeyEmpty) c = resolve_source(P, B, key, q);
+                if (wx >= 1 && wx <= kGuideBW && wy >= 1 && wy <= kGuideBH) {  // the block's own pixel
+                    plane_col(B, P->cur)[o] = c;
+                    if (c != kEmptyPixel) plane_xyz(B, P->cur)[o] = q;
+                }
+            } else {
+                c = __ldg(col + o);  // both loads in flight together
+                q = __ldg(xyz + o);
+            }
             // exact IEEE operations, so the CPU oracle finds the same start distances
             const float ax = __fsub_rn(q.x, cx), ay = __fsub_rn(q.y, cy), az = __fsub_rn(q.z, cz);
             if (c != kEmptyPixel) {
