@@ -347,7 +347,17 @@ svo_status plan_trace(svo_context* ctx, int kind, TraceLaunch& L) {
 
 // Persistent grid: as many blocks as fit on every SM; the access-policy
 // window travels with the launch so graph-captured launches keep it.
-svo_status launch_trace(svo_context* ctx, const TraceLaunch& L, void** args) {
+// Programmatic stream serialisation for a launch of the learned frame's
+// kernel chain: the kernel may start its own set-up while the kernel before
+// it finishes, and calls grid_dep_wait() before it reads that kernel's output.
+void add_chained(cudaLaunchConfig_t& cfg, cudaLaunchAttribute* attr) {
+    attr[cfg.numAttrs].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[cfg.numAttrs].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    ++cfg.numAttrs;
+}
+
+svo_status launch_trace(svo_context* ctx, const TraceLaunch& L, void** args, bool chained = false) {
     int per_sm = 0;
     SVO_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, L.fn, L.block, L.smem));
     cudaLaunchConfig_t cfg{};
@@ -355,7 +365,7 @@ svo_status launch_trace(svo_context* ctx, const TraceLaunch& L, void** args) {
     cfg.blockDim = dim3((unsigned)L.block);
     cfg.dynamicSmemBytes = L.smem;
     cfg.stream = ctx->stream;
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
     if (ctx->l2_window > 0) {
         attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
         attr[0].val.accessPolicyWindow.base_ptr = ctx->d_octree;
@@ -366,6 +376,7 @@ svo_status launch_trace(svo_context* ctx, const TraceLaunch& L, void** args) {
         cfg.attrs = attr;
         cfg.numAttrs = 1;
     }
+    if (chained) add_chained(cfg, attr);
     SVO_CUDA(ctx, cudaLaunchKernelExC(&cfg, L.fn, args));
     ++ctx->launches;
     return SVO_OK;
@@ -379,12 +390,12 @@ svo_status launch_trace_full(svo_context* ctx, FullBatch* d_batch) {
     return launch_trace(ctx, L, args);
 }
 
-svo_status launch_trace_warp(svo_context* ctx, svo_target* t, int kind = kTraceWarp) {
+svo_status launch_trace_warp(svo_context* ctx, svo_target* t, int kind = kTraceWarp, bool chained = false) {
     TraceLaunch L;
     svo_status st = plan_trace(ctx, kind, L);
     if (st != SVO_OK) return st;
     void* args[] = {&L.o, &t->d_params, &t->B, &ctx->d_fault};
-    return launch_trace(ctx, L, args);
+    return launch_trace(ctx, L, args, chained);
 }
 
 // Grid for a grid-stride loop over n items: enough blocks, capped at 32 per SM.
@@ -555,7 +566,14 @@ svo_status launch_net_infer(svo_context* ctx, const svo_net* net, bool pipeline,
     SVO_CUDA(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, kNetSmemBytes));
     const int grid = std::max(1, std::min(A.tiles, ctx->sm_count));
     void* args[] = {&A};
-    SVO_CUDA(ctx, cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kNetThreads), args, kNetSmemBytes, ctx->stream));
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kNetThreads);
+    cfg.dynamicSmemBytes = kNetSmemBytes;
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute attr[1];
+    if (pipeline) add_chained(cfg, attr);  // the frame's chain: set-up overlaps k_guide's tail
+    SVO_CUDA(ctx, cudaLaunchKernelExC(&cfg, fn, args));
     ++ctx->launches;
     return SVO_OK;
 }
@@ -572,14 +590,26 @@ svo_status enqueue_learned_body(svo_context* ctx, svo_target* t, const svo_net* 
     {
         const int threads = 256;
         int blocks = (int)std::min<size_t>((t->N + threads - 1) / threads, (size_t)ctx->sm_count * 8);
-        k_project<<<blocks, threads, 0, s>>>(t->d_params, t->B);
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3((unsigned)blocks);
+        cfg.blockDim = dim3(threads);
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        add_chained(cfg, attr);
+        SVO_CUDA(ctx, cudaLaunchKernelEx(&cfg, k_project, (const FrameParams*)t->d_params, t->B));
         SVO_LAUNCHED(ctx);
     }
     record(t, 1);
     const dim3 guide_grid((res_x + kGuideBW - 1) / kGuideBW, (res_y + kGuideBH - 1) / kGuideBH);
     if (guided_resolve(t, true)) {
         // the gather happens inside k_guide; the tracer clears the keys
-        k_guide<true><<<guide_grid, kGuideBW * kGuideBH, 0, s>>>(t->d_params, t->B);
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = guide_grid;
+        cfg.blockDim = dim3(kGuideBW * kGuideBH);
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        add_chained(cfg, attr);
+        SVO_CUDA(ctx, cudaLaunchKernelEx(&cfg, k_guide<true>, (const FrameParams*)t->d_params, t->B));
         SVO_LAUNCHED(ctx);
     } else {
         k_resolve_gather<<<dim3((res_x + 15) / 16, (res_y + 15) / 16), 256, 0, s>>>(t->d_params, t->B);
@@ -612,7 +642,7 @@ svo_status enqueue_learned_body(svo_context* ctx, svo_target* t, const svo_net* 
         SVO_LAUNCHED(ctx);
     }
     record(t, 3);
-    st = launch_trace_warp(ctx, t, kTraceWarpBgrx);
+    st = launch_trace_warp(ctx, t, kTraceWarpBgrx, true);
     if (st != SVO_OK) return st;
     record(t, 4);
     return SVO_OK;

@@ -162,6 +162,8 @@ __device__ __forceinline__ float dot3(float ax, float ay, float az, const float*
 // plane 2, then the lowest source pixel -- the order in which the reference's
 // work-items run.
 __global__ void __launch_bounds__(256) k_project(const FrameParams* __restrict__ P, TargetBuffers B) {
+    grid_dep_wait();
+    grid_dep_launch();
     if (!P->have_cache) return;
     const int res_x = B.res_x, res_y = B.res_y;
     const uint32_t N = (uint32_t)res_x * (uint32_t)res_y;
@@ -464,7 +466,8 @@ __global__ void __launch_bounds__(BLOCK) k_trace_warp(Octree o_in, const FramePa
     uint32_t* stk = svo_dsmem + threadIdx.x;
     uint32_t fault = 0;
     bool staged;
-    const Octree o = stage_octree<DEPTH, BLOCK>(o_in, &mbar, fault, staged);
+    const Octree o = stage_octree<DEPTH, BLOCK>(o_in, &mbar, fault, staged);  // the octree: no dependency
+    grid_dep_wait();
     const int res_x = B.res_x, res_y = B.res_y;
     const uint32_t tiles = (uint32_t)B.tiles_x * (uint32_t)B.tiles_y;
     const uint32_t holes = B.counters[1];

@@ -622,6 +622,8 @@ __device__ __forceinline__ bool certify_pixel(const RayCam& cam, int res_x, floa
 // hole tile masks: learned frames do not use them.
 template <bool kResolve>
 __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams* __restrict__ P, TargetBuffers B) {
+    grid_dep_wait();
+    grid_dep_launch();
     constexpr int kHW = kGuideBW + 2, kHH = kGuideBH + 2;
     __shared__ float dist[kHH][kHW];
     __shared__ uint8_t hole[kHH][kHW];  // a pixel of the frame without a point
@@ -878,11 +880,6 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_infer(NetInferArgs A) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[tid])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (kPipeline) {
-        const uint32_t* src = reinterpret_cast<const uint32_t*>(A.P);
-        uint32_t* dst = reinterpret_cast<uint32_t*>(&sP);
-        for (int i = tid; i < (int)(sizeof(FrameParams) / 4); i += kNetThreads) dst[i] = src[i];
-    }
     // weights, biases; zero every activation and input plane (guards included)
     {
         const uint4* src = reinterpret_cast<const uint4*>(A.packed);
@@ -892,6 +889,15 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_infer(NetInferArgs A) {
         for (int i = tid; i < kNetBias; i += kNetThreads) b[i] = A.bias[i];
         uint4* z = reinterpret_cast<uint4*>(smem);
         for (int i = tid; i < 6 * kNetPlaneBytes / 16; i += kNetThreads) z[i] = make_uint4(0, 0, 0, 0);
+    }
+    // everything above is this launch's own set-up; what follows reads the
+    // frame's parameters and the kernels before this one
+    grid_dep_wait();
+    grid_dep_launch();
+    if (kPipeline) {
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(A.P);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(&sP);
+        for (int i = tid; i < (int)(sizeof(FrameParams) / 4); i += kNetThreads) dst[i] = src[i];
     }
     __syncthreads();
     // Work: every tile, or (guided frames) the listed tiles.

@@ -87,6 +87,16 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
     return ok != 0;
 }
 
+// Programmatic dependent launch (the learned frame's kernel chain): a kernel
+// launched with programmatic stream serialisation may start while the kernel
+// before it in the stream still runs; it does its independent set-up first,
+// then waits here until that kernel has completed and its writes are
+// visible (an immediate return for a kernel launched normally).
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// Lets the next kernel in the stream start its set-up once every block of
+// this one has passed this point (called after grid_dep_wait).
+__device__ __forceinline__ void grid_dep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ uint64_t global_ns() {
     uint64_t t;
     asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
