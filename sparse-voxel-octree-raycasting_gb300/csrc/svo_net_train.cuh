@@ -200,7 +200,10 @@ template <int CIN>
 struct BwdWeightLayout {
     static constexpr int kRows = 9 * CIN;
     static constexpr int kA1 = kRows > 128;                      // a second 128-row operand
-    static constexpr int kWinPlane = (kNetPos + 2 * kNetGuard) * 2;  // bytes of one bf16 channel plane
+    // bytes of one bf16 channel plane: the positions with their guards, padded
+    // to 16 mod 128 so that 16-byte reads of the same slice of consecutive
+    // channels fall in different banks
+    static constexpr int kWinPlane = ((kNetPos + 2 * kNetGuard) * 2 + 127) / 128 * 128 + 16;
     static constexpr int kWin = CIN * kWinPlane;
     static constexpr int kK = 64;                                // positions per chunk (one window row)
     static constexpr int kABytes = 128 * kK * 2;                 // 16 KB
@@ -257,8 +260,26 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_net_bwd_weight_tc(NetBwdWeig
             reinterpret_cast<uint16_t*>(smem)[ci * (L::kWinPlane / 2) + kNetGuard + p] = (uint16_t)bf16_bits(v);
         }
         __syncthreads();
+        // gradient values of the first chunk (window row 1) in registers; each
+        // chunk loads the next chunk's before it stages its own operands, so
+        // the global loads overlap the staging and the MMAs
+        const int g_co = tid >> 5, g_k = 2 * lane;
+        float gv[2];
+        auto load_g = [&](int row, float* out) {
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int kk = g_k + e;
+                const int gx = wx + kk, gy = wy + row;
+                out[e] = (g_co < KIN && kk >= 1 && kk <= kBwdOutW && gx < W && gy < H)
+                             ? __ldg(A.g + g_co * n + (size_t)gy * W + gx)
+                             : 0.0f;
+            }
+        };
+        load_g(1, gv);
         for (int c = 0; c < kBwdOutH && ok; ++c, ++chunks) {
             const uint32_t buf = chunks & 1u;
+            float gnext[2] = {0.0f, 0.0f};
+            if (c + 1 < kBwdOutH) load_g(c + 2, gnext);
             if (chunks >= 2) {  // the MMAs of chunk (chunks - 2) read this buffer
                 const bool r = mbar_wait_phase(smem_addr(&mbar[buf]), ((chunks - 2) >> 1) & 1u);
                 if (!r) atomicOr(&abort_s, 1u);
@@ -271,40 +292,51 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_net_bwd_weight_tc(NetBwdWeig
             }
             uint8_t* bufp = smem + L::kWin + buf * L::kBuf;
             const int row = c + 1;  // window row of this chunk's positions
-            // im2col rows (t, ci): 8 positions of channel ci shifted by tap t per item
+            // im2col rows (t, ci): 8 positions of channel ci shifted by tap t per
+            // item, consecutive threads on consecutive rows (conflict-free stores).
+            // A slice starts 0, +1 or -1 positions off a 16-byte boundary: two
+            // aligned 16-byte reads and funnel shifts assemble it.
             for (int it = tid; it < L::kRows * (L::kK / 8); it += kBwdThreads) {
-                const int r = it >> 3, kc = it & 7;
+                const int kc = it / L::kRows, r = it - kc * L::kRows;
                 const int t = r / CIN, ci = r % CIN;
                 const int off = (t / 3 - 1) * kNetTW + (t % 3 - 1);
-                const int p0 = row * kNetTW + kc * 8 + off;
-                const uint16_t* s = win + ci * (L::kWinPlane / 2) + kNetGuard + p0;
+                const int e0 = kNetGuard + row * kNetTW + kc * 8 + off;  // element index in the plane
+                const uint32_t* pl = reinterpret_cast<const uint32_t*>(win + ci * (L::kWinPlane / 2));
+                const int a = e0 & ~7;                                  // aligned 8-element group
+                const uint4 lo = *reinterpret_cast<const uint4*>(pl + (a >> 1));
                 uint4 v;
-                v.x = (uint32_t)s[0] | (uint32_t)s[1] << 16;
-                v.y = (uint32_t)s[2] | (uint32_t)s[3] << 16;
-                v.z = (uint32_t)s[4] | (uint32_t)s[5] << 16;
-                v.w = (uint32_t)s[6] | (uint32_t)s[7] << 16;
+                if (e0 == a) {
+                    v = lo;
+                } else {
+                    const uint4 hi = *reinterpret_cast<const uint4*>(pl + (a >> 1) + 4);
+                    const uint32_t w[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+                    const int b = (e0 - a) * 2;  // byte offset: 2 (one position) or 14 (seven)
+                    const int wo = b >> 2;       // word offset 0 or 3, then a 16-bit shift
+                    v.x = __funnelshift_r(w[wo], w[wo + 1], 16);
+                    v.y = __funnelshift_r(w[wo + 1], w[wo + 2], 16);
+                    v.z = __funnelshift_r(w[wo + 2], w[wo + 3], 16);
+                    v.w = __funnelshift_r(w[wo + 3], w[wo + 4], 16);
+                }
                 const int op = r >> 7, rr = r & 127;  // operand and its row
                 *reinterpret_cast<uint4*>(bufp + op * L::kABytes + kc * 2048 + rr * 16) = v;
             }
             // gradient rows (co): hi and lo parts of 64 positions, zero outside the tile
             {
-                const int co = tid >> 5, k = 2 * lane;
                 uint16_t* bh = reinterpret_cast<uint16_t*>(bufp + (1 + L::kA1) * L::kABytes);
                 uint16_t* bl = bh + L::kBBytes / 2;
 #pragma unroll
                 for (int e = 0; e < 2; ++e) {
-                    const int kk = k + e;
-                    const int gx = wx + kk, gy = wy + row;
-                    float v = 0.0f;
-                    if (co < KIN && kk >= 1 && kk <= kBwdOutW && gx < W && gy < H)
-                        v = __ldg(A.g + co * n + (size_t)gy * W + gx);
+                    const int kk = g_k + e;
+                    const float v = gv[e];
                     bias_acc += v;
                     uint32_t hi, lo;
                     split_bf16(v, hi, lo);
-                    const int idx = (co >> 3) * (8 * L::kK) + (kk >> 3) * 64 + (co & 7) * 8 + (kk & 7);
+                    const int idx = (g_co >> 3) * (8 * L::kK) + (kk >> 3) * 64 + (g_co & 7) * 8 + (kk & 7);
                     bh[idx] = (uint16_t)hi;
                     bl[idx] = (uint16_t)lo;
                 }
+                gv[0] = gnext[0];
+                gv[1] = gnext[1];
             }
             fence_async_smem();
             tc_fence_before();

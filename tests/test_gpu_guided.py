@@ -237,3 +237,35 @@ def test_guided_toggle_and_all_requested(svo, scene, gpu_ctx):
     t.close()
     full.close()
     net.close()
+
+
+def test_guided_frames_same_with_and_without_the_feature_tap(svo, scene, gpu_ctx):
+    # Guided frames resolve the projection keys inside k_guide, unless the
+    # training tap reads the plane between the gather and the guide (then
+    # k_resolve_gather runs first): both orders give the same frames, and the
+    # keys the fused path leaves set are cleared for the next frame in both.
+    torch = pytest.importorskip("torch")
+    octree = scene(9, 77, True)
+    gpu_ctx.upload(octree)
+    net = gpu_ctx.net()
+    net.load_file(_weights(svo))
+    W, H = 160, 96
+    a, b = gpu_ctx.target(W, H), gpu_ctx.target(W, H)
+    for t in (a, b):
+        t.set_guided(True)
+        t.use_graph(True)
+    buf = torch.zeros(8 * W * H, dtype=torch.float32, device="cuda")
+    for f in range(12):
+        b.set_feature_tap(buf.data_ptr() if f % 3 != 1 else None)  # switch paths mid-run
+        v = svo.camera_path(2, 9, f, W, H)
+        gpu_ctx.warp_frame_learned(a, v, f, net, 0.5)
+        gpu_ctx.warp_frame_learned(b, v, f, net, 0.5)
+        gpu_ctx.synchronize()
+        assert np.array_equal(a.colour(2), b.colour(2)), f
+        assert np.array_equal(a.coords(0).view(np.uint32), b.coords(0).view(np.uint32)), f
+        assert np.array_equal(a.bgrx(), b.bgrx()), f
+        assert np.array_equal(a.guide().view(np.uint32), b.guide().view(np.uint32)), f
+    b.set_feature_tap(None)
+    a.close()
+    b.close()
+    net.close()
