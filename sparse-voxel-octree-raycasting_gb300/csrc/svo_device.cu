@@ -801,7 +801,7 @@ svo_status net_backward_layer(svo_net* net, const float* a, const float* g, floa
         constexpr int smem = BwdWeightLayout<CIN>::kSmem;
         SVO_CUDA(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         void* args[] = {&A};
-        SVO_CUDA(ctx, cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kBwdThreads), args, smem, ctx->stream));
+        SVO_CUDA(ctx, cudaLaunchKernel(fn, dim3((unsigned)grid), dim3(kBwdWThreads), args, smem, ctx->stream));
         ++ctx->launches;
         constexpr int vals = 9 * CIN * KIN + KIN;
         k_net_reduce<<<(vals + 255) / 256, 256, 0, ctx->stream>>>(net->partial, grid, vals,

@@ -196,6 +196,9 @@ struct NetBwdWeightArgs {
 // Rows of the im2col operand: (tap, input channel) pairs, t * cin + ci; the
 // first 128 in one operand, the rest (tap 8 when cin = 16) in a second one
 // whose other rows stay zero.
+constexpr int kBwdWStages = 3;                          // chunk buffers in flight
+constexpr int kBwdWProducers = 512;                     // 16 warps stage the chunks
+constexpr int kBwdWThreads = kBwdWProducers + 32;       // + the warp that issues the MMAs
 template <int CIN>
 struct BwdWeightLayout {
     static constexpr int kRows = 9 * CIN;
@@ -209,14 +212,31 @@ struct BwdWeightLayout {
     static constexpr int kABytes = 128 * kK * 2;                 // 16 KB
     static constexpr int kBBytes = 16 * kK * 2;                  // 2 KB
     static constexpr int kBuf = (1 + kA1) * kABytes + 2 * kBBytes;
-    static constexpr int kSmem = kWin + 2 * kBuf;
+    static constexpr int kSmem = kWin + kBwdWStages * kBuf;
 };
 
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+// Barrier 1 among the producer warps only (the issuing warp never joins it).
+__device__ __forceinline__ void producers_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kBwdWProducers) : "memory"); }
+
+// Warp-specialised pipeline: 16 producer warps stage one 64-position chunk
+// (a window row) at a time -- the im2col rows and the gradient rows -- into
+// a ring of kBwdWStages buffers, arriving on the chunk's `full` barrier; one
+// issuing thread waits for it, issues the chunk's MMAs and commits them to
+// the buffer's `empty` barrier, which the producers wait on before they
+// reuse the buffer. So the staging of later chunks runs while the tensor
+// core works on earlier ones. Every wait is bounded: a producer or the
+// issuer that gives up sets abort_s; after that the producers stop waiting
+// (their barriers stay in step), the issuer stops issuing, the CTA waits
+// (bounded) for the MMAs it issued, writes nothing and flags the fault.
 template <int CIN, int KIN, bool kFirst>
-__global__ void __launch_bounds__(kBwdThreads, 1) k_net_bwd_weight_tc(NetBwdWeightArgs A) {
+__global__ void __launch_bounds__(kBwdWThreads, 1) k_net_bwd_weight_tc(NetBwdWeightArgs A) {
     using L = BwdWeightLayout<CIN>;
     constexpr int kTmemCols = 32;  // D0 in columns 0-15, D1 in 16-31
-    __shared__ uint64_t mbar[2];
+    constexpr int S = kBwdWStages;
+    __shared__ uint64_t full[S], empty[S];
     __shared__ uint32_t tmem_base_s;
     __shared__ uint32_t abort_s;
     uint8_t* smem = reinterpret_cast<uint8_t*>(svo_dsmem);
@@ -232,122 +252,41 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_net_bwd_weight_tc(NetBwdWeig
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    if (tid < 2) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[tid])) : "memory");
+    if (tid < S) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&full[tid])), "n"(kBwdWProducers)
+                     : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&empty[tid])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (tid == 0) abort_s = 0;
     {  // zero everything: window guards and the operand rows staging never writes
         uint4* z = reinterpret_cast<uint4*>(smem);
-        for (int i = tid; i < L::kSmem / 16; i += kBwdThreads) z[i] = make_uint4(0, 0, 0, 0);
+        for (int i = tid; i < L::kSmem / 16; i += kBwdWThreads) z[i] = make_uint4(0, 0, 0, 0);
     }
+    tc_fence_before();
     __syncthreads();
+    tc_fence_after();
     const uint32_t tmem = tmem_base_s;
-    float bias_acc = 0.0f;  // thread i sums g of output channel i / 32
-    uint32_t chunks = 0, fault = 0;
-    bool ok = true;
+    int my_tiles = 0;
+    for (int item = blockIdx.x; item < A.tiles; item += gridDim.x) ++my_tiles;
+    const uint32_t n_chunks = (uint32_t)my_tiles * kBwdOutH;
+    float bias_acc = 0.0f;  // producer thread i sums g of output channel i / 32
+    uint32_t fault = 0;
 
-    for (int item = blockIdx.x; item < A.tiles && ok; item += gridDim.x) {
-        const int ox = (item % A.tiles_x) * kBwdOutW, oy = (item / A.tiles_x) * kBwdOutH;
-        const int wx = ox - 1, wy = oy - 1;
-        // the input window, bf16 channel planes with a guard of kNetGuard positions
-        for (int i = tid; i < CIN * kNetPos; i += kBwdThreads) {
-            const int ci = i / kNetPos, p = i % kNetPos;
-            const int gx = wx + (p & (kNetTW - 1)), gy = wy + (p >> 6);
-            float v = 0.0f;
-            if (gx >= 0 && gx < W && gy >= 0 && gy < H) v = __ldg(A.a + ci * n + (size_t)gy * W + gx);
-            if (kFirst) v = bf16_round(v);
-            reinterpret_cast<uint16_t*>(smem)[ci * (L::kWinPlane / 2) + kNetGuard + p] = (uint16_t)bf16_bits(v);
-        }
-        __syncthreads();
-        // gradient values of the first chunk (window row 1) in registers; each
-        // chunk loads the next chunk's before it stages its own operands, so
-        // the global loads overlap the staging and the MMAs
-        const int g_co = tid >> 5, g_k = 2 * lane;
-        float gv[2];
-        auto load_g = [&](int row, float* out) {
-#pragma unroll
-            for (int e = 0; e < 2; ++e) {
-                const int kk = g_k + e;
-                const int gx = wx + kk, gy = wy + row;
-                out[e] = (g_co < KIN && kk >= 1 && kk <= kBwdOutW && gx < W && gy < H)
-                             ? __ldg(A.g + g_co * n + (size_t)gy * W + gx)
-                             : 0.0f;
-            }
-        };
-        load_g(1, gv);
-        for (int c = 0; c < kBwdOutH && ok; ++c, ++chunks) {
-            const uint32_t buf = chunks & 1u;
-            float gnext[2] = {0.0f, 0.0f};
-            if (c + 1 < kBwdOutH) load_g(c + 2, gnext);
-            if (chunks >= 2) {  // the MMAs of chunk (chunks - 2) read this buffer
-                const bool r = mbar_wait_phase(smem_addr(&mbar[buf]), ((chunks - 2) >> 1) & 1u);
-                if (!r) atomicOr(&abort_s, 1u);
-                __syncthreads();
-                if (abort_s) {
-                    ok = false;
-                    fault |= kFaultNet;
-                    break;
-                }
-            }
-            uint8_t* bufp = smem + L::kWin + buf * L::kBuf;
-            const int row = c + 1;  // window row of this chunk's positions
-            // im2col rows (t, ci): 8 positions of channel ci shifted by tap t per
-            // item, consecutive threads on consecutive rows (conflict-free stores).
-            // A slice starts 0, +1 or -1 positions off a 16-byte boundary: two
-            // aligned 16-byte reads and funnel shifts assemble it.
-            for (int it = tid; it < L::kRows * (L::kK / 8); it += kBwdThreads) {
-                const int kc = it / L::kRows, r = it - kc * L::kRows;
-                const int t = r / CIN, ci = r % CIN;
-                const int off = (t / 3 - 1) * kNetTW + (t % 3 - 1);
-                const int e0 = kNetGuard + row * kNetTW + kc * 8 + off;  // element index in the plane
-                const uint32_t* pl = reinterpret_cast<const uint32_t*>(win + ci * (L::kWinPlane / 2));
-                const int a = e0 & ~7;                                  // aligned 8-element group
-                const uint4 lo = *reinterpret_cast<const uint4*>(pl + (a >> 1));
-                uint4 v;
-                if (e0 == a) {
-                    v = lo;
-                } else {
-                    const uint4 hi = *reinterpret_cast<const uint4*>(pl + (a >> 1) + 4);
-                    const uint32_t w[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
-                    const int b = (e0 - a) * 2;  // byte offset: 2 (one position) or 14 (seven)
-                    const int wo = b >> 2;       // word offset 0 or 3, then a 16-bit shift
-                    v.x = __funnelshift_r(w[wo], w[wo + 1], 16);
-                    v.y = __funnelshift_r(w[wo + 1], w[wo + 2], 16);
-                    v.z = __funnelshift_r(w[wo + 2], w[wo + 3], 16);
-                    v.w = __funnelshift_r(w[wo + 3], w[wo + 4], 16);
-                }
-                const int op = r >> 7, rr = r & 127;  // operand and its row
-                *reinterpret_cast<uint4*>(bufp + op * L::kABytes + kc * 2048 + rr * 16) = v;
-            }
-            // gradient rows (co): hi and lo parts of 64 positions, zero outside the tile
-            {
-                uint16_t* bh = reinterpret_cast<uint16_t*>(bufp + (1 + L::kA1) * L::kABytes);
-                uint16_t* bl = bh + L::kBBytes / 2;
-#pragma unroll
-                for (int e = 0; e < 2; ++e) {
-                    const int kk = g_k + e;
-                    const float v = gv[e];
-                    bias_acc += v;
-                    uint32_t hi, lo;
-                    split_bf16(v, hi, lo);
-                    const int idx = (g_co >> 3) * (8 * L::kK) + (kk >> 3) * 64 + (g_co & 7) * 8 + (kk & 7);
-                    bh[idx] = (uint16_t)hi;
-                    bl[idx] = (uint16_t)lo;
-                }
-                gv[0] = gnext[0];
-                gv[1] = gnext[1];
-            }
-            fence_async_smem();
-            tc_fence_before();
-            __syncthreads();
-            tc_fence_after();
-            if (tid == 0) {
-                const uint32_t a0 = sbase + (uint32_t)(L::kWin + buf * L::kBuf);
+    if (warp == kBwdWProducers / 32) {
+        // ---- the issuing warp: lane 0 issues every chunk's MMAs
+        if (lane == 0) {
+            uint32_t issued = 0;
+            for (uint32_t c = 0; c < n_chunks; ++c) {
+                const uint32_t st = c % S;
+                if (!mbar_wait_phase(smem_addr(&full[st]), (c / S) & 1u)) atomicOr(&abort_s, 1u);
+                if (*(volatile uint32_t*)&abort_s) break;
+                tc_fence_after();
+                const uint32_t a0 = sbase + (uint32_t)(L::kWin + st * L::kBuf);
                 const uint32_t bhi = a0 + (uint32_t)((1 + L::kA1) * L::kABytes), blo = bhi + (uint32_t)L::kBBytes;
 #pragma unroll
                 for (int s = 0; s < L::kK / 16; ++s) {
-                    const uint32_t acc = (chunks > 0 || s > 0) ? 1u : 0u;
+                    const uint32_t acc = (c > 0 || s > 0) ? 1u : 0u;
                     const uint64_t bdh = tc_desc(bhi + (uint32_t)s * 256u, 128u, 1024u);
                     const uint64_t bdl = tc_desc(blo + (uint32_t)s * 256u, 128u, 1024u);
                     const uint64_t ad0 = tc_desc(a0 + (uint32_t)s * 4096u, 2048u, 128u);
@@ -359,29 +298,140 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_net_bwd_weight_tc(NetBwdWeig
                         tc_mma(tmem + 16u, ad1, bdl, 1u);
                     }
                 }
-                tc_commit(smem_addr(&mbar[buf]));
+                tc_commit(smem_addr(&empty[st]));
+                issued = c + 1;
+            }
+            // the accumulators are complete once the last chunk's MMAs are
+            if (issued > 0) {
+                const uint32_t last = issued - 1;
+                if (!mbar_wait_phase(smem_addr(&empty[last % S]), (last / S) & 1u)) atomicOr(&abort_s, 1u);
+            }
+            if (issued < n_chunks) atomicOr(&abort_s, 1u);
+        }
+        __syncwarp();
+    } else {
+        // ---- the producers
+        const int g_co = warp, g_k = 2 * lane;  // gradient value (channel, 2 positions) of this thread
+        bool stop = false;                      // this thread saw the abort: no more waits
+        uint32_t c = 0;
+        for (int item = blockIdx.x; item < A.tiles; item += gridDim.x) {
+            const int ox = (item % A.tiles_x) * kBwdOutW, oy = (item / A.tiles_x) * kBwdOutH;
+            const int wx = ox - 1, wy = oy - 1;
+            producers_sync();  // every producer has read the last tile's window
+            // the input window, bf16 channel planes with a guard of kNetGuard
+            // positions: 16 loads in flight per thread, then their stores
+            constexpr int kPer = CIN * kNetPos / kBwdWProducers;
+            static_assert(kPer % 16 == 0, "window staging in groups of 16 loads");
+            for (int b = 0; b < kPer; b += 16) {
+                float v[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int i = tid + (b + j) * kBwdWProducers;
+                    const int ci = i / kNetPos, p = i % kNetPos;
+                    const int gx = wx + (p & (kNetTW - 1)), gy = wy + (p >> 6);
+                    v[j] = (gx >= 0 && gx < W && gy >= 0 && gy < H) ? __ldg(A.a + ci * n + (size_t)gy * W + gx) : 0.0f;
+                }
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int i = tid + (b + j) * kBwdWProducers;
+                    const int ci = i / kNetPos, p = i % kNetPos;
+                    const float x = kFirst ? bf16_round(v[j]) : v[j];
+                    reinterpret_cast<uint16_t*>(smem)[ci * (L::kWinPlane / 2) + kNetGuard + p] =
+                        (uint16_t)bf16_bits(x);
+                }
+            }
+            // gradient values of window row r of this tile, zero outside it
+            auto load_g = [&](int row, float* out) {
+#pragma unroll
+                for (int e = 0; e < 2; ++e) {
+                    const int kk = g_k + e;
+                    const int gx = wx + kk, gy = wy + row;
+                    out[e] = (g_co < KIN && kk >= 1 && kk <= kBwdOutW && gx < W && gy < H)
+                                 ? __ldg(A.g + g_co * n + (size_t)gy * W + gx)
+                                 : 0.0f;
+                }
+            };
+            // gradient values of the next kAhead chunks in flight (registers)
+            constexpr int kAhead = 3;
+            float gq[kAhead][2];
+#pragma unroll
+            for (int a = 0; a < kAhead; ++a) load_g(1 + a, gq[a]);
+            producers_sync();  // the window is complete
+            for (int cr = 0; cr < kBwdOutH; ++cr, ++c) {
+                const uint32_t st = c % S;
+                float gv[2] = {gq[0][0], gq[0][1]};
+#pragma unroll
+                for (int a = 0; a + 1 < kAhead; ++a) {
+                    gq[a][0] = gq[a + 1][0];
+                    gq[a][1] = gq[a + 1][1];
+                }
+                if (cr + kAhead < kBwdOutH) {
+                    load_g(cr + 1 + kAhead, gq[kAhead - 1]);
+                } else {
+                    gq[kAhead - 1][0] = gq[kAhead - 1][1] = 0.0f;
+                }
+                if (!stop && c >= S && !mbar_wait_phase(smem_addr(&empty[st]), (c / S - 1u) & 1u))
+                    atomicOr(&abort_s, 1u);
+                if (*(volatile uint32_t*)&abort_s) stop = true;
+                uint8_t* bufp = smem + L::kWin + st * L::kBuf;
+                const int row = cr + 1;  // window row of this chunk's positions
+                // im2col rows (t, ci): 8 positions of channel ci shifted by tap t per
+                // item, consecutive threads on consecutive rows (conflict-free stores).
+                // A slice starts 0, +1 or -1 positions off a 16-byte boundary: two
+                // aligned 16-byte reads and funnel shifts assemble it.
+                for (int it = tid; it < L::kRows * (L::kK / 8); it += kBwdWProducers) {
+                    const int kc = it / L::kRows, r = it - kc * L::kRows;
+                    const int t = r / CIN, ci = r % CIN;
+                    const int off = (t / 3 - 1) * kNetTW + (t % 3 - 1);
+                    const int e0 = kNetGuard + row * kNetTW + kc * 8 + off;  // element index in the plane
+                    const uint32_t* pl = reinterpret_cast<const uint32_t*>(win + ci * (L::kWinPlane / 2));
+                    const int a = e0 & ~7;                                  // aligned 8-element group
+                    const uint4 lo = *reinterpret_cast<const uint4*>(pl + (a >> 1));
+                    uint4 v;
+                    if (e0 == a) {
+                        v = lo;
+                    } else {
+                        const uint4 hi = *reinterpret_cast<const uint4*>(pl + (a >> 1) + 4);
+                        const uint32_t w[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
+                        const int wo = ((e0 - a) * 2) >> 2;  // byte offset 2 or 14: words 0 or 3, then 16 bits
+                        v.x = __funnelshift_r(w[wo], w[wo + 1], 16);
+                        v.y = __funnelshift_r(w[wo + 1], w[wo + 2], 16);
+                        v.z = __funnelshift_r(w[wo + 2], w[wo + 3], 16);
+                        v.w = __funnelshift_r(w[wo + 3], w[wo + 4], 16);
+                    }
+                    const int op = r >> 7, rr = r & 127;  // operand and its row
+                    *reinterpret_cast<uint4*>(bufp + op * L::kABytes + kc * 2048 + rr * 16) = v;
+                }
+                // gradient rows (co): hi and lo parts of 64 positions
+                {
+                    uint16_t* bh = reinterpret_cast<uint16_t*>(bufp + (1 + L::kA1) * L::kABytes);
+                    uint16_t* bl = bh + L::kBBytes / 2;
+#pragma unroll
+                    for (int e = 0; e < 2; ++e) {
+                        const int kk = g_k + e;
+                        const float v = gv[e];
+                        bias_acc += v;
+                        uint32_t hi, lo;
+                        split_bf16(v, hi, lo);
+                        const int idx = (g_co >> 3) * (8 * L::kK) + (kk >> 3) * 64 + (g_co & 7) * 8 + (kk & 7);
+                        bh[idx] = (uint16_t)hi;
+                        bl[idx] = (uint16_t)lo;
+                    }
+                }
+                fence_async_smem();  // the stores reach the tensor core's view of shared memory
+                mbar_arrive(smem_addr(&full[st]));
             }
         }
-        __syncthreads();  // every thread has read the window before the next tile restages it
-    }
-    // wait for the last chunk on each buffer
-    if (ok && chunks > 0) {
-        bool r = true;
-        for (uint32_t b = 0; b < 2 && b < chunks; ++b) {
-            const uint32_t last = (chunks - 1u) - ((chunks - 1u - b) & 1u);  // last chunk staged in buffer b
-            r = r && mbar_wait_phase(smem_addr(&mbar[b]), (last >> 1) & 1u);
-        }
-        if (!r) atomicOr(&abort_s, 1u);
     }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     constexpr int kVals = 9 * CIN * KIN + KIN;
     float* dst = A.partial + (size_t)blockIdx.x * kVals;
-    if (ok && !abort_s) {
+    if (!abort_s) {
         if (warp < 4) {
             float v[16];
-            if (chunks > 0) {
+            if (n_chunks > 0) {
                 tc_ld16(tmem + ((uint32_t)(32 * warp) << 16), v);
             } else {
 #pragma unroll
@@ -392,7 +442,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_net_bwd_weight_tc(NetBwdWeig
 #pragma unroll
                 for (int c = 0; c < KIN; ++c) dst[r * KIN + c] = v[c];
             if (L::kA1) {
-                if (chunks > 0) {
+                if (n_chunks > 0) {
                     tc_ld16(tmem + ((uint32_t)(32 * warp) << 16) + 16u, v);
                 }
                 if (r < L::kRows - 128)
@@ -400,11 +450,13 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_net_bwd_weight_tc(NetBwdWeig
                     for (int c = 0; c < KIN; ++c) dst[(128 + r) * KIN + c] = v[c];
             }
         }
-        // biases: warp co sums its lanes' partial sums in a fixed order
-        float s = bias_acc;
+        if (warp < kBwdWProducers / 32) {
+            // biases: warp co sums its lanes' partial sums in a fixed order
+            float s = bias_acc;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if (lane == 0 && warp < KIN) dst[9 * CIN * KIN + warp] = s;
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            if (lane == 0 && warp < KIN) dst[9 * CIN * KIN + warp] = s;
+        }
     } else {
         fault |= kFaultNet;
     }
