@@ -239,9 +239,9 @@ __global__ void __launch_bounds__(kBwdWThreads, 1) k_net_bwd_weight_tc(NetBwdWei
     __shared__ uint64_t full[S], empty[S];
     __shared__ uint32_t tmem_base_s;
     __shared__ uint32_t abort_s;
+    __shared__ float bias_s[kBwdWProducers / 32][8];  // per producer warp: its 8 channels' sums
     uint8_t* smem = reinterpret_cast<uint8_t*>(svo_dsmem);
     const uint32_t sbase = smem_addr(smem);
-    const uint16_t* win = reinterpret_cast<const uint16_t*>(smem);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int W = A.w, H = A.h;
     const size_t n = (size_t)W * H;
@@ -270,7 +270,6 @@ __global__ void __launch_bounds__(kBwdWThreads, 1) k_net_bwd_weight_tc(NetBwdWei
     int my_tiles = 0;
     for (int item = blockIdx.x; item < A.tiles; item += gridDim.x) ++my_tiles;
     const uint32_t n_chunks = (uint32_t)my_tiles * kBwdOutH;
-    float bias_acc = 0.0f;  // producer thread i sums g of output channel i / 32
     uint32_t fault = 0;
 
     if (warp == kBwdWProducers / 32) {
@@ -311,9 +310,38 @@ __global__ void __launch_bounds__(kBwdWThreads, 1) k_net_bwd_weight_tc(NetBwdWei
         __syncwarp();
     } else {
         // ---- the producers
-        const int g_co = warp, g_k = 2 * lane;  // gradient value (channel, 2 positions) of this thread
-        bool stop = false;                      // this thread saw the abort: no more waits
+        // This thread's gradient pair: 16 warps x 32 lanes cover the 16 x 64
+        // chunk, each warp one 8 x 8 block of the B operand's layout (channel
+        // group w >> 3, position group w & 7), so its stores fill 128
+        // contiguous bytes (conflict-free).
+        const int g_co = (warp >> 3) * 8 + (lane >> 2), g_k = (warp & 7) * 8 + (lane & 3) * 2;
+        const int b_idx = (g_co >> 3) * (8 * L::kK) + (g_k >> 3) * 64 + (g_co & 7) * 8 + (g_k & 7);
+        // This thread's im2col items (row (t, ci), 8-position group kc): what
+        // does not depend on the chunk -- the aligned source offset in the
+        // window (a chunk adds its row), how the slice sits in the two
+        // aligned 16-byte reads (word offset 0 or 3, shift 0 or 16 bits), and
+        // where it goes in the operand.
+        constexpr int kItems = L::kRows * (L::kK / 8);
+        constexpr int kMaxIt = (kItems + kBwdWProducers - 1) / kBwdWProducers;
+        uint32_t it_src[kMaxIt], it_dst[kMaxIt], it_sh[kMaxIt];
+        bool it_w3[kMaxIt], it_ok[kMaxIt];
+#pragma unroll
+        for (int k = 0; k < kMaxIt; ++k) {
+            const int it = tid + k * kBwdWProducers;
+            it_ok[k] = it < kItems;
+            const int kc = it / L::kRows, r = it - kc * L::kRows;
+            const int t = r / CIN, ci = r % CIN;
+            const int off = (t / 3 - 1) * kNetTW + (t % 3 - 1);
+            const int e0 = kNetGuard + kc * 8 + off;  // element index in the plane at row 0
+            const int a = e0 & ~7;                    // rows are 64 positions: alignment is the row's
+            it_src[k] = (uint32_t)(ci * L::kWinPlane + a * 2);
+            it_w3[k] = (e0 - a) == 7;                 // the slice starts in the group's last word
+            it_sh[k] = (e0 != a) ? 16u : 0u;
+            it_dst[k] = (uint32_t)((r >> 7) * L::kABytes + kc * 2048 + (r & 127) * 16);
+        }
+        bool stop = false;  // this thread saw the abort: no more waits
         uint32_t c = 0;
+        float bias_acc2 = 0.0f;  // g_co's sum over this thread's positions
         for (int item = blockIdx.x; item < A.tiles; item += gridDim.x) {
             const int ox = (item % A.tiles_x) * kBwdOutW, oy = (item / A.tiles_x) * kBwdOutH;
             const int wx = ox - 1, wy = oy - 1;
@@ -359,7 +387,7 @@ __global__ void __launch_bounds__(kBwdWThreads, 1) k_net_bwd_weight_tc(NetBwdWei
             producers_sync();  // the window is complete
             for (int cr = 0; cr < kBwdOutH; ++cr, ++c) {
                 const uint32_t st = c % S;
-                float gv[2] = {gq[0][0], gq[0][1]};
+                const float g0 = gq[0][0], g1 = gq[0][1];
 #pragma unroll
                 for (int a = 0; a + 1 < kAhead; ++a) {
                     gq[a][0] = gq[a + 1][0];
@@ -374,54 +402,43 @@ __global__ void __launch_bounds__(kBwdWThreads, 1) k_net_bwd_weight_tc(NetBwdWei
                     atomicOr(&abort_s, 1u);
                 if (*(volatile uint32_t*)&abort_s) stop = true;
                 uint8_t* bufp = smem + L::kWin + st * L::kBuf;
-                const int row = cr + 1;  // window row of this chunk's positions
-                // im2col rows (t, ci): 8 positions of channel ci shifted by tap t per
-                // item, consecutive threads on consecutive rows (conflict-free stores).
-                // A slice starts 0, +1 or -1 positions off a 16-byte boundary: two
-                // aligned 16-byte reads and funnel shifts assemble it.
-                for (int it = tid; it < L::kRows * (L::kK / 8); it += kBwdWProducers) {
-                    const int kc = it / L::kRows, r = it - kc * L::kRows;
-                    const int t = r / CIN, ci = r % CIN;
-                    const int off = (t / 3 - 1) * kNetTW + (t % 3 - 1);
-                    const int e0 = kNetGuard + row * kNetTW + kc * 8 + off;  // element index in the plane
-                    const uint32_t* pl = reinterpret_cast<const uint32_t*>(win + ci * (L::kWinPlane / 2));
-                    const int a = e0 & ~7;                                  // aligned 8-element group
-                    const uint4 lo = *reinterpret_cast<const uint4*>(pl + (a >> 1));
+                const uint32_t rofs = (uint32_t)(cr + 1) * (kNetTW * 2);  // this chunk's window row, bytes
+                // im2col: two aligned 16-byte reads and a funnel shift per item
+#pragma unroll
+                for (int k = 0; k < kMaxIt; ++k) {
+                    if (!it_ok[k]) continue;
+                    const uint4 lo = *reinterpret_cast<const uint4*>(smem + it_src[k] + rofs);
+                    const uint4 hi = *reinterpret_cast<const uint4*>(smem + it_src[k] + rofs + 16);
+                    const bool w3 = it_w3[k];
+                    const uint32_t sh = it_sh[k];
                     uint4 v;
-                    if (e0 == a) {
-                        v = lo;
-                    } else {
-                        const uint4 hi = *reinterpret_cast<const uint4*>(pl + (a >> 1) + 4);
-                        const uint32_t w[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
-                        const int wo = ((e0 - a) * 2) >> 2;  // byte offset 2 or 14: words 0 or 3, then 16 bits
-                        v.x = __funnelshift_r(w[wo], w[wo + 1], 16);
-                        v.y = __funnelshift_r(w[wo + 1], w[wo + 2], 16);
-                        v.z = __funnelshift_r(w[wo + 2], w[wo + 3], 16);
-                        v.w = __funnelshift_r(w[wo + 3], w[wo + 4], 16);
-                    }
-                    const int op = r >> 7, rr = r & 127;  // operand and its row
-                    *reinterpret_cast<uint4*>(bufp + op * L::kABytes + kc * 2048 + rr * 16) = v;
+                    v.x = __funnelshift_r(w3 ? lo.w : lo.x, w3 ? hi.x : lo.y, sh);
+                    v.y = __funnelshift_r(w3 ? hi.x : lo.y, w3 ? hi.y : lo.z, sh);
+                    v.z = __funnelshift_r(w3 ? hi.y : lo.z, w3 ? hi.z : lo.w, sh);
+                    v.w = __funnelshift_r(w3 ? hi.z : lo.w, w3 ? hi.w : hi.x, sh);
+                    *reinterpret_cast<uint4*>(bufp + it_dst[k]) = v;
                 }
-                // gradient rows (co): hi and lo parts of 64 positions
+                // gradient pair: hi and lo parts (the B operands), one 32-bit store each
                 {
+                    bias_acc2 += g0 + g1;
+                    uint32_t h0, l0, h1, l1;
+                    split_bf16(g0, h0, l0);
+                    split_bf16(g1, h1, l1);
                     uint16_t* bh = reinterpret_cast<uint16_t*>(bufp + (1 + L::kA1) * L::kABytes);
                     uint16_t* bl = bh + L::kBBytes / 2;
-#pragma unroll
-                    for (int e = 0; e < 2; ++e) {
-                        const int kk = g_k + e;
-                        const float v = gv[e];
-                        bias_acc += v;
-                        uint32_t hi, lo;
-                        split_bf16(v, hi, lo);
-                        const int idx = (g_co >> 3) * (8 * L::kK) + (kk >> 3) * 64 + (g_co & 7) * 8 + (kk & 7);
-                        bh[idx] = (uint16_t)hi;
-                        bl[idx] = (uint16_t)lo;
-                    }
+                    *reinterpret_cast<uint32_t*>(bh + b_idx) = h0 | (h1 << 16);
+                    *reinterpret_cast<uint32_t*>(bl + b_idx) = l0 | (l1 << 16);
                 }
                 fence_async_smem();  // the stores reach the tensor core's view of shared memory
                 mbar_arrive(smem_addr(&full[st]));
             }
         }
+        // biases: the 4 lanes of a channel in this warp, then (below) the 8
+        // warps of its channel group, in a fixed order
+        float s = bias_acc2;
+        s += __shfl_xor_sync(0xffffffffu, s, 1);
+        s += __shfl_xor_sync(0xffffffffu, s, 2);
+        if ((lane & 3) == 0) bias_s[warp][lane >> 2] = s;
     }
     tc_fence_before();
     __syncthreads();
@@ -450,12 +467,11 @@ __global__ void __launch_bounds__(kBwdWThreads, 1) k_net_bwd_weight_tc(NetBwdWei
                     for (int c = 0; c < KIN; ++c) dst[(128 + r) * KIN + c] = v[c];
             }
         }
-        if (warp < kBwdWProducers / 32) {
-            // biases: warp co sums its lanes' partial sums in a fixed order
-            float s = bias_acc;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-            if (lane == 0 && warp < KIN) dst[9 * CIN * KIN + warp] = s;
+        if (tid < KIN) {
+            // channel tid: the 8 warps of its group, in order
+            float s = 0.0f;
+            for (int w = 0; w < 8; ++w) s += bias_s[(tid >> 3) * 8 + w][tid & 7];
+            dst[9 * CIN * KIN + tid] = s;
         }
     } else {
         fault |= kFaultNet;
