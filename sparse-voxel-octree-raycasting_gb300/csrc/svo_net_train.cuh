@@ -196,7 +196,7 @@ struct NetBwdWeightArgs {
 // Rows of the im2col operand: (tap, input channel) pairs, t * cin + ci; the
 // first 128 in one operand, the rest (tap 8 when cin = 16) in a second one
 // whose other rows stay zero.
-constexpr int kBwdWStages = 3;                          // chunk buffers in flight
+constexpr int kBwdWStages = 4;                          // chunk buffers in flight
 constexpr int kBwdWProducers = 512;                     // 16 warps stage the chunks
 constexpr int kBwdWThreads = kBwdWProducers + 32;       // + the warp that issues the MMAs
 template <int CIN>
