@@ -1020,11 +1020,16 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
         # every source pixel's colour + float4 read, one 8-byte atomic per
         # cached point (counted for every pixel: holes are few)
         "k_project": fracs(N * (20.0 + 8.0), stage_ms_learned["project"]),
-        # gather: key read + reset, winner colour + float4 read, plane write;
-        # k_guide: 3x3 halo of colour + float4 (34x10 per 32x8 block), start distance write
-        "k_resolve_gather+k_guide": fracs(N * (8.0 + 8.0 + 20.0 + 20.0) + N * (20.0 * 340.0 / 256.0 + 4.0),
-                                          stage_ms_learned["resolve"]),
     }
+    halo = 340.0 / 256.0  # pixels read per pixel by k_guide's 34x10 halo of a 32x8 block
+    if args.guided:
+        # k_guide<1>: the halo's keys and winning sources' colour + float4, the
+        # block's plane write, the start distance (the tracer clears the keys)
+        stage_rooflines["k_guide (gather fused)"] = fracs(N * ((8.0 + 20.0) * halo + 20.0 + 4.0),
+                                                          stage_ms_learned["resolve"])
+    else:
+        # gather: key read + reset, winner colour + float4 read, plane write
+        stage_rooflines["k_resolve_gather"] = fracs(N * (8.0 + 8.0 + 20.0 + 20.0), stage_ms_learned["resolve"])
     roofline = None
     roofline_net = None
     # rays of one learned frame's trace launch: the requested pixels and the
@@ -1065,7 +1070,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                         **{k: v for k, v in fracs(24.0 * net_pixels, stage_ms_learned["net"]).items()
                            if k in ("achieved_gbs", "l2_frac", "hbm_frac")},
                         "flops_per_launch": flops, "net_pixels_per_launch": net_pixels,
-                        "note": "net stage events: k_net_infer plus the request scan"}
+                        "note": ("net stage events: k_net_infer (its warps append the requests)" if args.guided
+                                 else "net stage events: k_net_infer plus the request scan")}
     if rank == 0:
         like = None
         if cpu:
