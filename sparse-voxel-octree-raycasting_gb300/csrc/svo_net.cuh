@@ -649,29 +649,55 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
         if (c) d1col[threadIdx.x] = t;
         else d1row[threadIdx.x - kGuideBW] = t;
     }
-    for (int i = threadIdx.x; i < kHW * kHH; i += kGuideBW * kGuideBH) {
+    // The halo: with kResolve each thread's (at most two) pixels first load
+    // their keys, then both winning sources, so the two dependent loads of
+    // each chain overlap the other pixel's instead of following them.
+    constexpr int kHalo = kHW * kHH, kPer = (kHalo + kGuideBW * kGuideBH - 1) / (kGuideBW * kGuideBH);
+    uint32_t hc[kPer];
+    float4 hq[kPer];
+    bool hin[kPer];
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+        const int i = threadIdx.x + k * kGuideBW * kGuideBH;
         const int wx = i % kHW, wy = i / kHW;
         const int gx = x0 + wx - 1, gy = y0 + wy - 1;
+        hin[k] = i < kHalo && gx >= 0 && gx < res_x && gy >= 0 && gy < res_y;
+        hc[k] = kEmptyPixel;
+        hq[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (!kResolve && hin[k]) {
+            const size_t o = (size_t)gy * res_x + gx;
+            hc[k] = __ldg(col + o);  // both loads in flight together
+            hq[k] = __ldg(xyz + o);
+        }
+    }
+    if (kResolve) {
+        uint64_t key[kPer];
+#pragma unroll
+        for (int k = 0; k < kPer; ++k) {
+            const int i = threadIdx.x + k * kGuideBW * kGuideBH;
+            const int wx = i % kHW, wy = i / kHW;
+            key[k] = (hin[k] && P->have_cache) ? B.keys[(size_t)(y0 + wy - 1) * res_x + (x0 + wx - 1)] : kKeyEmpty;
+        }
+#pragma unroll
+        for (int k = 0; k < kPer; ++k)
+            if (key[k] != kKeyEmpty) hc[k] = resolve_source(P, B, key[k], hq[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < kPer; ++k) {
+        const int i = threadIdx.x + k * kGuideBW * kGuideBH;
+        if (i >= kHalo) break;
+        const int wx = i % kHW, wy = i / kHW;
         float d = INFINITY;
         uint8_t h = 0;
         uint32_t cc = kEmptyPixel;
         float4 cq = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
-        if (gx >= 0 && gx < res_x && gy >= 0 && gy < res_y) {
-            const size_t o = (size_t)gy * res_x + gx;
-            uint32_t c;
-            float4 q;
-            if (kResolve) {
-                const uint64_t key = P->have_cache ? B.keys[o] : kKeyEmpty;
-                c = kEmptyPixel;
-                q = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                if (key != kKeyEmpty) c = resolve_source(P, B, key, q);
-                if (wx >= 1 && wx <= kGuideBW && wy >= 1 && wy <= kGuideBH) {  // the block's own pixel
-                    plane_col(B, P->cur)[o] = c;
-                    if (c != kEmptyPixel) plane_xyz(B, P->cur)[o] = q;
-                }
-            } else {
-                c = __ldg(col + o);  // both loads in flight together
-                q = __ldg(xyz + o);
+        if (hin[k]) {
+            const uint32_t c = hc[k];
+            const float4 q = hq[k];
+            if (kResolve && wx >= 1 && wx <= kGuideBW && wy >= 1 && wy <= kGuideBH) {  // the block's own pixel
+                const size_t o = (size_t)(y0 + wy - 1) * res_x + (x0 + wx - 1);
+                plane_col(B, P->cur)[o] = c;
+                if (c != kEmptyPixel) plane_xyz(B, P->cur)[o] = q;
             }
             // exact IEEE operations, so the CPU oracle finds the same start distances
             const float ax = __fsub_rn(q.x, cx), ay = __fsub_rn(q.y, cy), az = __fsub_rn(q.z, cz);
