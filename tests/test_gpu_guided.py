@@ -9,7 +9,9 @@ their 3x3 neighbourhood are walked from just in front of it.
   raycast's colour;
 * the start distances are conservative for nearly every pixel (in front of
   the pixel's true hit);
-* the frames stay close to the full raycast of the same view.
+* the frames stay close to the full raycast of the same view;
+* the gather inside k_guide (the default) and the separate gather (with the
+  training tap on) give the same frames, switching between them mid-run.
 """
 import os
 
