@@ -35,7 +35,7 @@ oracle port of kernel.cl/raycast.h), with all host threads, on scenes and
 cameras from oracle/scene_gen.py: that process never loads the product library.
 
 --profile-case NAME runs one small fixed workload for a profiler capture and
-exits (learned, guided, plain, full, build, config1, train).
+exits (learned, guided, plain, full, build, full512, train).
 
 Multi-GPU: replicas only (the per-frame pipeline does not shard); each rank
 renders its own camera path on its own GPU, scaling "weak".
@@ -62,7 +62,7 @@ WORKLOAD = ("warped + learned pipeline 1920x1024 (guided walks from the reprojec
             "unguided pixels), depth-11 terrain octree, 256-frame orbit (0.5 deg/frame), confidence threshold 0.5")
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 TRACE_PROFILE = "profiles/k_trace_warp_guided_1920x1024_depth11.md"
-PROFILE_CASES = ("learned", "guided", "plain", "full", "build", "config1", "train")
+PROFILE_CASES = ("learned", "guided", "plain", "full", "build", "full512", "train")
 
 
 def parse_args(argv=None):
@@ -494,7 +494,7 @@ def measure_training(svo, torch, args, device, W=1920, H=1024, steps=6):
             "note": "tensor-core forward and backward convolutions; gradients enter the MMAs as two bf16 parts"}
 
 
-def measure_config1(svo, torch, device, seed, no_cpu: bool, steps: int = 20):
+def measure_full_512(svo, torch, device, seed, no_cpu: bool, steps: int = 20):
     """The plain full raycast configuration: 512x512, depth-9 (512^3) solid
     terrain (the GPU builder from the seeded voxels), one camera at 1.5x
     extent looking at the centre, 60 degree vertical field of view."""
@@ -555,7 +555,7 @@ def run_profile_case(case: str) -> None:
     learned / guided: 8 learned warp frames (committed weights, threshold
     0.5, orbit) without / with guided walks; plain: 8 plain warp frames;
     full: 4 full raycasts; build: 2 GPU octree builds of the benchmark
-    terrain's voxels (all 1920x1024, depth-11 benchmark terrain); config1: 4
+    terrain's voxels (all 1920x1024, depth-11 benchmark terrain); full512: 4
     full raycasts of the 512x512 depth-9 solid-terrain configuration; train:
     3 training steps of the net at 1920x1024 on seeded features."""
     sys.path.insert(0, PKG)
@@ -580,17 +580,17 @@ def run_profile_case(case: str) -> None:
         net.close()
         ctx.close()
         return
-    if case in ("build", "config1"):
+    if case in ("build", "full512"):
         import torch
 
-        depth = 9 if case == "config1" else DEPTH
+        depth = 9 if case == "full512" else DEPTH
         x, y, z, c = svo.terrain_voxels(SEED, depth, case == "build")
         dev = [torch.from_numpy(np.ascontiguousarray(a, np.uint32).view(np.int32)).cuda() for a in (x, y, z, c)]
         torch.cuda.synchronize()
         ctx = svo.Context(0)
         for _ in range(2 if case == "build" else 1):
             ctx.build_octree(*(t.data_ptr() for t in dev), len(x), depth)
-        if case == "config1":
+        if case == "full512":
             t = ctx.target(512, 512)
             for _ in range(4):
                 ctx.raycast_full(t, svo.camera_path(0, depth, 0, 512, 512, fov=1.1547))
@@ -994,7 +994,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
 
     extras = {}
     if args.extras and rank == 0:
-        extras["config1"] = measure_config1(svo, torch, device, args.seed, args.no_cpu)
+        extras["full_raycast_512x512_depth9"] = measure_full_512(svo, torch, device, args.seed, args.no_cpu)
         extras["net_training"] = measure_training(svo, torch, args, device)
         extras["octree_builder"] = measure_builder(svo, torch, octree, depth, args.seed, device)
         extras["batch_64_views"] = measure_batch(svo, torch, ctx, depth, device)
