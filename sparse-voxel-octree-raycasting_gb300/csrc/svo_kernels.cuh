@@ -208,18 +208,22 @@ __global__ void __launch_bounds__(256) k_project(const FrameParams* __restrict__
             const uint32_t t = (uint32_t)sy * (uint32_t)res_x + (uint32_t)sx;
             atomicMin((unsigned long long*)(B.keys + t), (unsigned long long)(((uint64_t)(sz | (uint32_t)r) << 32) | s));
         };
-        // two sources per thread and iteration, their loads in flight together
+        // four sources per thread and iteration, their loads in flight together
         // (the atomicMin outcome does not depend on the order)
+        constexpr int kPer = 4;
         const uint32_t stride = gridDim.x * blockDim.x;
-        for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += 2u * stride) {
-            const uint32_t s2 = s + stride;
-            const bool two = s2 < N;
-            const uint32_t c1 = col[s];
-            const float4 q1 = __ldg(xyz + s);
-            const uint32_t c2 = two ? col[s2] : kEmptyPixel;
-            const float4 q2 = two ? __ldg(xyz + s2) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            project_one(s, c1, q1);
-            if (two) project_one(s2, c2, q2);
+        for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < N; s += kPer * stride) {
+            uint32_t c[kPer];
+            float4 q[kPer];
+#pragma unroll
+            for (int k = 0; k < kPer; ++k) {
+                const uint32_t sk = s + (uint32_t)k * stride;
+                const bool in = sk < N;
+                c[k] = in ? col[sk] : kEmptyPixel;
+                q[k] = in ? __ldg(xyz + sk) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            }
+#pragma unroll
+            for (int k = 0; k < kPer; ++k) project_one(s + (uint32_t)k * stride, c[k], q[k]);
         }
     }
 }
