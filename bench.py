@@ -27,7 +27,10 @@ Timing: each step is bracketed by CUDA events on the library's stream; the L2
 is flushed (256 MiB device write) before every timed step and outside its
 events. `value` = frames of all ranks / max over ranks of the summed step
 times. `e2e` times the C-ABI calls a user makes with host buffers: camera in,
-svo_warp_frame_learned, BGRX8 image out to pinned host memory, per step.
+svo_warp_frame_learned, BGRX8 image out to pinned host memory -- pipelined
+(svo_read_bgrx_async: each image's copy overlaps the next frame's first
+kernels; host wall time less the L2 flushes), with the blocking readback's
+figure beside it.
 
 --impl reference times the reference algorithm on the host CPU cores instead
 (oracle/_ref when it was compiled from the reference tree here, else the
@@ -341,13 +344,17 @@ def measure_batch(svo, torch, ctx, depth, device, n_views=64, steps=8):
 def streams_timed(torch, ctxs, go, frames, first, device, flush=None):
     """Device time of `frames` steps in which every context renders one frame
     on its own stream: a start event on the first stream that every other
-    stream waits for, an end event per stream, the step's time the latest end."""
+    stream waits for, an end event per stream, the step's time the latest end.
+    The host enqueues every step before reading the events (the first stream
+    waits for all ends of a step before the next one starts), so no host
+    launch latency falls inside a step; `flush(stream)` enqueues the L2 flush
+    ahead of a step's start event."""
     exts = [torch.cuda.ExternalStream(c.stream, device=device) for c in ctxs]
-    total = 0.0
+    steps = []
     for i in range(frames):
         f = first + i
         if flush is not None:
-            flush()
+            flush(exts[0])
         start = torch.cuda.Event(enable_timing=True)
         start.record(exts[0])
         for e in exts[1:]:
@@ -358,10 +365,12 @@ def streams_timed(torch, ctxs, go, frames, first, device, flush=None):
             ev = torch.cuda.Event(enable_timing=True)
             ev.record(exts[k])
             ends.append(ev)
-        for ev in ends:
-            ev.synchronize()
-        total += max(start.elapsed_time(ev) for ev in ends)
-    return total
+        for ev in ends[1:]:
+            exts[0].wait_event(ev)
+        steps.append((start, ends))
+    for ev in steps[-1][1]:
+        ev.synchronize()
+    return sum(max(start.elapsed_time(ev) for ev in ends) for start, ends in steps)
 
 
 def measure_large(svo, torch, args, device, frames=16, views=8):
@@ -515,16 +524,17 @@ def measure_full_512(svo, torch, device, seed, no_cpu: bool, steps: int = 20):
     for _ in range(3):
         ctx.raycast_full(tgt, view)
     ctx.synchronize()
-    ms = []
+    evs = []
     for _ in range(steps):
-        flush.zero_()
-        torch.cuda.synchronize(device)
+        with torch.cuda.stream(ext):  # the flush on the launch's stream: no host latency inside the events
+            flush.zero_()
         s_ev, e_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s_ev.record(ext)
         ctx.raycast_full(tgt, view)
         e_ev.record(ext)
-        e_ev.synchronize()
-        ms.append(s_ev.elapsed_time(e_ev))
+        evs.append((s_ev, e_ev))
+    ctx.synchronize()
+    ms = [s_ev.elapsed_time(e_ev) for s_ev, e_ev in evs]
     t_ms = float(np.mean(ms))
     out = {"workload": "plain full raycast 512x512, depth-9 solid terrain, 60 deg vertical FOV, one camera",
            "voxels": int(n), "ms_per_frame": t_ms, "mrays_per_s": W * H / t_ms / 1e3,
@@ -673,6 +683,13 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
         flush.zero_()
         torch.cuda.synchronize(device)
 
+    def flush_on_stream():
+        # the L2 flush enqueued on the frames' stream ahead of the next step's
+        # start event: the host keeps enqueueing, so each step's events time
+        # the device work only (no host launch latency inside them)
+        with torch.cuda.stream(ext):
+            flush.zero_()
+
     def new_target(guided=None):
         t = ctx.target(W, H)
         if args.graph:
@@ -698,7 +715,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
         for i in range(args.steps):
             f = args.warmup + i
             v = view(f, kind)
-            flush_l2()
+            flush_on_stream()
             starts[i].record(ext)
             render(f, v)
             ends[i].record(ext)
@@ -719,7 +736,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     for i in range(args.steps):
         f = args.warmup + i
         v = view(f)
-        flush_l2()
+        flush_on_stream()
         starts[i].record(ext)
         ctx.warp_frame_learned(tgt_l, v, f, net, thr)
         ends[i].record(ext)
@@ -765,18 +782,18 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     t_sl.close()
 
     # ---- plain full raycast of the same frames
-    full_ms = []
+    full_ev = []
     for i in range(args.steps):
         f = args.warmup + i
         v = view(f)
-        flush_l2()
+        flush_on_stream()
         s_ev, e_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s_ev.record(ext)
         ctx.raycast_full(full, v)
         e_ev.record(ext)
-        e_ev.synchronize()
-        full_ms.append(s_ev.elapsed_time(e_ev))
+        full_ev.append((s_ev, e_ev))
     ctx.synchronize()
+    full_ms = [s_ev.elapsed_time(e_ev) for s_ev, e_ev in full_ev]
     full_fps = 1000.0 / statistics.mean(full_ms)
     mrays_full = N * full_fps / 1e6
 
@@ -786,15 +803,47 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
     for f in range(args.warmup):
         ctx.warp_frame_learned(tgt3, view(f), f, net, thr)
         tgt3.bgrx_into(host_img)
-    e2e_s = 0.0
+    # blocking: every frame's image read back before the next frame is issued
+    e2e_block_s = 0.0
     for i in range(args.steps):
         f = args.warmup + i
         flush_l2()
         t0 = time.perf_counter()
         ctx.warp_frame_learned(tgt3, view(f), f, net, thr)  # camera host -> device inside the call
         tgt3.bgrx_into(host_img)                              # BGRX8 frame device -> pinned host, synchronising
-        e2e_s += time.perf_counter() - t0
-    e2e_value, _ = aggregate(args.steps, e2e_s, world, device if world > 1 else None)
+        e2e_block_s += time.perf_counter() - t0
+    e2e_block, _ = aggregate(args.steps, e2e_block_s, world, device if world > 1 else None)
+    # pipelined, as an application renders: frame i's image is copied to pinned
+    # host memory (svo_read_bgrx_async) while frame i + 1 renders -- the copy is
+    # issued after the L2 flush that precedes frame i + 1, so it overlaps that
+    # frame's first kernels and not the flush; the flushes (device events on the
+    # frames' stream) are not counted; the last image is waited for
+    hosts = [torch.empty(N, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32) for _ in range(2)]
+    base = args.warmup + args.steps  # the orbit continues where the blocking loop stopped
+    for i in range(args.warmup):  # the graph with the copy's wait node is captured here
+        f = base + i
+        ctx.warp_frame_learned(tgt3, view(f), f, net, thr)
+        tgt3.bgrx_into_async(hosts[i % 2])
+    tgt3.readback_wait()
+    ctx.synchronize()
+    fl_s = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    fl_e = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        f = base + args.warmup + i
+        with torch.cuda.stream(ext):
+            fl_s[i].record(ext)
+            flush.zero_()
+            fl_e[i].record(ext)
+        if i > 0:
+            tgt3.bgrx_into_async(hosts[(i - 1) % 2])  # frame f - 1's image, behind this flush
+        ctx.warp_frame_learned(tgt3, view(f), f, net, thr)
+    tgt3.bgrx_into_async(hosts[(args.steps - 1) % 2])
+    tgt3.readback_wait()
+    t1 = time.perf_counter()
+    ctx.synchronize()
+    flush_s = sum(fl_s[i].elapsed_time(fl_e[i]) for i in range(args.steps)) / 1e3
+    e2e_value, _ = aggregate(args.steps, (t1 - t0) - flush_s, world, device if world > 1 else None)
     tgt3.close()
 
     # ---- quality over fixed windows against the full raycast of the same cameras
@@ -908,6 +957,10 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
         def mv_view(k, f):
             return svo.camera_path(1, depth, frame_offset + 37 * k + f, W, H)
 
+        def flush_stream(st):
+            with torch.cuda.stream(st):
+                flush.zero_()
+
         multiview = {"views": args.views,
                      "timing": "device events: a start event every stream waits for, the latest stream's end "
                                "event, L2 flushed before every step"}
@@ -922,7 +975,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                     go(k, f)
             for c in ctxs:
                 c.synchronize()
-            mv_ms = streams_timed(torch, ctxs, go, args.steps, args.warmup, device, flush_l2)
+            mv_ms = streams_timed(torch, ctxs, go, args.steps, args.warmup, device, flush_stream)
             multiview[mode] = {"frames_per_s": args.views * args.steps / (mv_ms * 1e-3),
                                "ms_per_step": mv_ms / args.steps}
         for t in tgts:
@@ -1092,7 +1145,12 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
                        "l2": "flushed before every timed step (256 MiB device write, outside the step events)",
                        "cuda_graph": bool(args.graph), "replicas": world},
             "e2e": {"value": e2e_value, "unit": "frames/s", "h2d_bytes_per_step": 4 * 33,
-                    "d2h_bytes_per_step": 4 * N},
+                    "d2h_bytes_per_step": 4 * N,
+                    "how": "svo_warp_frame_learned (camera in) then svo_read_bgrx_async of each BGRX8 frame into "
+                           "pinned host memory, overlapping the next frame's first kernels; host wall time of the "
+                           "steps until the last image is on the host, less the L2 flushes between frames",
+                    "blocking": {"value": e2e_block,
+                                 "how": "svo_read_bgrx after every frame (the frame and its copy serialised)"}},
             "gpu_launches": int(launches),
             "clocks": clock_info,
             "roofline": roofline,

@@ -259,6 +259,17 @@ svo_status svo_read_coords(svo_target* t, int plane, float* host);
 svo_status svo_read_holes(svo_target* t, uint32_t* host, size_t cap_words, uint32_t* count);
 /* The BGRX8 image of the last frame (warped or full). */
 svo_status svo_read_bgrx(svo_target* t, uint32_t* host);
+/* Asynchronous BGRX readback (no reference counterpart; replaces the blocking
+ * PBO readback of src/raycast.h:425-441 for hosts that pipeline frames):
+ * enqueues the copy of the target's last image into `host` (res_x*res_y words;
+ * pinned host memory, or the copy is not asynchronous) on the target's own
+ * copy stream and returns at once. The next frame renders meanwhile; its first
+ * write to the image (the net, the certified pixels, the filter or a full
+ * raycast) waits for the copy. `host` must stay valid, and untouched, until
+ * svo_target_readback_wait returns. */
+svo_status svo_read_bgrx_async(svo_target* t, uint32_t* host);
+/* Returns when the target's last asynchronous readback is complete. */
+svo_status svo_target_readback_wait(svo_target* t);
 /* Outputs of the last svo_raycast_full on this target. */
 svo_status svo_read_full(svo_target* t, uint32_t* colour, float* xyzw);
 /* Packed hit voxel of the last full raycast: bits 0-15 x, 16-31 y, 32-47 z

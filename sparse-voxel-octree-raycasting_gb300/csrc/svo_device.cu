@@ -69,6 +69,7 @@ struct FrameGraph {
     float* tap = nullptr;
     bool coarse = false;
     bool guided = false;
+    bool readback = false;
     uint64_t config_gen = 0;
     void reset() {
         if (exec) cudaGraphExecDestroy(exec);
@@ -119,6 +120,12 @@ struct svo_target {
     cudaEvent_t ev[8] = {};
     int n_events = 0;
     int last_mode = 0;  // 1 warp, 2 full, 3 learned warp
+    // asynchronous BGRX readback: the copy runs on the target's own stream
+    // while the next frame renders; that frame's first write to the image
+    // waits for it (readback_guard)
+    bool async_readback = false;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t frame_done = nullptr, copy_done = nullptr;
 };
 
 // The reconstruction net: FP32 master parameters with Adam moments, their
@@ -403,6 +410,14 @@ inline unsigned grid_for(size_t n, int threads, int sm_count) {
     return (unsigned)std::max<size_t>(1, std::min<size_t>((n + threads - 1) / threads, (size_t)sm_count * 32));
 }
 
+// Before a frame's first write to the BGRX image: wait for the asynchronous
+// readback of the previous image (a no-op until svo_read_bgrx_async is used;
+// a wait node in a captured graph).
+void readback_guard(svo_target* t) {
+    if (!t->async_readback || !t->copy_done) return;
+    cudaStreamWaitEvent(t->ctx->stream, t->copy_done, t->capturing ? cudaEventWaitExternal : 0);
+}
+
 void record(svo_target* t, int i) {
     if (!t->profiling) return;
     if (t->capturing)
@@ -549,6 +564,7 @@ svo_status enqueue_warp_body(svo_context* ctx, svo_target* t) {
     svo_status st = launch_trace_warp(ctx, t);
     if (st != SVO_OK) return st;
     record(t, 5);
+    readback_guard(t);
     k_fill_colorize<<<dim3((res_x + 31) / 32, (res_y + 7) / 8), 256, 0, s>>>(t->d_params, t->B);
     SVO_LAUNCHED(ctx);
     record(t, 6);
@@ -600,6 +616,8 @@ svo_status enqueue_learned_body(svo_context* ctx, svo_target* t, const svo_net* 
         SVO_LAUNCHED(ctx);
     }
     record(t, 1);
+    const bool certified = t->B.guide && t->certify;  // k_guide writes certified pixels' BGRX
+    if (certified) readback_guard(t);
     const dim3 guide_grid((res_x + kGuideBW - 1) / kGuideBW, (res_y + kGuideBH - 1) / kGuideBH);
     if (guided_resolve(t, true)) {
         // the gather happens inside k_guide; the tracer clears the keys
@@ -625,6 +643,7 @@ svo_status enqueue_learned_body(svo_context* ctx, svo_target* t, const svo_net* 
         }
     }
     record(t, 2);
+    if (!certified) readback_guard(t);  // the net writes the BGRX of the pixels it fills
     NetInferArgs A{};
     A.P = t->d_params;
     A.B = t->B;
@@ -660,7 +679,8 @@ svo_status run_frame(svo_context* ctx, svo_target* t, const FrameParams& p, Fram
         return body();
     }
     if (!g.exec || g.profiled != t->profiling || g.net != net || g.threshold != threshold || g.tap != t->feature_tap ||
-        g.coarse != t->coarse || g.guided != t->guided || g.config_gen != ctx->config_gen) {
+        g.coarse != t->coarse || g.guided != t->guided || g.readback != t->async_readback ||
+        g.config_gen != ctx->config_gen) {
         g.reset();
         const uint64_t l0 = ctx->launches;
         SVO_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
@@ -699,6 +719,7 @@ svo_status run_frame(svo_context* ctx, svo_target* t, const FrameParams& p, Fram
         g.tap = t->feature_tap;
         g.coarse = t->coarse;
         g.guided = t->guided;
+        g.readback = t->async_readback;
         g.config_gen = ctx->config_gen;
     }
     cudaKernelNodeParams kp;
@@ -1395,6 +1416,12 @@ svo_status svo_target_destroy(svo_target* t) {
     svo_context* ctx = t->ctx;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    if (t->copy_stream) {
+        cudaStreamSynchronize(t->copy_stream);
+        cudaStreamDestroy(t->copy_stream);
+    }
+    if (t->frame_done) cudaEventDestroy(t->frame_done);
+    if (t->copy_done) cudaEventDestroy(t->copy_done);
     for (auto& g : t->graphs) g.reset();
     void* ptrs[] = {t->B.col[0], t->B.col[1], t->B.col[2], t->B.xyz[0], t->B.xyz[1], t->B.xyz[2], t->B.disp, t->B.bgrx, t->B.keys, t->B.ids,
                     t->B.tile_mask, t->B.counters, t->d_params, t->full_col, t->full_xyzw, t->full_vox,
@@ -1500,6 +1527,7 @@ svo_status svo_raycast_full_batch(svo_context* ctx, svo_target* const* targets, 
         cudaEventRecord(t0->ev[0], ctx->stream);
     }
     SVO_CUDA(ctx, cudaMemcpyAsync(ctx->d_batch[slot], hb, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    for (int i = 0; i < n; ++i) readback_guard(targets[i]);
     k_reset_counter<<<1, 1, 0, ctx->stream>>>(ctx->d_counter);
     SVO_LAUNCHED(ctx);
     svo_status st = launch_trace_full(ctx, ctx->d_batch[slot]);
@@ -1988,6 +2016,30 @@ svo_status svo_read_holes(svo_target* t, uint32_t* host, size_t cap_words, uint3
 svo_status svo_read_bgrx(svo_target* t, uint32_t* host) {
     if (!t) return SVO_ERR_INVALID_ARGUMENT;
     return read_back(t, host, t->B.bgrx, t->N * 4);
+}
+
+svo_status svo_read_bgrx_async(svo_target* t, uint32_t* host) {
+    if (!t || !host) return SVO_ERR_INVALID_ARGUMENT;
+    svo_context* ctx = t->ctx;
+    SVO_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (!t->copy_stream) {
+        SVO_CUDA(ctx, cudaStreamCreateWithFlags(&t->copy_stream, cudaStreamNonBlocking));
+        SVO_CUDA(ctx, cudaEventCreateWithFlags(&t->frame_done, cudaEventDisableTiming));
+        SVO_CUDA(ctx, cudaEventCreateWithFlags(&t->copy_done, cudaEventDisableTiming));
+    }
+    // the next frame's graph gains the wait on this copy (captured once)
+    t->async_readback = true;
+    SVO_CUDA(ctx, cudaEventRecord(t->frame_done, ctx->stream));
+    SVO_CUDA(ctx, cudaStreamWaitEvent(t->copy_stream, t->frame_done, 0));
+    SVO_CUDA(ctx, cudaMemcpyAsync(host, t->B.bgrx, t->N * 4, cudaMemcpyDeviceToHost, t->copy_stream));
+    SVO_CUDA(ctx, cudaEventRecord(t->copy_done, t->copy_stream));
+    return SVO_OK;
+}
+
+svo_status svo_target_readback_wait(svo_target* t) {
+    if (!t) return SVO_ERR_INVALID_ARGUMENT;
+    if (t->copy_done) SVO_CUDA(t->ctx, cudaEventSynchronize(t->copy_done));
+    return SVO_OK;
 }
 
 svo_status svo_read_full(svo_target* t, uint32_t* colour, float* xyzw) {

@@ -40,7 +40,8 @@ EXPORTS = [
     "svo_launch_count", "svo_context_set_option", "svo_octree_upload", "svo_octree_upload_device", "svo_octree_set_l2_window",
     "svo_target_create", "svo_target_destroy", "svo_raycast_full", "svo_raycast_full_batch", "svo_warp_frame",
     "svo_target_use_graph", "svo_target_set_profiling", "svo_target_stage_times", "svo_read_colour",
-    "svo_read_coords", "svo_read_holes", "svo_read_bgrx", "svo_read_full", "svo_read_voxels",
+    "svo_read_coords", "svo_read_holes", "svo_read_bgrx", "svo_read_bgrx_async", "svo_target_readback_wait",
+    "svo_read_full", "svo_read_voxels",
     "svo_target_device_outputs", "svo_builder_create", "svo_builder_destroy", "svo_builder_set_voxel",
     "svo_builder_set_voxels", "svo_builder_finish", "svo_builder_copy_words", "svo_builder_stats",
     "svo_octree_save", "svo_octree_load_header", "svo_octree_load_words", "svo_terrain_build",
@@ -145,6 +146,8 @@ def load(path: str | None = None) -> ctypes.CDLL:
         "svo_read_coords": (i, [_P, i, _P]),
         "svo_read_holes": (i, [_P, _P, sz, ctypes.POINTER(u32)]),
         "svo_read_bgrx": (i, [_P, _P]),
+        "svo_read_bgrx_async": (i, [_P, _P]),
+        "svo_target_readback_wait": (i, [_P]),
         "svo_read_full": (i, [_P, _P, _P]),
         "svo_read_voxels": (i, [_P, _P]),
         "svo_target_device_outputs": (i, [_P, ctypes.POINTER(DeviceOutputs)]),
@@ -517,6 +520,14 @@ class Target:
 
     def bgrx_into(self, out: np.ndarray) -> None:
         _check(self._lib.svo_read_bgrx(self._h, _ptr(out)), self.ctx)
+
+    def bgrx_into_async(self, out: np.ndarray) -> None:
+        """svo_read_bgrx_async: the copy overlaps the next frame; `out` (pinned)
+        is complete after readback_wait()."""
+        _check(self._lib.svo_read_bgrx_async(self._h, _ptr(out)), self.ctx)
+
+    def readback_wait(self) -> None:
+        _check(self._lib.svo_target_readback_wait(self._h), self.ctx)
 
     def full(self) -> tuple[np.ndarray, np.ndarray]:
         col = np.empty(self.n, np.uint32)

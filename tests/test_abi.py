@@ -51,6 +51,8 @@ def test_null_handles_are_rejected(svo):
     assert lib.svo_read_guide(None, None) == 1
     assert lib.svo_context_autotune_learned(None, None, None, 0, None, 0.5, None, 0, None) == 1
     assert lib.svo_context_set_option(None, svo.OPT_LEARNED_PACKET_WIDTH, 8) == 1
+    assert lib.svo_read_bgrx_async(None, None) == 1
+    assert lib.svo_target_readback_wait(None) == 1
 
 
 def test_look_at_rows_are_orthonormal_and_aim(svo):

@@ -51,6 +51,48 @@ def test_graph_replay_matches_direct_launches(svo, scene, gpu_ctx):
 
 
 @pytest.mark.parametrize("graph", [False, True])
+def test_async_readback_matches_blocking_readback(svo, scene, gpu_ctx, graph):
+    # svo_read_bgrx_async: each image copied while the next frame renders (the
+    # frame's first write to the image waits for the copy) equals the image a
+    # blocking readback of a twin target returns -- guided learned frames
+    # (the net writes the image), plain warp frames (the filter) and full
+    # raycasts, interleaved on the same targets
+    torch = pytest.importorskip("torch")
+    octree = scene(9, 77, True)
+    gpu_ctx.upload(octree)
+    net = gpu_ctx.net()
+    net.load_file(os.path.join(os.path.dirname(svo.__file__), "net_weights.npy"))
+    W, H = 160, 96
+    a, b = gpu_ctx.target(W, H), gpu_ctx.target(W, H)
+    for t in (a, b):
+        t.use_graph(graph)
+        t.set_guided(True)
+    hosts = [torch.empty(W * H, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32) for _ in range(3)]
+    want = []
+    for f in range(12):
+        v = svo.camera_path(2, 9, f, W, H)
+        kind = f % 4
+        for t in (a, b):
+            if kind == 3:
+                gpu_ctx.raycast_full(t, v)
+            elif kind == 2:
+                gpu_ctx.warp_frame(t, v, f)
+            else:
+                gpu_ctx.warp_frame_learned(t, v, f, net, 0.5)
+        a.bgrx_into_async(hosts[f % 3])
+        want.append(b.bgrx())  # blocking
+        if f >= 2:  # the copy of frame f - 2 is done once the one of f - 1 is (same stream)
+            a.readback_wait()
+            assert np.array_equal(hosts[(f - 2) % 3], want[f - 2]), f - 2
+    a.readback_wait()
+    for f in (10, 11):
+        assert np.array_equal(hosts[f % 3], want[f]), f
+    a.close()
+    b.close()
+    net.close()
+
+
+@pytest.mark.parametrize("graph", [False, True])
 def test_stage_timing(svo, scene, gpu_ctx, graph):
     octree = scene(8, 99, True)
     gpu_ctx.upload(octree)
