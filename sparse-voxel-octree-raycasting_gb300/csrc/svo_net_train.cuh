@@ -150,12 +150,33 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_net_bwd_data_tc(NetBwdDataAr
             }
             tc_commit(smem_addr(&mbar[warp]));
         }
+        // While the MMAs run: the ReLU masks of this thread's output positions
+        // (act > 0 per channel, one bit each), so the read-back below only waits
+        // for tensor memory.
+        constexpr int kMine = (kBwdBlocks + kNetWarps / 4 - 1) / (kNetWarps / 4);
+        uint32_t relu[kMine];
+        const int g = warp & 3;
+#pragma unroll
+        for (int k = 0; k < kMine; ++k) {
+            const int j = (warp >> 2) + k * (kNetWarps / 4);
+            relu[k] = 0u;
+            const int p = kNetTW + 128 * j + 32 * g + lane;
+            const int col = p & (kNetTW - 1);
+            const int gx = wx + col, gy = wy + (p >> 6);
+            if (j < kBwdBlocks && col >= 1 && col <= kBwdOutW && gx < W && gy < H) {
+                const size_t o = (size_t)gy * W + gx;
+#pragma unroll
+                for (int c = 0; c < 16; ++c) relu[k] |= (__ldg(A.act + c * n + o) > 0.0f ? 1u : 0u) << c;
+            }
+        }
         const bool ready = mbar_wait_phase(bar, phase);
         phase ^= 1u;
         tc_fence_after();
         if (ready) {
-            const int g = warp & 3;
-            for (int j = warp >> 2; j < kBwdBlocks; j += kNetWarps / 4) {
+#pragma unroll
+            for (int k = 0; k < kMine; ++k) {
+                const int j = (warp >> 2) + k * (kNetWarps / 4);
+                if (j >= kBwdBlocks) continue;
                 float v[16];
                 tc_ld16(tmem + ((uint32_t)(32 * g) << 16) + 16u * j, v);
                 const int p = kNetTW + 128 * j + 32 * g + lane;
@@ -164,7 +185,7 @@ __global__ void __launch_bounds__(kBwdThreads, 1) k_net_bwd_data_tc(NetBwdDataAr
                 if (col >= 1 && col <= kBwdOutW && gx < W && gy < H) {
                     const size_t o = (size_t)gy * W + gx;
 #pragma unroll
-                    for (int c = 0; c < 16; ++c) A.g_in[c * n + o] = __ldg(A.act + c * n + o) > 0.0f ? v[c] : 0.0f;
+                    for (int c = 0; c < 16; ++c) A.g_in[c * n + o] = ((relu[k] >> c) & 1u) ? v[c] : 0.0f;
                 }
             }
         }
