@@ -413,9 +413,10 @@ inline unsigned grid_for(size_t n, int threads, int sm_count) {
 // Before a frame's first write to the BGRX image: wait for the asynchronous
 // readback of the previous image (a no-op until svo_read_bgrx_async is used;
 // a wait node in a captured graph).
-void readback_guard(svo_target* t) {
-    if (!t->async_readback || !t->copy_done) return;
-    cudaStreamWaitEvent(t->ctx->stream, t->copy_done, t->capturing ? cudaEventWaitExternal : 0);
+svo_status readback_guard(svo_target* t) {
+    if (!t->async_readback || !t->copy_done) return SVO_OK;
+    SVO_CUDA(t->ctx, cudaStreamWaitEvent(t->ctx->stream, t->copy_done, t->capturing ? cudaEventWaitExternal : 0));
+    return SVO_OK;
 }
 
 void record(svo_target* t, int i) {
@@ -564,7 +565,7 @@ svo_status enqueue_warp_body(svo_context* ctx, svo_target* t) {
     svo_status st = launch_trace_warp(ctx, t);
     if (st != SVO_OK) return st;
     record(t, 5);
-    readback_guard(t);
+    if (svo_status gs = readback_guard(t); gs != SVO_OK) return gs;
     k_fill_colorize<<<dim3((res_x + 31) / 32, (res_y + 7) / 8), 256, 0, s>>>(t->d_params, t->B);
     SVO_LAUNCHED(ctx);
     record(t, 6);
@@ -617,7 +618,9 @@ svo_status enqueue_learned_body(svo_context* ctx, svo_target* t, const svo_net* 
     }
     record(t, 1);
     const bool certified = t->B.guide && t->certify;  // k_guide writes certified pixels' BGRX
-    if (certified) readback_guard(t);
+    if (certified) {
+        if (svo_status gs = readback_guard(t); gs != SVO_OK) return gs;
+    }
     const dim3 guide_grid((res_x + kGuideBW - 1) / kGuideBW, (res_y + kGuideBH - 1) / kGuideBH);
     if (guided_resolve(t, true)) {
         // the gather happens inside k_guide; the tracer clears the keys
@@ -643,7 +646,9 @@ svo_status enqueue_learned_body(svo_context* ctx, svo_target* t, const svo_net* 
         }
     }
     record(t, 2);
-    if (!certified) readback_guard(t);  // the net writes the BGRX of the pixels it fills
+    if (!certified) {  // the net writes the BGRX of the pixels it fills
+        if (svo_status gs = readback_guard(t); gs != SVO_OK) return gs;
+    }
     NetInferArgs A{};
     A.P = t->d_params;
     A.B = t->B;
@@ -1527,7 +1532,8 @@ svo_status svo_raycast_full_batch(svo_context* ctx, svo_target* const* targets, 
         cudaEventRecord(t0->ev[0], ctx->stream);
     }
     SVO_CUDA(ctx, cudaMemcpyAsync(ctx->d_batch[slot], hb, bytes, cudaMemcpyHostToDevice, ctx->stream));
-    for (int i = 0; i < n; ++i) readback_guard(targets[i]);
+    for (int i = 0; i < n; ++i)
+        if (svo_status gs = readback_guard(targets[i]); gs != SVO_OK) return gs;
     k_reset_counter<<<1, 1, 0, ctx->stream>>>(ctx->d_counter);
     SVO_LAUNCHED(ctx);
     svo_status st = launch_trace_full(ctx, ctx->d_batch[slot]);
