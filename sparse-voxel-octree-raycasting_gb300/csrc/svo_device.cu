@@ -600,6 +600,11 @@ svo_status launch_net_infer(svo_context* ctx, const svo_net* net, bool pipeline,
 // a ray request for every pixel below the threshold), then the tracer over
 // the requests and the refresh tile. Nothing is filtered or copied: the
 // current plane keeps reprojected and traced pixels and becomes the cache.
+// Guided frames: k_project -> k_guide<true> (the gather, start distances,
+// walk lists) -> the net on the listed tiles (it appends its requests) ->
+// the tracer (requests, refresh tile, walks); these four launches use
+// programmatic stream serialisation, each waiting (griddepcontrol.wait)
+// before it reads what the one before wrote.
 svo_status enqueue_learned_body(svo_context* ctx, svo_target* t, const svo_net* net, float logit_threshold) {
     cudaStream_t s = ctx->stream;
     const int res_x = t->res_x, res_y = t->res_y;
