@@ -1037,24 +1037,29 @@ svo_status svo_measure_read_bandwidth(svo_context* ctx, const void* d_buf, size_
     if (!ctx || !d_buf || !gbs || bytes < 16 || passes < 1 || (reinterpret_cast<uintptr_t>(d_buf) & 15u))
         return SVO_ERR_INVALID_ARGUMENT;
     const int sms = ctx->sm_count;
-    cudaEvent_t e0, e1;
-    SVO_CUDA(ctx, cudaEventCreate(&e0));
-    SVO_CUDA(ctx, cudaEventCreate(&e1));
+    struct Events {  // released on every return path
+        cudaEvent_t e[2] = {nullptr, nullptr};
+        ~Events() {
+            for (cudaEvent_t x : e)
+                if (x) cudaEventDestroy(x);
+        }
+    } ev;
+    SVO_CUDA(ctx, cudaEventCreate(&ev.e[0]));
+    SVO_CUDA(ctx, cudaEventCreate(&ev.e[1]));
+    cudaEvent_t e0 = ev.e[0], e1 = ev.e[1];
     const size_t n16 = bytes / 16;
     const dim3 grid((unsigned)(sms * 4)), block(512);
     // one untimed launch warms the buffer into L2 (when it fits there)
     k_read_probe<<<grid, block, 0, ctx->stream>>>(static_cast<const uint4*>(d_buf), n16, 1, ctx->d_fault + 1);
     SVO_LAUNCHED(ctx);
-    cudaEventRecord(e0, ctx->stream);
+    SVO_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
     k_read_probe<<<grid, block, 0, ctx->stream>>>(static_cast<const uint4*>(d_buf), n16, passes, ctx->d_fault + 1);
     SVO_LAUNCHED(ctx);
-    cudaEventRecord(e1, ctx->stream);
+    SVO_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
     svo_status st = SVO_OK;
     if (cudaEventSynchronize(e1) != cudaSuccess) st = fail(ctx, SVO_ERR_CUDA, "read probe");
     float ms = 0.0f;
     if (st == SVO_OK && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) st = fail(ctx, SVO_ERR_CUDA, "read probe events");
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
     if (st == SVO_OK) *gbs = (double)(n16 * 16) * passes / ((double)ms * 1e-3) / 1e9;
     return st;
 }
