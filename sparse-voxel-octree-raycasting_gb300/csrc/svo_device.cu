@@ -2038,11 +2038,9 @@ svo_status svo_read_bgrx_async(svo_target* t, uint32_t* host) {
     if (!t || !host) return SVO_ERR_INVALID_ARGUMENT;
     svo_context* ctx = t->ctx;
     SVO_CUDA(ctx, cudaSetDevice(ctx->device));
-    if (!t->copy_stream) {
-        SVO_CUDA(ctx, cudaStreamCreateWithFlags(&t->copy_stream, cudaStreamNonBlocking));
-        SVO_CUDA(ctx, cudaEventCreateWithFlags(&t->frame_done, cudaEventDisableTiming));
-        SVO_CUDA(ctx, cudaEventCreateWithFlags(&t->copy_done, cudaEventDisableTiming));
-    }
+    if (!t->copy_stream) SVO_CUDA(ctx, cudaStreamCreateWithFlags(&t->copy_stream, cudaStreamNonBlocking));
+    if (!t->frame_done) SVO_CUDA(ctx, cudaEventCreateWithFlags(&t->frame_done, cudaEventDisableTiming));
+    if (!t->copy_done) SVO_CUDA(ctx, cudaEventCreateWithFlags(&t->copy_done, cudaEventDisableTiming));
     // the next frame's graph gains the wait on this copy (captured once)
     t->async_readback = true;
     SVO_CUDA(ctx, cudaEventRecord(t->frame_done, ctx->stream));
