@@ -347,7 +347,7 @@ svo_status plan_trace(svo_context* ctx, int kind, TraceLaunch& L) {
     }
     L.fn = L.block == 1024 ? trace_fn_depth<1024>(ctx->depth, kind) : trace_fn_depth<256>(ctx->depth, kind);
     if (!L.fn) return fail(ctx, SVO_ERR_NOT_SUPPORTED, "octree depth");
-    L.smem = (size_t)(ctx->depth + 1) * L.block * 4u + stage_bytes;
+    L.smem = (size_t)(ctx->depth + 2) * L.block * 4u + stage_bytes;  // stack: kStackLevels
     SVO_CUDA(ctx, cudaFuncSetAttribute(L.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smem));
     return SVO_OK;
 }
@@ -2262,7 +2262,7 @@ extern "C" svo_status svo_raycast_full_noalloc(const uint32_t* d_words, size_t n
     }
     const int block = stage_bytes > 48u * 1024u ? 1024 : 256;
     const void* fn = block == 1024 ? noalloc_kernel<1024>(depth) : noalloc_kernel<256>(depth);
-    const size_t smem = (size_t)(depth + 1) * block * 4u + stage_bytes;
+    const size_t smem = (size_t)(depth + 2) * block * 4u + stage_bytes;  // stack: kStackLevels
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
         return SVO_ERR_CUDA;
     int per_sm = 0, sms = 0;

@@ -400,9 +400,10 @@ __global__ void __launch_bounds__(256) k_hole_write(TargetBuffers B) {
 // latency per fetch.
 template <int DEPTH, int BLOCK>
 __device__ __forceinline__ Octree stage_octree(Octree o, uint64_t* mbar, uint32_t& fault, bool& staged) {
+    stack_init<DEPTH>(svo_dsmem + threadIdx.x, BLOCK, o.root);
     staged = false;
     if (o.n_smem > 0) {
-        o.smem_base = (DEPTH + 1) * BLOCK;
+        o.smem_base = kStackLevels<DEPTH> * BLOCK;
         staged = stage_prefix(o.words, o.n_smem, o.smem_base, mbar, fault);
         if (!staged) o.n_smem = 0;
     }

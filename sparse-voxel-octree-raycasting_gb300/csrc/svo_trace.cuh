@@ -150,6 +150,19 @@ __device__ __forceinline__ bool stage_prefix(const uint32_t* src, uint32_t n, ui
 // the copy still in flight so it never lands in released shared memory.
 __device__ __forceinline__ void stage_drain(uint64_t* mbar) { (void)mbar_wait_bounded(smem_addr(mbar)); }
 
+// Levels of the per-thread node stack: the walk's levels 0..DEPTH-1 and the
+// root twice above them (read by a pop to the top level and by the colour
+// fetch of a ray that never descended).
+template <int DEPTH>
+constexpr int kStackLevels = DEPTH + 2;
+// Writes the root into this thread's stack column at levels DEPTH and
+// DEPTH + 1; a kernel calls it once, before its first walk.
+template <int DEPTH>
+__device__ __forceinline__ void stack_init(uint32_t* stk, int stride, uint32_t root) {
+    stk[DEPTH * stride] = root;
+    stk[(DEPTH + 1) * stride] = root;
+}
+
 __device__ __forceinline__ uint32_t popc8(uint32_t v) { return __popc(v & 0xffu); }
 
 // fetchColor (kernel.cl:64-112).
@@ -181,32 +194,34 @@ __device__ __forceinline__ uint32_t fetch_colour(const Octree& o, uint32_t node,
     return load_word(o, n + nadd, fault);
 }
 
-// Exact int<->float conversions on the FMA pipe for values in [0, 2^23):
-// float(v) = (2^23 + v as bits) - 2^23, and trunc(x) = bits(x + 2^23 rounded
-// toward zero) - bits(2^23). They replace the I2F/F2I instructions of the
-// stepping loop, which run on a narrow pipe and throttled the trace kernel.
-__device__ __forceinline__ float u23_to_float(int v) {
-    return __fsub_rn(__int_as_float(0x4B000000 | v), 8388608.0f);
-}
-__device__ __forceinline__ int trunc_u23(float x) {
-    return __float_as_int(__fadd_rz(x, 8388608.0f)) - 0x4B000000;
-}
+// Cell coordinates of the walk. On the fast path (coordinates in [0, 2^23))
+// a coordinate is carried biased, as the float bits of 2^23 + trunc(x):
+// bits(x + 2^23 rounded toward zero) = 0x4B000000 | trunc(x). The low 23 bits
+// are the integer itself, so bit tests, the XOR of two coordinates and the
+// next cell boundary need no conversion back, and the I2F/F2I instructions
+// (a narrow pipe, which throttled the stepping loop) are FMA-pipe adds.
 template <bool kFast>
-__device__ __forceinline__ float int_to_float(int v) {
-    return kFast ? u23_to_float(v) : (float)v;
-}
-// The next cell boundary above coordinate r at level rek, as a float:
-// ((r >> rek) + 1) << rek = (r | (2^rek - 1)) + 1, whose float bits on the
-// fast path are (r | mask) + bits(2^23) + 1 (no carry past bit 23 for
-// r < 2^23; a sum of exactly 2^23 gives bits(2^24), also exact).
+constexpr int kCellBias = kFast ? 0x4B000000 : 0;
 template <bool kFast>
-__device__ __forceinline__ float next_boundary(int r, int rek) {
-    if (kFast) return __fsub_rn(__int_as_float((r | ((1 << rek) - 1)) + 0x4B000001), 8388608.0f);
-    return (float)(((r >> rek) + 1) << rek);
+__device__ __forceinline__ int float_to_cell(float x) {
+    return kFast ? __float_as_int(__fadd_rz(x, 8388608.0f)) : __float2int_rz(x);
 }
+// (1 << n) - 1 in one instruction.
+__device__ __forceinline__ uint32_t low_mask(int n) {
+    uint32_t m;
+    asm("bmsk.clamp.b32 %0, 0, %1;" : "=r"(m) : "r"(n));
+    return m;
+}
+// The next cell boundary above coordinate r at level rek, as a float, given
+// mask = 2^rek - 1: ((r >> rek) + 1) << rek = (r | mask) + 1. On the fast
+// path r is biased and (r | mask) + 1 are the float bits of 2^23 plus that
+// boundary (no carry past bit 23 for a boundary below 2^23; a boundary of
+// exactly 2^23 gives bits(2^24), also exact), so one subtraction of 2^23
+// gives it.
 template <bool kFast>
-__device__ __forceinline__ int float_to_int(float x) {
-    return kFast ? trunc_u23(x) : __float2int_rz(x);
+__device__ __forceinline__ float next_boundary(int r, uint32_t mask) {
+    if (kFast) return __fsub_rn(__int_as_float((int)(((uint32_t)r | mask) + 1u)), 8388608.0f);
+    return (float)(int)(((uint32_t)r | mask) + 1u);
 }
 
 struct Walk {
@@ -237,11 +252,17 @@ __device__ __forceinline__ uint32_t load_word_sel(const Octree& o, uint32_t i, u
 //     flight; block-node addressing uses selects instead of nested branches;
 //   * the descent loop needs no step cap (rek strictly decreases); the view
 //     distance and y-exit tests share one branch.
+//   * the stack holds the root at levels DEPTH and DEPTH + 1 (written once
+//     per thread by the kernel), so a pop reads its node and its parent
+//     without testing for the root;
+//   * the step cap shares the exit branch (a capped walk has done one more
+//     step when it stops; its result is discarded with the fault flag).
 // The state changes are those of the reference loop, in the same order.
 // kFast: every coordinate of the walk stays in [0, 2^23), checked by the
 // caller from the mirrored start point (each step moves a coordinate by at
 // most the distance it adds, and the walk stops once the distance passes
-// VIEW_DIST_MAX).
+// VIEW_DIST_MAX); the cell coordinates are then carried biased
+// (float_to_cell).
 template <int DEPTH, bool kFast>
 __device__ __forceinline__ void walk(const Octree& o, Walk& w, uint32_t sxyz, float g0y, float g0z, float g1x,
                                      float g1z, float g2x, float g2y, float lx, float ly, float lz, float lodswitch,
@@ -249,7 +270,7 @@ __device__ __forceinline__ void walk(const Octree& o, Walk& w, uint32_t sxyz, fl
     constexpr int kDepthAnd = (1 << DEPTH) - 1;
     constexpr int kTopBit = 2 * kDepthAnd + 2;
     float rpx = w.rpx, rpy = w.rpy, rpz = w.rpz;
-    int rix = float_to_int<kFast>(rpx), riy = float_to_int<kFast>(rpy), riz = float_to_int<kFast>(rpz);
+    int rix = float_to_cell<kFast>(rpx), riy = float_to_cell<kFast>(rpy), riz = float_to_cell<kFast>(rpz);
     int rek = DEPTH;
     float distance = w.distance;
     const uint32_t root = o.root;
@@ -294,18 +315,16 @@ __device__ __forceinline__ void walk(const Octree& o, Walk& w, uint32_t sxyz, fl
         }
         if (hit) {
             w.hit = true;
-            w.hcx = rix >> rek;
-            w.hcy = riy >> rek;
-            w.hcz = riz >> rek;
+            w.hcx = (rix - kCellBias<kFast>) >> rek;
+            w.hcy = (riy - kCellBias<kFast>) >> rek;
+            w.hcz = (riz - kCellBias<kFast>) >> rek;
             break;
         }
-        if (++steps > kStepCap) {
-            fault |= kFaultSteps;
-            break;
-        }
-        const float m0x = __fsub_rn(next_boundary<kFast>(rix, rek), rpx);
-        const float m0y = __fsub_rn(next_boundary<kFast>(riy, rek), rpy);
-        const float m0z = __fsub_rn(next_boundary<kFast>(riz, rek), rpz);
+        ++steps;
+        const uint32_t mask = low_mask(rek);
+        const float m0x = __fsub_rn(next_boundary<kFast>(rix, mask), rpx);
+        const float m0y = __fsub_rn(next_boundary<kFast>(riy, mask), rpy);
+        const float m0z = __fsub_rn(next_boundary<kFast>(riz, mask), rpz);
         float best = __fmul_rn(m0x, lx);
         const float idy_ = __fmul_rn(m0y, ly), idz_ = __fmul_rn(m0z, lz);
         float mm = m0x, gx = 1.0f, gy = g0y, gz = g0z;
@@ -315,28 +334,26 @@ __device__ __forceinline__ void walk(const Octree& o, Walk& w, uint32_t sxyz, fl
         rpy = __fadd_rn(rpy, __fmul_rn(gy, mm));
         rpz = __fadd_rn(rpz, __fmul_rn(gz, mm));
         const int bx = rix, by = riy, bz = riz;
-        rix = float_to_int<kFast>(rpx);
-        riy = float_to_int<kFast>(rpy);
-        riz = float_to_int<kFast>(rpz);
+        rix = float_to_cell<kFast>(rpx);
+        riy = float_to_cell<kFast>(rpy);
+        riz = float_to_cell<kFast>(rpz);
         distance = __fadd_rn(distance, best);
         const int x0ry = by ^ riy;
         const uint32_t x0r = (uint32_t)(((bx ^ rix) ^ x0ry ^ (bz ^ riz)) & kDepthAnd);
         const bool far = distance > kViewDistMax;
         if (!far && (x0r >> rek)) {
-            rek = 32 - __clz(x0r);
-            const bool at_root = rek >= DEPTH;
-            const uint32_t s0 = at_root ? root : stk[rek * stride];
-            const uint32_t s1 = (rek + 1 >= DEPTH) ? root : stk[(rek + 1) * stride];
-            nodeid = s0;
-            nodeid_before = at_root ? root : s1;
+            rek = 32 - __clz(x0r);  // <= DEPTH: x0r has DEPTH bits
+            nodeid = stk[rek * stride];
+            nodeid_before = stk[(rek + 1) * stride];
             if (distance > lodswitch) {
                 lodswitch = __fmul_rn(lodswitch, 2.0f);
                 ++lod;
             }
         }
-        if (far || (x0ry & kTopBit)) break;
+        if (far || (x0ry & kTopBit) || steps > kStepCap) break;
         ni = child_index(rek);
     }
+    if (steps > kStepCap) fault |= kFaultSteps;
     w.rpx = rpx;
     w.rpy = rpy;
     w.rpz = rpz;
@@ -350,7 +367,8 @@ __device__ __forceinline__ void walk(const Octree& o, Walk& w, uint32_t sxyz, fl
 
 // Ray setup of raycast_fine_2/raycast_holes (kernel.cl:883-899) + CAST_RAY +
 // the colour fetch. `stk` points at this thread's column of the shared stack
-// (entry for level L at stk[L * stride]); levels 1..DEPTH-1 are used.
+// (entry for level L at stk[L * stride]); the walk writes levels 0..DEPTH-1,
+// levels DEPTH and DEPTH + 1 hold the root (stack_init).
 //
 // kGuided with s0 > 0: the walk starts s0 (raypos units, 16 per world unit)
 // along the ray instead of at the camera -- but at most up to
@@ -437,7 +455,7 @@ __device__ __forceinline__ RayResult trace_ray(const Octree& o, const RayCam& c,
     if (sxyz & 1u) rpx = __fsub_rn(fscale, rpx);
     if (sxyz & 2u) rpy = __fsub_rn(fscale, rpy);
     if (sxyz & 4u) rpz = __fsub_rn(fscale, rpz);
-    const uint32_t before2 = (rek + 1 >= DEPTH) ? o.root : stk[(rek + 1) * stride];
+    const uint32_t before2 = stk[(rek + 1) * stride];
     const uint32_t col = fetch_colour(o, w.nodeid, w.nodeid_before, before2, w.local_root, rek, w.node_test, fault);
 
     RayResult r;
