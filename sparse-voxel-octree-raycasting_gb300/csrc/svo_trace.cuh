@@ -276,9 +276,13 @@ __device__ __forceinline__ void walk(const Octree& o, Walk& w, uint32_t sxyz, fl
     const uint32_t root = o.root;
     uint32_t nodeid = root, nodeid_before = root, local_root = 0, node_test = 0;
     uint32_t steps = 0;
+    // y and z pre-shifted by 1 and 2, so the child index at level r is three
+    // shifts and a bit merge: bit 0 from x >> r, bit 1 from y2 >> r, bit 2
+    // from z4 >> r.
+    uint32_t ry2 = (uint32_t)riy << 1, rz4 = (uint32_t)riz << 2;
     auto child_index = [&](int r) -> uint32_t {
-        return ((uint32_t)((rix >> r) & 1) | ((uint32_t)((riy >> r) & 1) << 1) | ((uint32_t)((riz >> r) & 1) << 2)) ^
-               sxyz;
+        const uint32_t a = (uint32_t)rix >> r, b = ry2 >> r, c = rz4 >> r;
+        return ((((a & 1u) | (b & ~1u)) & 3u) | (c & 4u)) ^ sxyz;
     };
     uint32_t ni = child_index(rek);
     for (;;) {
@@ -337,11 +341,13 @@ __device__ __forceinline__ void walk(const Octree& o, Walk& w, uint32_t sxyz, fl
         rix = float_to_cell<kFast>(rpx);
         riy = float_to_cell<kFast>(rpy);
         riz = float_to_cell<kFast>(rpz);
+        ry2 = (uint32_t)riy << 1;
+        rz4 = (uint32_t)riz << 2;
         distance = __fadd_rn(distance, best);
         const int x0ry = by ^ riy;
         const uint32_t x0r = (uint32_t)(((bx ^ rix) ^ x0ry ^ (bz ^ riz)) & kDepthAnd);
         const bool far = distance > kViewDistMax;
-        if (!far && (x0r >> rek)) {
+        if (!far && x0r > mask) {  // x0r >> rek != 0
             rek = 32 - __clz(x0r);  // <= DEPTH: x0r has DEPTH bits
             nodeid = stk[rek * stride];
             nodeid_before = stk[(rek + 1) * stride];
