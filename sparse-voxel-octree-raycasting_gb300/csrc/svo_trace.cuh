@@ -287,8 +287,12 @@ __device__ __forceinline__ void walk(const Octree& o, Walk& w, uint32_t sxyz, fl
     uint32_t ni = child_index(rek);
     for (;;) {
         node_test = nodeid & (1u << ni);
+        // One exit test per descent: the level-of-detail test of a descent is
+        // taken after the next level's child index, stack entry and bit test
+        // have been computed; a hit then restores the level and the bit test
+        // (the stack entry one level below the hit is never read).
         bool hit = false;
-        while (node_test) {
+        while (node_test && !hit) {
             const uint32_t parent = nodeid;
             const uint32_t n = nodeid >> 9;
             if (!(nodeid & 256u)) {
@@ -308,16 +312,15 @@ __device__ __forceinline__ void walk(const Octree& o, Walk& w, uint32_t sxyz, fl
                 }
             }
             nodeid_before = parent;
-            if (rek <= lod) {
-                hit = true;
-                break;
-            }
+            hit = rek <= lod;
             --rek;
             ni = child_index(rek);
             stk[rek * stride] = nodeid;
             node_test = nodeid & (1u << ni);
         }
         if (hit) {
+            ++rek;
+            node_test = nodeid_before & (1u << child_index(rek));
             w.hit = true;
             w.hcx = (rix - kCellBias<kFast>) >> rek;
             w.hcy = (riy - kCellBias<kFast>) >> rek;
