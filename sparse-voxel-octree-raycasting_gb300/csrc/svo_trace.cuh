@@ -214,13 +214,12 @@ __device__ __forceinline__ uint32_t low_mask(int n) {
 }
 // The next cell boundary above coordinate r at level rek, as a float, given
 // mask = 2^rek - 1: ((r >> rek) + 1) << rek = (r | mask) + 1. On the fast
-// path r is biased and (r | mask) + 1 are the float bits of 2^23 plus that
-// boundary (no carry past bit 23 for a boundary below 2^23; a boundary of
-// exactly 2^23 gives bits(2^24), also exact), so one subtraction of 2^23
-// gives it.
+// path r is biased, so r | mask are the float bits of 2^23 + v with
+// v = (unbiased r) | mask < 2^23, and adding 1 - 2^23 (exactly
+// representable) gives v + 1 exactly (at most 2^23).
 template <bool kFast>
 __device__ __forceinline__ float next_boundary(int r, uint32_t mask) {
-    if (kFast) return __fsub_rn(__int_as_float((int)(((uint32_t)r | mask) + 1u)), 8388608.0f);
+    if (kFast) return __fadd_rn(__int_as_float((int)((uint32_t)r | mask)), -8388607.0f);
     return (float)(int)(((uint32_t)r | mask) + 1u);
 }
 
