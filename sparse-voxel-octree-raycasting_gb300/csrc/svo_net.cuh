@@ -466,14 +466,16 @@ constexpr int kGuideBW = 32, kGuideBH = 8;  // pixels per block (whole ray packe
 constexpr float kGuideCertified = -2.0f;  // guide value of a certified pixel
 constexpr float kCertifyGap = 2.0f;       // cells
 
+// The walk's lodswitch doublings in closed form: 1 + the smallest k >= 0
+// with s <= sw * 2^k (sw = 2 * res_x), at most 24. For s > sw, with
+// s = ms * 2^es and sw = mw * 2^ew (mantissas in [1, 2)), k = es - ew when
+// ms <= mw, else es - ew + 1; the mantissas compare as their low 23 bits.
 __device__ __forceinline__ int lod_at(float s, int res_x) {
-    float sw = (float)(2 * res_x);
-    int lod = 1;
-    while (s > sw && lod < 24) {  // the walk's lodswitch doublings
-        sw *= 2.0f;
-        ++lod;
-    }
-    return lod;
+    const float sw = (float)(2 * res_x);
+    if (!(s > sw)) return 1;
+    const int bs = __float_as_int(s), bw = __float_as_int(sw);
+    const int k = ((bs >> 23) - (bw >> 23)) + ((bs & 0x7fffff) > (bw & 0x7fffff) ? 1 : 0);
+    return min(1 + k, 24);
 }
 
 // Candidate data of the halo, one array per field (conflict-free reads): the
@@ -734,7 +736,7 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
         if (m < INFINITY) {
             const float s = __fmul_rn(m, 16.0f);  // raypos units
             const int lod = lod_at(s, res_x);
-            const float cell = (float)(1 << lod);
+            const float cell = __int_as_float((127 + lod) << 23);  // 2^lod
             g = holes >= kGuideHoleCount ? __fmul_rn(s, kGuideNearHole)
                                          : fmaxf(__fsub_rn(s, __fmul_rn(kGuideMargin, cell)), 0.0f);
             const bool in_tile = x >= P->add_x && x < P->x_end && y >= P->add_y && y < P->y_end;
@@ -764,9 +766,10 @@ __global__ void __launch_bounds__(kGuideBW * kGuideBH) k_guide(const FrameParams
     {  // warp w appends the pixels of packet w of the block, in packet order;
        // one atomic per list and block (not per warp: 8x fewer on three counters)
         const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        const int ps = P->pw_shift, pw = 1 << ps, ph = 32 >> ps;
-        const int per_row = kGuideBW / pw;
-        const int bx = (w % per_row) * pw + (lane & (pw - 1)), by = (w / per_row) * ph + (lane >> ps);
+        // packets per block row: kGuideBW / pw = 2^rs, packet height ph = 2^rs
+        static_assert(kGuideBW == 32, "packet shapes 2^ps x 2^(5-ps) tile a 32-pixel row");
+        const int ps = P->pw_shift, pw = 1 << ps, rs = 5 - ps;
+        const int bx = ((w & ((1 << rs) - 1)) << ps) + (lane & (pw - 1)), by = ((w >> rs) << rs) + (lane >> ps);
         const int k = kind[by][bx];
         const uint32_t xy = (uint32_t)(x0 + bx) | ((uint32_t)(y0 + by) << 16);
         const uint32_t below = (1u << lane) - 1u;
