@@ -118,10 +118,13 @@ svo_status svo_context_set_option(svo_context* ctx, int option, int64_t value);
 svo_status svo_measure_read_bandwidth(svo_context* ctx, const void* d_buf, size_t bytes, int passes, double* gbs);
 
 /* Autotuner (no reference counterpart): times `repeats` full raycasts of
- * `view` into `t` for every packet shape (4x8, 8x4, 16x2, 32x1), block size
- * (256, 1024) and node staging (on, off), keeps the fastest in the context
- * and returns every measurement (up to cap) in results. Results are
- * identical under every setting; only the speed differs. Synchronises. */
+ * `view` into `t` for every packet shape (8x4 first, then 4x8, 16x2,
+ * 32x1), block size (256, 1024) and node staging (on, off), keeps the
+ * fastest in the context -- a configuration replaces the best one measured
+ * before it only when it is more than 1% faster, so near-ties keep the
+ * earlier one -- and returns every measurement (up to cap) in results.
+ * Results are identical under every setting; only the speed differs.
+ * Synchronises. */
 typedef struct svo_tune_result {
     int packet_w, packet_h, block, stage_nodes;
     float ms;
@@ -132,7 +135,8 @@ svo_status svo_context_autotune(svo_context* ctx, svo_target* t, const svo_view*
  * the n_views (>= 6) views as learned frames 0..n_views-1 into `t` (with the
  * target's guided setting, the net and threshold given) for every packet
  * shape and block size, times frames 4.. with CUDA events, and keeps the
- * fastest as SVO_OPT_LEARNED_PACKET_WIDTH / SVO_OPT_LEARNED_TRACE_BLOCK.
+ * fastest (with the same 1% rule) as SVO_OPT_LEARNED_PACKET_WIDTH /
+ * SVO_OPT_LEARNED_TRACE_BLOCK.
  * results[i].ms = milliseconds per frame. Synchronises. */
 svo_status svo_context_autotune_learned(svo_context* ctx, svo_target* t, const svo_view* views, int n_views,
                                         const svo_net* net, float threshold, svo_tune_result* results, int cap,

@@ -1562,6 +1562,11 @@ svo_status svo_raycast_full(svo_context* ctx, svo_target* t, const svo_view* vie
     return svo_raycast_full_batch(ctx, &t, view, 1);
 }
 
+// The autotuners measure the default packet shape (8x4) first and move to
+// another configuration only when it is faster by more than this margin:
+// configurations within the timing noise of each other keep the default.
+constexpr float kTuneMargin = 0.99f;
+
 svo_status svo_context_autotune(svo_context* ctx, svo_target* t, const svo_view* view, int repeats,
                                 svo_tune_result* results, int cap, int* n_results) {
     if (!ctx || !t || !view || repeats < 1) return SVO_ERR_INVALID_ARGUMENT;
@@ -1571,7 +1576,7 @@ svo_status svo_context_autotune(svo_context* ctx, svo_target* t, const svo_view*
         int pw, block, stage;
     };
     std::vector<Cfg> cfgs;
-    for (int pw : {4, 8, 16, 32})
+    for (int pw : {8, 4, 16, 32})
         for (int stage : {1, 0})
             for (int block : {256, 1024}) cfgs.push_back({pw, block, stage});
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -1599,7 +1604,7 @@ svo_status svo_context_autotune(svo_context* ctx, svo_target* t, const svo_view*
         if (st != SVO_OK) break;
         if (results && k < cap) results[k] = svo_tune_result{c.pw, 32 / c.pw, c.block, c.stage, ms};
         ++k;
-        if (ms < best) {
+        if (ms < best * kTuneMargin) {
             best = ms;
             best_cfg = c;
         }
@@ -1627,7 +1632,7 @@ svo_status svo_context_autotune_learned(svo_context* ctx, svo_target* t, const s
     svo_status st = SVO_OK;
     float best = 1e30f;
     int best_pw = pw0, best_block = block0, k = 0;
-    for (int pw : {4, 8, 16, 32})
+    for (int pw : {8, 4, 16, 32})
         for (int block : {256, 1024}) {
             ctx->learned_pw_shift = pw == 4 ? 2 : pw == 8 ? 3 : pw == 16 ? 4 : 5;
             ctx->learned_block_pref = block;
@@ -1648,7 +1653,7 @@ svo_status svo_context_autotune_learned(svo_context* ctx, svo_target* t, const s
             if (st != SVO_OK) break;
             if (results && k < cap) results[k] = svo_tune_result{pw, 32 / pw, block, ctx->stage_normal ? 1 : 0, ms};
             ++k;
-            if (ms < best) {
+            if (ms < best * kTuneMargin) {
                 best = ms;
                 best_pw = ctx->learned_pw_shift;
                 best_block = block;
