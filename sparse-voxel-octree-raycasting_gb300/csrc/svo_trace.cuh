@@ -350,7 +350,9 @@ __device__ __forceinline__ void walk(const Octree& o, Walk& w, uint32_t sxyz, fl
         const uint32_t x0r = (uint32_t)(((bx ^ rix) ^ x0ry ^ (bz ^ riz)) & kDepthAnd);
         const bool far = distance > kViewDistMax;
         if (!far && x0r > mask) {  // x0r >> rek != 0
-            rek = 32 - __clz(x0r);  // <= DEPTH: x0r has DEPTH bits
+            // top set bit + 1 (<= DEPTH: x0r has DEPTH bits), from the exponent
+            // of float(x0r), exact for x0r < 2^23: shorter latency than clz
+            rek = (__float_as_int(__fsub_rn(__int_as_float((int)(0x4B000000u | x0r)), 8388608.0f)) >> 23) - 126;
             nodeid = stk[rek * stride];
             nodeid_before = stk[(rek + 1) * stride];
             if (distance > lodswitch) {
