@@ -14,9 +14,10 @@
 //     instead of reading outside the allocation);
 //   * the per-ray node stack lives in shared memory as [level][thread], so the
 //     32 lanes of a warp always hit 32 different banks;
-//   * loop state stays in registers; the pop level is a count-leading-zeros
-//     instead of kernel.cl:202's log2 of a float (identical for every input
-//     the walk can produce, pinned by a known-answer test);
+//   * loop state stays in registers; the pop level is the exponent of the
+//     exactly converted XOR mask instead of kernel.cl:202's log2 of a float
+//     (the same top set bit for every input the walk can produce, pinned by
+//     a known-answer test);
 //   * every walk is capped at kStepCap steps (fault flag 2) so no input can
 //     keep a kernel spinning.
 #pragma once
