@@ -554,8 +554,14 @@ svo_status enqueue_warp_body(svo_context* ctx, svo_target* t) {
         SVO_LAUNCHED(ctx);
     }
     record(t, 2);
-    k_hole_scan<<<1, 1024, 0, s>>>(t->B);
-    SVO_LAUNCHED(ctx);
+    {
+        const uint32_t tiles = (uint32_t)t->B.tiles_x * (uint32_t)t->B.tiles_y;
+        const int staged = tiles <= kScanStageTiles ? 1 : 0;
+        const size_t smem = staged ? (size_t)tiles * 8u : 0u;
+        SVO_CUDA(ctx, cudaFuncSetAttribute(k_hole_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_hole_scan<<<1, 1024, smem, s>>>(t->B, staged);
+        SVO_LAUNCHED(ctx);
+    }
     record(t, 3);
     if (t->tiles > 0) {
         k_hole_write<<<(unsigned)((t->tiles + 7) / 8), 256, 0, s>>>(t->B);

@@ -319,13 +319,28 @@ __global__ void __launch_bounds__(256) k_hole_mask(const FrameParams* __restrict
 // host readback: one block scans the tile counts and leaves the total on the
 // device. ids[t] = 4*holes(t) except ids[0] = total; ids[tiles+t] = exclusive
 // offset of tile t.
-__global__ void __launch_bounds__(1024) k_hole_scan(TargetBuffers B) {
+// Tiles whose counts and prefixes the hole scan stages in shared memory
+// (8 bytes per tile; beyond it the scan works on global memory).
+constexpr uint32_t kScanStageTiles = 28u * 1024u;
+
+// staged: the launch gave 8 bytes of dynamic shared memory per tile. The
+// counts are then read and the prefixes written coalesced, and each thread
+// scans its contiguous run of tiles in shared memory: a one-block kernel
+// whose per-thread runs touched global memory 8 tiles apart spent its time
+// in the one SM's scattered loads and stores.
+__global__ void __launch_bounds__(1024) k_hole_scan(TargetBuffers B, int staged) {
     __shared__ uint32_t warp_sums[32];
+    uint32_t* cnt_s = svo_dsmem;  // [tiles] counts, then [tiles] exclusive prefixes
     const uint32_t tiles = (uint32_t)B.tiles_x * (uint32_t)B.tiles_y;
+    uint32_t* pre_s = svo_dsmem + tiles;
     const uint32_t per = (tiles + blockDim.x - 1) / blockDim.x;
     const uint32_t a = threadIdx.x * per, b = min(a + per, tiles);
+    if (staged) {
+        for (uint32_t t = threadIdx.x; t < tiles; t += blockDim.x) cnt_s[t] = 4u * (uint32_t)__popcll(B.tile_mask[t]);
+        __syncthreads();
+    }
     uint32_t local = 0;
-    for (uint32_t t = a; t < b; ++t) local += 4u * (uint32_t)__popcll(B.tile_mask[t]);
+    for (uint32_t t = a; t < b; ++t) local += staged ? cnt_s[t] : 4u * (uint32_t)__popcll(B.tile_mask[t]);
     // block exclusive scan of `local`
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t incl = local;
@@ -345,11 +360,23 @@ __global__ void __launch_bounds__(1024) k_hole_scan(TargetBuffers B) {
     }
     __syncthreads();
     uint32_t acc = incl - local + (warp > 0 ? warp_sums[warp - 1] : 0u);
-    for (uint32_t t = a; t < b; ++t) {
-        const uint32_t cnt = 4u * (uint32_t)__popcll(B.tile_mask[t]);
-        B.ids[tiles + t] = acc;
-        if (t > 0) B.ids[t] = cnt;
-        acc += cnt;
+    if (staged) {
+        for (uint32_t t = a; t < b; ++t) {
+            pre_s[t] = acc;
+            acc += cnt_s[t];
+        }
+        __syncthreads();
+        for (uint32_t t = threadIdx.x; t < tiles; t += blockDim.x) {
+            B.ids[tiles + t] = pre_s[t];
+            if (t > 0) B.ids[t] = cnt_s[t];
+        }
+    } else {
+        for (uint32_t t = a; t < b; ++t) {
+            const uint32_t cnt = 4u * (uint32_t)__popcll(B.tile_mask[t]);
+            B.ids[tiles + t] = acc;
+            if (t > 0) B.ids[t] = cnt;
+            acc += cnt;
+        }
     }
     if (threadIdx.x == blockDim.x - 1) {
         const uint32_t total = warp_sums[(blockDim.x >> 5) - 1];
