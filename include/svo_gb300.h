@@ -87,6 +87,9 @@ svo_status svo_synchronize(svo_context* ctx);
 uint64_t svo_launch_count(const svo_context* ctx);
 
 /* Tuning switches of the trace kernels (no counterpart in the reference).
+ * SVO_OPT_STAGE_NODES, SVO_OPT_PACKET_WIDTH and SVO_OPT_TRACE_BLOCK configure
+ * the tracer of full raycasts and of plain warp frames; svo_context_autotune
+ * overrides them for full raycasts only, until one of the three is set again.
  * SVO_OPT_STAGE_NODES: 1 (default) copies the octree's normal-node region into
  * each trace block's shared memory (when it fits, <= 160 KiB); 0 reads every
  * node word from global memory. */
@@ -120,11 +123,12 @@ svo_status svo_measure_read_bandwidth(svo_context* ctx, const void* d_buf, size_
 /* Autotuner (no reference counterpart): times `repeats` full raycasts of
  * `view` into `t` for every packet shape (8x4 first, then 4x8, 16x2,
  * 32x1), block size (256, 1024) and node staging (on, off), keeps the
- * fastest in the context -- a configuration replaces the best one measured
- * before it only when it is more than 1% faster, so near-ties keep the
- * earlier one -- and returns every measurement (up to cap) in results.
- * Results are identical under every setting; only the speed differs.
- * Synchronises. */
+ * fastest in the context for full raycasts -- a configuration replaces the
+ * best one measured before it only when it is more than 1% faster, so
+ * near-ties keep the earlier one; warp frames keep the options' settings,
+ * which suit their shorter, hole- and tile-bound launches -- and returns
+ * every measurement (up to cap) in results. Results are identical under
+ * every setting; only the speed differs. Synchronises. */
 typedef struct svo_tune_result {
     int packet_w, packet_h, block, stage_nodes;
     float ms;

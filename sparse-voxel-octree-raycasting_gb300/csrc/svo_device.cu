@@ -50,6 +50,9 @@ struct svo_context {
     int block_pref = 0;                     // trace block size, 0: chosen by the staging size
     int learned_block_pref = 0;             // the same for learned frames' tracer
     int learned_pw_shift = -1;              // learned frames' ray packets; -1: as pw_shift
+    // svo_context_autotune's choice for full raycasts only (-1: as the three
+    // options above, which warp frames always follow)
+    int full_pw_shift = -1, full_block_pref = -1, full_stage = -1;
     uint64_t config_gen = 0;                // bumped by every option change (captured graphs re-capture)
     uint64_t launches = 0;
     std::vector<svo_target*> targets;  // live targets, destroyed with the context
@@ -326,10 +329,15 @@ const void* trace_fn_depth(int depth, int kind) {
     return nullptr;
 }
 
+// Packet shape of full raycasts: the autotuner's choice, else the option.
+int full_pw_shift(const svo_context* ctx) { return ctx->full_pw_shift >= 0 ? ctx->full_pw_shift : ctx->pw_shift; }
+
 svo_status plan_trace(svo_context* ctx, int kind, TraceLaunch& L) {
     L.o = Octree{ctx->d_octree, (uint32_t)ctx->n_words, ctx->root, 0u, 0u};
     uint32_t stage_bytes = 0;
-    if (ctx->stage_normal && !(ctx->root & 256u) && (reinterpret_cast<uintptr_t>(ctx->d_octree) & 15u) == 0) {
+    const bool full = kind == kTraceFull;
+    const bool stage = full && ctx->full_stage >= 0 ? ctx->full_stage != 0 : ctx->stage_normal;
+    if (stage && !(ctx->root & 256u) && (reinterpret_cast<uintptr_t>(ctx->d_octree) & 15u) == 0) {
         const uint64_t nw = (uint64_t)(ctx->root >> 9) + 10u;
         const uint64_t bytes = (nw * 4u + 15u) & ~15ull;
         if (bytes <= kStageMaxBytes && bytes <= (uint64_t)ctx->n_words * 4u) {
@@ -337,7 +345,9 @@ svo_status plan_trace(svo_context* ctx, int kind, TraceLaunch& L) {
             stage_bytes = (uint32_t)bytes;
         }
     }
-    const int pref = kind == kTraceWarpBgrx ? ctx->learned_block_pref : ctx->block_pref;
+    const int pref = kind == kTraceWarpBgrx                ? ctx->learned_block_pref
+                     : full && ctx->full_block_pref >= 0 ? ctx->full_block_pref
+                                                         : ctx->block_pref;
     L.block = stage_bytes > kStageSmallBytes ? 1024 : 256;
     if (pref == 1024) L.block = 1024;
     if (pref == 256 && L.block == 1024) {  // the staged region does not fit a 256-thread block
@@ -992,16 +1002,19 @@ svo_status svo_context_set_option(svo_context* ctx, int option, int64_t value) {
     switch (option) {
         case SVO_OPT_STAGE_NODES:
             ctx->stage_normal = value != 0;
+            ctx->full_pw_shift = ctx->full_block_pref = ctx->full_stage = -1;  // an explicit choice wins
             return SVO_OK;
         case SVO_OPT_PACKET_WIDTH:
             if (value != 4 && value != 8 && value != 16 && value != 32)
                 return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "packet width 4, 8, 16 or 32");
             ctx->pw_shift = value == 4 ? 2 : value == 8 ? 3 : value == 16 ? 4 : 5;
+            ctx->full_pw_shift = ctx->full_block_pref = ctx->full_stage = -1;
             return SVO_OK;
         case SVO_OPT_TRACE_BLOCK:
             if (value != 0 && value != 256 && value != 1024)
                 return fail(ctx, SVO_ERR_INVALID_ARGUMENT, "trace block 0 (auto), 256 or 1024");
             ctx->block_pref = (int)value;
+            ctx->full_pw_shift = ctx->full_block_pref = ctx->full_stage = -1;
             return SVO_OK;
         case SVO_OPT_LEARNED_TRACE_BLOCK:
             if (value != 0 && value != 256 && value != 1024)
@@ -1516,7 +1529,7 @@ svo_status svo_raycast_full_batch(svo_context* ctx, svo_target* const* targets, 
     // The slot's previous copy must have left the staging buffer.
     SVO_CUDA(ctx, cudaEventSynchronize(ctx->batch_done[slot]));
     {  // the packet numbers of the whole batch must fit the 32-bit work counter
-        const int pw = 1 << ctx->pw_shift, ph = 32 >> ctx->pw_shift;
+        const int pw = 1 << full_pw_shift(ctx), ph = 32 >> full_pw_shift(ctx);
         uint64_t total = 0;
         for (int i = 0; i < n; ++i)
             total += (uint64_t)((views[i].res_x + pw - 1) / pw) * (uint64_t)((views[i].res_y + ph - 1) / ph);
@@ -1531,8 +1544,8 @@ svo_status svo_raycast_full_batch(svo_context* ctx, svo_target* const* targets, 
         fv.ray = make_raycam(v);
         fv.res_x = v.res_x;
         fv.res_y = v.res_y;
-        const int pw = 1 << ctx->pw_shift, ph = 32 >> ctx->pw_shift;
-        fv.pw_shift = ctx->pw_shift;
+        const int pw = 1 << full_pw_shift(ctx), ph = 32 >> full_pw_shift(ctx);
+        fv.pw_shift = full_pw_shift(ctx);
         fv.packets_x = (v.res_x + pw - 1) / pw;
         fv.packet_begin = packets;
         packets += (uint32_t)fv.packets_x * (uint32_t)((v.res_y + ph - 1) / ph);
@@ -1588,15 +1601,16 @@ svo_status svo_context_autotune(svo_context* ctx, svo_target* t, const svo_view*
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     SVO_CUDA(ctx, cudaEventCreate(&e0));
     SVO_CUDA(ctx, cudaEventCreate(&e1));
-    const bool stage0 = ctx->stage_normal;
-    const int pw0 = ctx->pw_shift, block0 = ctx->block_pref;
+    // The candidates and the choice are full-raycast overrides: warp frames
+    // keep the options' configuration.
+    const int fpw0 = ctx->full_pw_shift, fblock0 = ctx->full_block_pref, fstage0 = ctx->full_stage;
     float best = 1e30f;
-    Cfg best_cfg{1 << pw0, block0, stage0 ? 1 : 0};
+    Cfg best_cfg{-1, -1, -1};
     int k = 0;
     for (const Cfg& c : cfgs) {
-        ctx->pw_shift = c.pw == 4 ? 2 : c.pw == 8 ? 3 : c.pw == 16 ? 4 : 5;
-        ctx->block_pref = c.block;
-        ctx->stage_normal = c.stage != 0;
+        ctx->full_pw_shift = c.pw == 4 ? 2 : c.pw == 8 ? 3 : c.pw == 16 ? 4 : 5;
+        ctx->full_block_pref = c.block;
+        ctx->full_stage = c.stage;
         st = svo_raycast_full(ctx, t, view);  // warm-up
         float ms = 0.0f;
         if (st == SVO_OK && cudaEventRecord(e0, ctx->stream) == cudaSuccess) {
@@ -1617,9 +1631,15 @@ svo_status svo_context_autotune(svo_context* ctx, svo_target* t, const svo_view*
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    ctx->pw_shift = best_cfg.pw == 4 ? 2 : best_cfg.pw == 8 ? 3 : best_cfg.pw == 16 ? 4 : best_cfg.pw == 32 ? 5 : pw0;
-    ctx->block_pref = best_cfg.block;
-    ctx->stage_normal = best_cfg.stage != 0;
+    if (best_cfg.pw > 0) {
+        ctx->full_pw_shift = best_cfg.pw == 4 ? 2 : best_cfg.pw == 8 ? 3 : best_cfg.pw == 16 ? 4 : 5;
+        ctx->full_block_pref = best_cfg.block;
+        ctx->full_stage = best_cfg.stage;
+    } else {  // nothing measured: keep what was there
+        ctx->full_pw_shift = fpw0;
+        ctx->full_block_pref = fblock0;
+        ctx->full_stage = fstage0;
+    }
     ++ctx->config_gen;
     if (n_results) *n_results = k;
     return st;
