@@ -43,6 +43,30 @@ def test_full_raycast_bit_exact(svo, orc, scene, gpu_ctx, depth, shell, kind, W,
     tgt.close()
 
 
+@pytest.mark.parametrize("dx,dz", [(262244.3, 0.0), (-2000.6, -5000.3), (0.0, 300000.7), (400000.0, -310000.0)])
+def test_full_raycast_far_camera_bit_exact(svo, orc, scene, gpu_ctx, dx, dz):
+    """Cameras far out in the periodic terrain: rays whose mirrored start point
+    lies outside [0, 2^22) raypos units (x or z beyond 262,144 world units, or
+    negative) walk with the I2F/F2I conversions instead of the biased
+    FMA-pipe coordinates; every ray still matches the oracle bit for bit."""
+    octree = scene(9, 1234, True)
+    gpu_ctx.upload(octree)
+    W, H = 160, 96
+    tgt = gpu_ctx.target(W, H)
+    view = svo.camera_path(1, 9, 5, W, H)
+    view.pos[0] = view.pos[0] + dx
+    view.pos[2] = view.pos[2] + dz
+    gpu_ctx.raycast_full(tgt, view)
+    gpu_ctx.synchronize()
+    col, xyzw = tgt.full()
+    ocol, oxyzw, ovox, _ = _full_oracle(orc, octree, view)
+    assert (ovox >> np.uint64(63)).astype(bool).sum() > W * H // 2  # mostly terrain, not sky
+    assert np.array_equal(col, ocol), f"{int((col != ocol).sum())} colour words differ"
+    assert np.array_equal(xyzw.view(np.uint32), oxyzw.view(np.uint32)), "hit position/distance bits differ"
+    assert np.array_equal(tgt.voxels(), ovox), "hit voxels differ"
+    tgt.close()
+
+
 @pytest.mark.parametrize("depth,shell,kind,W,H,frames", [
     (8, True, 1, 128, 96, 40),    # covers a whole 8x4 refresh cycle
     (9, True, 2, 200, 120, 12),   # ragged: 200x120 is not a multiple of 16
