@@ -1182,7 +1182,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> None:
             "multiview": multiview,
             "autotune": {"chosen": tuned, "default_8x4_ms": next((r["ms"] for r in tune if r["packet_w"] == 8 and
                                                                  r["stage_nodes"] == 1 and r["block"] == 256), None),
-                         "candidates": len(tune)} if tune else None,
+                         "candidates": len(tune), "applies_to": "full raycasts (warp frames keep the options)"}
+            if tune else None,
             "autotune_learned": {"chosen": tuned_l, "ms_per_frame": {f'{r["packet_w"]}x{r["packet_h"]}/{r["block"]}':
                                                                     round(r["ms"], 4) for r in tune_l}}
                                 if tune_l else None,
