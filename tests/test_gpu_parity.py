@@ -97,6 +97,30 @@ def test_warp_frames_bit_exact(svo, orc, scene, gpu_ctx, depth, shell, kind, W, 
     tgt.close()
 
 
+def test_warp_frames_past_the_staged_scan_bit_exact(svo, orc, scene, gpu_ctx):
+    """4096x1808 has 256 x 113 = 28,928 hole tiles, more than the hole scan
+    stages in shared memory (28,672): it scans in global memory. Frames 0-1
+    list every pixel as a hole, frames 2-3 warp; the hole count, the hole id
+    buffer, the cache plane and the BGRX image match the oracle's."""
+    depth, W, H = 8, 4096, 1808
+    assert (W // 16) * (H // 16) > 28 * 1024
+    octree = scene(depth, 99, True)
+    gpu_ctx.upload(octree)
+    tgt = gpu_ctx.target(W, H)
+    warp = orc.Warp(depth, W, H)
+    for f in range(4):
+        v = svo.camera_path(1, depth, f, W, H)
+        gpu_ctx.warp_frame(tgt, v, f)
+        warp.frame(octree.words, octree.root, v.pos_array, v.m_array, f)
+        gpu_ctx.synchronize()
+        ids, count = tgt.holes()
+        assert count == warp.hole_count(), f"frame {f}: hole count"
+        assert np.array_equal(ids, warp.ids()), f"frame {f}: hole id buffer"
+        assert np.array_equal(tgt.colour(2), warp.screen()[2]), f"frame {f}: cache plane"
+        assert np.array_equal(tgt.bgrx(), warp.tex()), f"frame {f}: BGRX"
+    tgt.close()
+
+
 @pytest.mark.parametrize("depth,kind,W,H,frames", [(9, 2, 160, 96, 40), (8, 1, 128, 64, 36)])
 def test_warp_frames_alternating_cache_bit_exact(svo, orc, scene, gpu_ctx, depth, kind, W, H, frames):
     # raycast.h:395's commented-out copy target ((frame>>4)%2)+1: both cache
